@@ -1,0 +1,437 @@
+#!/usr/bin/env python3
+"""Fast-winding-number benchmark (one JSON line on rank 0).
+
+Workload (default): displaced geodesic icosphere, frequency 316 (1,997,120 triangles, seed 1),
+10M queries (5M uniform in bbox*1.2, 5M on the surface offset by +-U(1e-6, 1e-3)), beta = 2.
+A step = one winding-number query pass over the 10M points against the built tree.
+
+  value      queries/s of the mixed-precision engine with inputs resident in HBM (device time,
+             CUDA events on the launching stream, L2 flushed before every step)
+  e2e        the same metric through the C ABI's host-buffer call fwn_query_host (pinned host
+             buffers; H2D of the points and D2H of Omega + inside inside the timed region)
+  plain_fp64 the plain FP64 form (FP64 everywhere, same tree), its queries/s and the max / RMS
+             |dw| between the two forms over all queries (gate: <= 1e-4)
+  roofline   FP32-issue roofline of the traversal kernel from device work counters
+  cpu_baseline  the CPU restatement of the reference path (oracle O2) on the host cores
+
+``--impl reference`` times the reference path's CPU implementation (the oracle restatement,
+since the reference library cannot be built here) on the same workload and prints the same
+line with ``"impl": "reference"``.
+
+Multi-GPU (torchrun): every rank builds its own replica of the tree and answers its own 10M
+queries (seed offset by rank) — no collective on the data path; value = all ranks' queries /
+the slowest rank's time (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "winding queries/s @2M tris (mixed precision, |dw|<=1e-4 vs plain FP64 GPU form)"
+FOUR_PI = 4.0 * math.pi
+
+# Algorithmic work per unit (constants of the traversal kernel):
+FLOPS_FAR = 82      # order-0/1/2 Taylor term incl. far test and Kahan add (FMA = 2)
+FLOPS_TRI = 95      # Van Oosterom triangle incl. FP64-band test and Kahan add (atan2/sqrt on SFU)
+FLOPS_TEST = 12     # far test of a near node (d = P - q, |d|^2, beta r, compare)
+BYTES_NODE_TEST = 32   # sector 0 of a NodeF32 record
+BYTES_NODE_FAR = 96    # sectors 1-3 (far-field coefficients)
+BYTES_TRI = 48
+BYTES_QUERY_IO = 12 + 4 + 1 + 4  # point in, Omega + inside out, sort index
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--nu", type=int, default=316)
+    p.add_argument("--queries", type=int, default=10_000_000)
+    p.add_argument("--leaf", type=int, default=4)
+    p.add_argument("--traversal", default="thread", choices=["thread", "warp"])
+    p.add_argument("--block", type=int, default=128)
+    p.add_argument("--fp64-steps", type=int, default=2)
+    p.add_argument("--cpu-sample", type=int, default=100_000)
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-fp64", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-clocks", action="store_true")
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------------------------------------
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def init_dist(world, backend):
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group(backend=backend)
+        return dist
+    return None
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, x: float, device=None) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------------------------
+class Clocks:
+    """nvidia-smi sampling (200 ms) during the timed region."""
+
+    def __init__(self, enabled: bool, index: int):
+        self.enabled = enabled
+        self.index = index
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        if not self.enabled:
+            return self
+        self.path.parent.mkdir(exist_ok=True)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["not sampled"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except Exception:
+            pass
+    return {}
+
+
+# ---------------------------------------------------------------------------------------------
+def run_reference(args, rank, world):
+    """CPU implementation of the reference path (oracle restatement O2), all host threads."""
+    dist = init_dist(world, "gloo")
+    if rank != 0:
+        barrier(dist)
+        return
+    import oracle
+    from lagrange_gb300 import workloads as W
+    wl = W.displaced_icosphere_workload(nu=args.nu, n_queries=args.queries)
+    nthr = oracle.nthreads_default()
+    t0 = time.perf_counter()
+    tree = oracle.RefTree(wl.V, wl.F, leaf_size=args.leaf)
+    build_s = time.perf_counter() - t0
+    rng = np.random.default_rng(7)
+    nb = len(wl.Q) // 2
+    half = args.cpu_sample // 2
+    sample = np.concatenate([wl.Q[rng.choice(nb, half, replace=False)],
+                             wl.Q[nb + rng.choice(len(wl.Q) - nb, args.cpu_sample - half,
+                                                  replace=False)]])
+    for _ in range(args.warmup):
+        tree.query(sample[:2000], beta=wl.beta, nthreads=nthr)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        tree.query(sample, beta=wl.beta, nthreads=nthr)
+    dt = (time.perf_counter() - t0) / args.steps
+    qps = len(sample) / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": qps, "unit": "queries/s", "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": wl.name, "triangles": int(len(wl.F)), "queries": int(len(wl.Q)),
+                   "beta": wl.beta, "leaf_size": args.leaf},
+        "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": nthr, "kind": "port",
+                         "sample": f"{len(sample)} queries per step (half box, half near-surface)"
+                                   f" of the {len(wl.Q)}-query workload; tree build "
+                                   f"{build_s:.2f} s single-thread",
+                         "build_s": build_s},
+        "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference library (jdumas/WindingNumber via lagrange_winding) cannot be built in "
+                "this environment; this arm times the CPU restatement of its algorithm (float "
+                "order-2 Barill tree, beta=2, per-point queries over all host threads)",
+    }
+    print(json.dumps(line), flush=True)
+    barrier(dist)
+
+
+# ---------------------------------------------------------------------------------------------
+def run_ours(args, rank, world, local):
+    import torch
+    torch.cuda.set_device(local)
+    dist = init_dist(world, "nccl")
+    dev = torch.device("cuda", local)
+    import lagrange_gb300 as fwn
+    from lagrange_gb300 import workloads as W
+
+    wl = W.displaced_icosphere_workload(nu=args.nu, n_queries=args.queries)
+    if world > 1 and rank > 0:  # each rank answers its own shuffle of the queries on its replica
+        perm = np.random.default_rng(1000 + rank).permutation(len(wl.Q))
+        wl.Q = wl.Q[perm]
+        wl.near_mask = wl.near_mask[perm]
+    n = len(wl.Q)
+    trav = fwn.TRAVERSAL_WARP if args.traversal == "warp" else fwn.TRAVERSAL_THREAD
+    Vd = torch.from_numpy(wl.V).to(dev)
+    Fd = torch.from_numpy(wl.F).to(dev)
+    Qd = torch.from_numpy(wl.Q).to(dev)
+    stream = torch.cuda.current_stream(dev)
+    eng = fwn.FastWindingNumber(Vd, Fd, leaf_size=args.leaf,
+                                records=fwn.RECORDS_F32 | (0 if args.no_fp64 else fwn.RECORDS_F64))
+    torch.cuda.synchronize()
+    # build timing (device, CUDA events inside the library): best of 3 extra builds
+    build_ms = []
+    for _ in range(3):
+        e2 = fwn.FastWindingNumber(Vd, Fd, leaf_size=args.leaf, records=fwn.RECORDS_F32)
+        build_ms.append(e2.info()["build_ms"])
+        e2.close()
+    info = eng.info()
+    w_out = torch.empty(n, dtype=torch.float32, device=dev)
+    i_out = torch.empty(n, dtype=torch.uint8, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > L2 (129 MB)
+    L = fwn.library()
+    opts = fwn._opts(precision=fwn.PRECISION_MIXED, traversal=trav, block_size=args.block)
+    sptr = C.c_void_p(stream.cuda_stream)
+
+    def query_mixed():
+        fwn._check(L.fwn_query_ex(eng.handle, C.byref(opts), C.c_void_p(Qd.data_ptr()), n,
+                                  C.c_void_p(w_out.data_ptr()), C.c_void_p(i_out.data_ptr()),
+                                  None, None, sptr))
+
+    for _ in range(args.warmup):
+        query_mixed()
+    torch.cuda.synchronize()
+    # work counters (untimed)
+    _, _, stats = eng.query(Qd, traversal=trav, block_size=args.block, stats=True)
+    torch.cuda.synchronize()
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    barrier(dist)
+    torch.cuda.synchronize()
+    with Clocks(not args.no_clocks and rank == 0, local) as clk:
+        t_wall = time.perf_counter()
+        for k in range(args.steps):
+            flush.zero_()  # L2 flush between timed steps (not inside the events)
+            ev[k][0].record(stream)
+            query_mixed()
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall
+    barrier(dist)
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    ms = sum(step_ms) / args.steps
+    ms = max_over_ranks(dist, ms, dev)
+    value = world * n / (ms / 1e3)
+    clocks = clk.summary()
+
+    result = {
+        "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 near field/refit)",
+        "data": "synthetic",
+        "config": {"workload": wl.name, "triangles": int(len(wl.F)), "queries_per_gpu": n,
+                   "beta": wl.beta, "leaf_size": args.leaf, "traversal": args.traversal,
+                   "block": args.block, "l2": "flushed before every step (256 MB write)",
+                   "parallelism": f"replicas x{world} (query shards, no collective)"},
+        "build_ms": min(build_ms), "tree": {"nodes": info["num_nodes"], "leaves": info["num_leaves"],
+                                            "device_bytes": info["device_bytes"]},
+        "step_ms_min": min(step_ms), "wall_s_timed": t_wall,
+        "gpu_launches": (1 + (4 * 3 + 1)) * args.steps,  # per step: 4 sort passes x3 + keys + traversal
+        "clocks": clocks,
+    }
+
+    # ---- roofline from the counters --------------------------------------------------------
+    far, tri, nodes = stats["far_evals"], stats["tri_evals"], stats["nodes_tested"]
+    flops = far * FLOPS_FAR + tri * FLOPS_TRI + (nodes - far) * FLOPS_TEST
+    l2_bytes = nodes * BYTES_NODE_TEST + far * BYTES_NODE_FAR + tri * BYTES_TRI + n * BYTES_QUERY_IO
+    props = torch.cuda.get_device_properties(dev)
+    sm_max = clocks.get("sm_max_mhz") or measured_peaks().get("sm_max_mhz") or 2070.0
+    peak_fp32 = props.multi_processor_count * 128 * 2 * sm_max * 1e6 / 1e12
+    achieved = flops / (ms / 1e3) / 1e12
+    result["roofline"] = {
+        "bound": "fp32", "achieved": achieved, "peak": peak_fp32, "unit": "TFLOP/s",
+        "frac": achieved / peak_fp32, "traffic": None,
+        "peak_source": f"nominal FP32: {props.multi_processor_count} SMs x 128 lanes x 2 x "
+                       f"{sm_max:.0f} MHz (no FP32 figure in MEASURED_PEAKS.json)",
+        "per_query": {"far_evals": far / n, "tri_evals": tri / n, "nodes_tested": nodes / n,
+                      "tri_fp64": stats["tri_evals_fp64"] / n,
+                      "far_tests_fp64": stats["far_tests_fp64"] / n,
+                      "flops": flops / n, "l2_bytes": l2_bytes / n},
+        "l2_gbs_algorithmic": l2_bytes / (ms / 1e3) / 1e9,
+    }
+
+    # ---- plain FP64 form + accuracy gate ----------------------------------------------------
+    if not args.no_fp64:
+        w64 = torch.empty(n, dtype=torch.float64, device=dev)
+        o64 = fwn._opts(precision=fwn.PRECISION_FP64)
+
+        def query_fp64():
+            fwn._check(L.fwn_query_ex(eng.handle, C.byref(o64), C.c_void_p(Qd.data_ptr()), n,
+                                      None, None, C.c_void_p(w64.data_ptr()), None, sptr))
+        query_fp64()
+        torch.cuda.synchronize()
+        t64 = []
+        for _ in range(max(1, args.fp64_steps)):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            query_fp64()
+            b.record(stream)
+            torch.cuda.synchronize()
+            t64.append(a.elapsed_time(b))
+        ms64 = sum(t64) / len(t64)
+        query_mixed()
+        torch.cuda.synchronize()
+        dw = (w_out.double() - w64).abs() / FOUR_PI
+        near = torch.from_numpy(wl.near_mask).to(dev)
+        result["plain_fp64"] = {
+            "value": n / (ms64 / 1e3), "unit": "queries/s", "ms_per_step": ms64,
+            "speedup_mixed_over_fp64": ms64 / ms,
+            "max_dw": float(dw.max()), "rms_dw": float(dw.pow(2).mean().sqrt()),
+            "max_dw_near": float(dw[near].max()), "max_dw_far": float(dw[~near].max()),
+            "gate_1e-4": bool(float(dw.max()) <= 1e-4),
+            "inside_disagree_band": int(((i_out.bool() != (w64 > 2 * math.pi)) &
+                                         ((w64 / FOUR_PI - 0.5).abs() > 1e-3)).sum()),
+        }
+        del w64
+
+    # ---- e2e through the C ABI with host buffers ---------------------------------------------
+    if not args.no_e2e:
+        Qh = torch.from_numpy(wl.Q).pin_memory()
+        wh = torch.empty(n, dtype=torch.float32).pin_memory()
+        ih = torch.empty(n, dtype=torch.uint8).pin_memory()
+
+        def e2e_call():
+            fwn._check(L.fwn_query_host(eng.handle, C.c_void_p(Qh.data_ptr()), n,
+                                        C.c_void_p(wh.data_ptr()), C.c_void_p(ih.data_ptr())))
+        e2e_call()
+        ts = []
+        barrier(dist)
+        for _ in range(max(3, args.steps // 2)):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            e2e_call()
+            ts.append(time.perf_counter() - t0)
+        e2e_s = max_over_ranks(dist, sum(ts) / len(ts), dev)
+        result["e2e"] = {"value": world * n / e2e_s, "unit": "queries/s",
+                         "h2d_bytes_per_step": n * 12, "d2h_bytes_per_step": n * 5,
+                         "ms_per_step": e2e_s * 1e3, "api": "fwn_query_host (pinned host buffers)"}
+
+    # ---- CPU baseline (rank 0, N=1 only) -----------------------------------------------------
+    if rank == 0 and world == 1 and not args.no_cpu:
+        import oracle
+        nthr = oracle.nthreads_default()
+        t0 = time.perf_counter()
+        tree = oracle.RefTree(wl.V, wl.F, leaf_size=args.leaf)
+        build_s = time.perf_counter() - t0
+        rng = np.random.default_rng(7)
+        nb = n // 2
+        half = args.cpu_sample // 2
+        sample = np.concatenate([wl.Q[rng.choice(nb, half, replace=False)],
+                                 wl.Q[nb + rng.choice(n - nb, args.cpu_sample - half, replace=False)]])
+        tree.query(sample[:1000], nthreads=nthr)
+        t0 = time.perf_counter()
+        om_cpu, in_cpu = tree.query(sample, beta=wl.beta, nthreads=nthr)
+        dt = time.perf_counter() - t0
+        result["cpu_baseline"] = {
+            "value": len(sample) / dt, "unit": "queries/s", "cores": nthr, "kind": "port",
+            "sample": f"{len(sample)} queries (half box, half near-surface) of the workload; "
+                      f"float order-2 Barill tree restating the reference path; build "
+                      f"{build_s:.2f} s single-thread",
+        }
+        # is_inside agreement with the restated reference outside the +-1e-3 band
+        Qs = torch.from_numpy(sample).to(dev)
+        wg, ig = eng.query(Qs, traversal=trav)
+        torch.cuda.synchronize()
+        wg, ig = wg.cpu().numpy(), ig.cpu().numpy()
+        band = np.abs(om_cpu / FOUR_PI - 0.5) > 1e-3
+        result["inside_vs_reference"] = {
+            "sample": len(sample), "disagree_outside_band": int(np.sum(ig[band] != in_cpu[band])),
+            "max_dw_vs_reference_restatement": float(np.max(np.abs(wg - om_cpu)) / FOUR_PI)}
+
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    barrier(dist)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,206 @@
+/*
+ * fwn_gb300.h — C ABI of the GB300 (sm_103a) fast-winding-number engine.
+ *
+ * This is the drop-in boundary for the `lagrange::winding::FastWindingNumber` path of
+ * adobe/lagrange. Every entry point is plain C: POD arguments, raw pointers and sizes, a status
+ * code instead of exceptions, no CUDA or torch types (streams are passed as `void*` holding a
+ * `cudaStream_t`, 0 meaning the legacy default stream).
+ *
+ * Reference interfaces replaced (paths relative to the adobe/lagrange tree):
+ *   - fwn_build          <- FastWindingNumber::FastWindingNumber(const SurfaceMesh<S,I>&)
+ *                           modules/winding/src/FastWindingNumber.cpp:87-98, whose Impl::initialize
+ *                           (:31-58) casts vertices to float and indices to int and calls
+ *                           UT_SolidAngle<float,float>::init (:57).
+ *   - fwn_query[_host]   <- FastWindingNumber::solid_angle / is_inside
+ *                           modules/winding/src/FastWindingNumber.cpp:105-113 -> Impl::is_inside
+ *                           (:60-67, `Omega / (4*pi) > 0.5f`) and Impl::solid_angle (:69-76), both
+ *                           per point; here they are batched.
+ *   - fwn_destroy        <- FastWindingNumber::~FastWindingNumber (:101, value_ptr<Impl> release).
+ *   - fwn_forest_*       <- no single reference call: the reference builds one engine per mesh
+ *                           and queries per point; the forest batches many meshes.
+ *
+ * Threading: a built handle is immutable. Concurrent fwn_query calls on one handle from several
+ * host threads are safe (each call allocates its own stream-ordered scratch), matching the
+ * reference's const query methods called from OpenVDB worker threads
+ * (modules/volume/src/mesh_to_volume.cpp:175-183).
+ */
+#ifndef FWN_GB300_H
+#define FWN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define FWN_API __declspec(dllexport)
+#else
+#define FWN_API __attribute__((visibility("default")))
+#endif
+
+/* Status codes. Every entry point returns one; fwn_last_error() gives the message. */
+typedef enum fwn_status {
+    FWN_OK = 0,
+    FWN_INVALID_ARG = 1,   /* bad sizes, null pointers, out-of-range indices, non-finite vertices */
+    FWN_OOM = 2,           /* device allocation failed */
+    FWN_CUDA_ERROR = 3,    /* a CUDA runtime call or kernel failed */
+    FWN_TIMEOUT = 4,       /* a bounded device-side wait gave up */
+    FWN_INTERNAL = 5,      /* a device-side consistency check failed (corrupt tree links) */
+    FWN_NOT_BUILT = 6      /* handle is null / default-constructed */
+} fwn_status;
+
+/* Precision forms of the query. */
+enum {
+    FWN_PRECISION_MIXED = 0, /* FP32 traversal + far field, Kahan sum, FP64 for close triangles */
+    FWN_PRECISION_FP64 = 1   /* plain form: FP64 everywhere */
+};
+
+/* Traversal schedules of the mixed form. */
+enum {
+    FWN_TRAVERSAL_AUTO = 0,   /* autotuned choice (thread schedule until tuned) */
+    FWN_TRAVERSAL_THREAD = 1, /* one thread per query, stackless skip-link walk */
+    FWN_TRAVERSAL_WARP = 2    /* warp-shared cursor over 32 queries, leaf triangles in smem */
+};
+
+/* Which node-record sets a build keeps (bit mask). */
+enum {
+    FWN_RECORDS_F32 = 1, /* 128 B FP32 records for the mixed form */
+    FWN_RECORDS_F64 = 2, /* 256 B FP64 records for the plain FP64 form */
+    FWN_RECORDS_MOMENTS = 4 /* keep the FP64 refit moments (fwn_export_moments, tests) */
+};
+
+typedef struct fwn_config {
+    float beta;            /* far-field accuracy scale: node is far if |q-P| > beta*r. Default 2 */
+    int32_t leaf_size;     /* max triangles per tree leaf, 1..16. Default 4 */
+    int32_t records;       /* FWN_RECORDS_* mask. Default FWN_RECORDS_F32 */
+    int32_t precision;     /* default query form, FWN_PRECISION_*. Default MIXED */
+    int32_t traversal;     /* default schedule, FWN_TRAVERSAL_*. Default AUTO */
+    int32_t block_size;    /* query kernel block size (multiple of 32, <= 1024); 0 = tuned */
+    int32_t sort_queries;  /* 1: Morton-sort queries before traversal (default), 0: input order */
+    float fp64_near_scale; /* FP64 near field if triangle is within scale*bbox_diagonal. 1e-3 */
+    int32_t reserved[8];
+} fwn_config;
+
+/* Per-query options (override the handle's defaults; pass NULL for defaults). */
+typedef struct fwn_query_opts {
+    int32_t precision;     /* FWN_PRECISION_* or -1 for the handle default */
+    int32_t traversal;     /* FWN_TRAVERSAL_* or -1 */
+    int32_t block_size;    /* 0 = handle default */
+    int32_t sort_queries;  /* -1 = handle default */
+    float beta;            /* <= 0: handle default */
+    int32_t reserved[7];
+} fwn_query_opts;
+
+/* Work counters of one query call (filled when a non-NULL pointer is passed to fwn_query_ex). */
+typedef struct fwn_query_stats {
+    uint64_t nodes_tested;     /* node visits (far test evaluated) */
+    uint64_t far_evals;        /* order-2 Taylor evaluations */
+    uint64_t tri_evals;        /* exact triangle solid angles (all precisions) */
+    uint64_t tri_evals_fp64;   /* of which evaluated in FP64 (mixed form only) */
+    uint64_t far_tests_fp64;   /* far tests re-decided in FP64 inside the guard band */
+} fwn_query_stats;
+
+typedef struct fwn_info {
+    int64_t num_vertices;
+    int64_t num_triangles;
+    int64_t num_nodes;         /* nodes in traversal order (all meshes) */
+    int64_t num_leaves;
+    int64_t num_meshes;
+    int64_t device_bytes;      /* resident bytes of the built structure */
+    double build_ms;           /* device time of the last build (CUDA events) */
+    float bbox_min[3];         /* bbox of mesh 0 */
+    float bbox_max[3];
+    int32_t leaf_size;
+    int32_t records;
+} fwn_info;
+
+typedef struct fwn_engine* fwn_handle;
+
+FWN_API void fwn_config_default(fwn_config* cfg);
+
+/* Copies the last error message of the calling thread into buf (always NUL-terminated) and
+ * returns the full message length. */
+FWN_API size_t fwn_last_error(char* buf, size_t buflen);
+
+/* Library version string, e.g. "0.1.0 sm_103a". */
+FWN_API const char* fwn_version(void);
+
+/* Build from HOST arrays: vertices [nv x 3] float row-major, triangles [nf x 3] int32.
+ * Mirrors FastWindingNumber.cpp:40-57 (float vertices, int indices). nf == 0 gives an engine
+ * whose solid angle is 0 everywhere. Out-of-range indices or non-finite referenced vertex
+ * coordinates return FWN_INVALID_ARG. Synchronous. */
+FWN_API fwn_status fwn_build(const float* vertices, int64_t num_vertices,
+                             const int32_t* triangles, int64_t num_triangles,
+                             const fwn_config* cfg, fwn_handle* out);
+
+/* Same, from DEVICE arrays (already resident in HBM). Synchronous on `stream`. */
+FWN_API fwn_status fwn_build_device(const float* d_vertices, int64_t num_vertices,
+                                    const int32_t* d_triangles, int64_t num_triangles,
+                                    const fwn_config* cfg, void* stream, fwn_handle* out);
+
+FWN_API fwn_status fwn_destroy(fwn_handle h);
+
+FWN_API fwn_status fwn_get_info(fwn_handle h, fwn_info* info);
+
+/* Queries on DEVICE buffers: points [n x 3] float; omega [n] float (solid angle, steradians) and
+ * inside [n] uint8 (Omega/(4*pi) > 0.5, FastWindingNumber.cpp:66), either output may be NULL.
+ * Asynchronous on `stream`; scratch is stream-ordered. */
+FWN_API fwn_status fwn_query(fwn_handle h, const float* d_points, int64_t n,
+                             float* d_omega, uint8_t* d_inside, void* stream);
+
+/* Extended query: per-call options, optional FP64 solid-angle output (plain FP64 form only,
+ * may be NULL), optional work counters (synchronises the stream when non-NULL). */
+FWN_API fwn_status fwn_query_ex(fwn_handle h, const fwn_query_opts* opts,
+                                const float* d_points, int64_t n, float* d_omega,
+                                uint8_t* d_inside, double* d_omega_f64,
+                                fwn_query_stats* stats, void* stream);
+
+/* Queries on HOST buffers (pinned or pageable): copies in, runs, copies out. Synchronous. */
+FWN_API fwn_status fwn_query_host(fwn_handle h, const float* points, int64_t n,
+                                  float* omega, uint8_t* inside);
+
+/* Exports the tree for inspection/tests into HOST arrays (any may be NULL):
+ *   skip [num_nodes] int32, tri_begin [num_nodes] int32, tri_count [num_nodes] int32
+ *   (0 for internal nodes), center_radius [num_nodes x 4] double (P.xyz, r) from the FP64
+ *   refit, sorted_tri [num_triangles] int32 (original triangle id of each leaf slot),
+ *   mesh_root [num_meshes x 2] int32 (first node, end node) */
+FWN_API fwn_status fwn_export_tree(fwn_handle h, int32_t* skip, int32_t* tri_begin,
+                                   int32_t* tri_count, double* center_radius,
+                                   int32_t* sorted_tri, int32_t* mesh_root);
+
+/* Exports the FP64 moments of every node [num_nodes x 33] double: P(3) N(3) M1(9, row i=normal
+ * component, column j=offset component) M2(18, [i][xx,yy,zz,xy,xz,yz]). Needs FWN_RECORDS_F64 or
+ * a build that kept the staging records (tests). */
+FWN_API fwn_status fwn_export_moments(fwn_handle h, double* moments);
+
+/* ---- Forest: many meshes built and queried together (one launch per stage over all meshes).
+ * vertices/triangles are concatenated; triangle indices are LOCAL to their mesh.
+ * vertex_offsets [num_meshes+1], triangle_offsets [num_meshes+1] (host int64 prefix offsets).
+ * Host arrays; synchronous. */
+FWN_API fwn_status fwn_forest_build(const float* vertices, const int64_t* vertex_offsets,
+                                    const int32_t* triangles, const int64_t* triangle_offsets,
+                                    int64_t num_meshes, const fwn_config* cfg, fwn_handle* out);
+
+/* Forest build from DEVICE vertex/triangle arrays (offsets stay on the host). */
+FWN_API fwn_status fwn_forest_build_device(const float* d_vertices,
+                                           const int64_t* vertex_offsets,
+                                           const int32_t* d_triangles,
+                                           const int64_t* triangle_offsets, int64_t num_meshes,
+                                           const fwn_config* cfg, void* stream,
+                                           fwn_handle* out);
+
+/* Forest query on DEVICE buffers: points of mesh m are d_points[query_offsets[m] ..
+ * query_offsets[m+1]) (host int64 offsets, num_meshes+1 entries). One persistent launch over
+ * a work queue of (mesh, chunk) items. */
+FWN_API fwn_status fwn_forest_query(fwn_handle h, const float* d_points,
+                                    const int64_t* query_offsets, float* d_omega,
+                                    uint8_t* d_inside, const fwn_query_opts* opts,
+                                    void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FWN_GB300_H */

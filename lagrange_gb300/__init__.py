@@ -1,0 +1,354 @@
+"""GB300 fast-winding-number engine — Python host surface over the C ABI (include/fwn_gb300.h).
+
+Mirrors ``lagrange::winding::FastWindingNumber`` (modules/winding/include/lagrange/winding/
+FastWindingNumber.h:24-108): construct from a triangle mesh, then ``solid_angle`` / ``is_inside``
+— here over batches of points (numpy arrays on the host, or CUDA tensors already in HBM).
+
+The compiled library ``lagrange_gb300/_lib/libfwn_gb300.so`` is REQUIRED: there is no CPU
+fallback. Build it with ``python -c "import __graft_entry__ as g; g.build()"`` (or
+``python lagrange_gb300/build.py``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from pathlib import Path
+
+import numpy as np
+
+__all__ = ["FastWindingNumber", "Forest", "WindingError", "library", "config_default",
+           "PRECISION_MIXED", "PRECISION_FP64", "TRAVERSAL_AUTO", "TRAVERSAL_THREAD",
+           "TRAVERSAL_WARP", "RECORDS_F32", "RECORDS_F64", "RECORDS_MOMENTS"]
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libfwn_gb300.so"
+
+PRECISION_MIXED, PRECISION_FP64 = 0, 1
+TRAVERSAL_AUTO, TRAVERSAL_THREAD, TRAVERSAL_WARP = 0, 1, 2
+RECORDS_F32, RECORDS_F64, RECORDS_MOMENTS = 1, 2, 4
+
+STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA_ERROR", 4: "TIMEOUT", 5: "INTERNAL",
+          6: "NOT_BUILT"}
+FOUR_PI = 4.0 * math.pi
+
+
+class WindingError(RuntimeError):
+    """Raised when a C-ABI call returns a non-OK status (the reference raises lagrange::Error)."""
+
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+class fwn_config(C.Structure):
+    _fields_ = [("beta", C.c_float), ("leaf_size", C.c_int32), ("records", C.c_int32),
+                ("precision", C.c_int32), ("traversal", C.c_int32), ("block_size", C.c_int32),
+                ("sort_queries", C.c_int32), ("fp64_near_scale", C.c_float),
+                ("reserved", C.c_int32 * 8)]
+
+
+class fwn_query_opts(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("traversal", C.c_int32), ("block_size", C.c_int32),
+                ("sort_queries", C.c_int32), ("beta", C.c_float), ("reserved", C.c_int32 * 7)]
+
+
+class fwn_query_stats(C.Structure):
+    _fields_ = [("nodes_tested", C.c_uint64), ("far_evals", C.c_uint64),
+                ("tri_evals", C.c_uint64), ("tri_evals_fp64", C.c_uint64),
+                ("far_tests_fp64", C.c_uint64)]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
+
+
+class fwn_info(C.Structure):
+    _fields_ = [("num_vertices", C.c_int64), ("num_triangles", C.c_int64),
+                ("num_nodes", C.c_int64), ("num_leaves", C.c_int64), ("num_meshes", C.c_int64),
+                ("device_bytes", C.c_int64), ("build_ms", C.c_double),
+                ("bbox_min", C.c_float * 3), ("bbox_max", C.c_float * 3),
+                ("leaf_size", C.c_int32), ("records", C.c_int32)]
+
+
+_lib = None
+
+# every entry point declared in include/fwn_gb300.h
+EXPORTS = ["fwn_config_default", "fwn_last_error", "fwn_version", "fwn_build", "fwn_build_device",
+           "fwn_destroy", "fwn_get_info", "fwn_query", "fwn_query_ex", "fwn_query_host",
+           "fwn_export_tree", "fwn_export_moments", "fwn_forest_build",
+           "fwn_forest_build_device", "fwn_forest_query"]
+
+
+def library():
+    """Loads the engine library (raises if it has not been built — no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(
+            f"{LIB_PATH} is missing: the CUDA engine must be built first "
+            "(python -c 'import __graft_entry__ as g; g.build()'); there is no CPU fallback")
+    L = C.CDLL(str(LIB_PATH))
+    P, i64, st = C.c_void_p, C.c_int64, C.c_int
+    L.fwn_config_default.argtypes = [C.POINTER(fwn_config)]
+    L.fwn_config_default.restype = None
+    L.fwn_last_error.argtypes = [C.c_char_p, C.c_size_t]
+    L.fwn_last_error.restype = C.c_size_t
+    L.fwn_version.argtypes = []
+    L.fwn_version.restype = C.c_char_p
+    L.fwn_build.argtypes = [P, i64, P, i64, C.POINTER(fwn_config), C.POINTER(P)]
+    L.fwn_build_device.argtypes = [P, i64, P, i64, C.POINTER(fwn_config), P, C.POINTER(P)]
+    L.fwn_destroy.argtypes = [P]
+    L.fwn_get_info.argtypes = [P, C.POINTER(fwn_info)]
+    L.fwn_query.argtypes = [P, P, i64, P, P, P]
+    L.fwn_query_ex.argtypes = [P, C.POINTER(fwn_query_opts), P, i64, P, P, P,
+                               C.POINTER(fwn_query_stats), P]
+    L.fwn_query_host.argtypes = [P, P, i64, P, P]
+    L.fwn_export_tree.argtypes = [P, P, P, P, P, P, P]
+    L.fwn_export_moments.argtypes = [P, P]
+    L.fwn_forest_build.argtypes = [P, P, P, P, i64, C.POINTER(fwn_config), C.POINTER(P)]
+    L.fwn_forest_build_device.argtypes = [P, P, P, P, i64, C.POINTER(fwn_config), P,
+                                          C.POINTER(P)]
+    L.fwn_forest_query.argtypes = [P, P, P, P, P, C.POINTER(fwn_query_opts), P]
+    for name in ("fwn_build", "fwn_build_device", "fwn_destroy", "fwn_get_info", "fwn_query",
+                 "fwn_query_ex", "fwn_query_host", "fwn_export_tree", "fwn_export_moments",
+                 "fwn_forest_build", "fwn_forest_build_device", "fwn_forest_query"):
+        getattr(L, name).restype = st
+    _lib = L
+    return L
+
+
+def _check(status: int):
+    if status != 0:
+        buf = C.create_string_buffer(1024)
+        library().fwn_last_error(buf, 1024)
+        raise WindingError(status, buf.value.decode(errors="replace"))
+
+
+def config_default(**overrides) -> fwn_config:
+    c = fwn_config()
+    library().fwn_config_default(C.byref(c))
+    for k, v in overrides.items():
+        if not hasattr(c, k):
+            raise TypeError(f"unknown config field {k!r}")
+        setattr(c, k, v)
+    return c
+
+
+def _opts(precision=None, traversal=None, block_size=None, sort_queries=None, beta=None):
+    o = fwn_query_opts()
+    o.precision = -1 if precision is None else int(precision)
+    o.traversal = -1 if traversal is None else int(traversal)
+    o.block_size = 0 if block_size is None else int(block_size)
+    o.sort_queries = -1 if sort_queries is None else int(sort_queries)
+    o.beta = 0.0 if beta is None else float(beta)
+    return o
+
+
+def _is_cuda_tensor(x) -> bool:
+    return type(x).__module__.startswith("torch") and getattr(x, "is_cuda", False)
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        try:
+            import torch
+            return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        except Exception:
+            return C.c_void_p(0)
+    if isinstance(stream, int):
+        return C.c_void_p(stream)
+    return C.c_void_p(stream.cuda_stream)
+
+
+def _host_mesh(vertices, facets):
+    V = np.ascontiguousarray(np.asarray(vertices), dtype=np.float32)   # FastWindingNumber.cpp:40-44
+    F = np.ascontiguousarray(np.asarray(facets), dtype=np.int64)
+    if V.ndim != 2 or V.shape[1] != 3:
+        raise WindingError(1, "Fast winding number engine only supports 3D meshes")
+    if F.size and (F.ndim != 2 or F.shape[1] != 3):
+        raise WindingError(1, "Fast winding number engine only supports triangle meshes")
+    F = F.reshape(-1, 3)
+    # indices are cast to int (FastWindingNumber.cpp:46-50); out-of-range ones are rejected by
+    # the device build
+    F32 = F.astype(np.int32)
+    if F.size and (F.max() > np.iinfo(np.int32).max or F.min() < np.iinfo(np.int32).min):
+        raise WindingError(1, "triangle vertex index out of range")
+    return V, F32
+
+
+class FastWindingNumber:
+    """Winding-number engine for one triangle mesh.
+
+    ``FastWindingNumber(vertices [nv,3], facets [nf,3], beta=2, leaf_size=4, ...)``.
+    Host numpy inputs use the synchronous host path; CUDA tensors stay on the device.
+    """
+
+    def __init__(self, vertices=None, facets=None, *, config: fwn_config | None = None,
+                 **cfg_overrides):
+        self._h = C.c_void_p(None)
+        if vertices is None:
+            return  # default-constructed: queries raise NOT_BUILT
+        cfg = config if config is not None else config_default(**cfg_overrides)
+        L = library()
+        if _is_cuda_tensor(vertices):
+            import torch
+            V = vertices.detach().to(torch.float32).contiguous()
+            F = facets.detach().to(torch.int32).contiguous()
+            if V.dim() != 2 or V.shape[1] != 3:
+                raise WindingError(1, "Fast winding number engine only supports 3D meshes")
+            _check(L.fwn_build_device(C.c_void_p(V.data_ptr()), V.shape[0],
+                                      C.c_void_p(F.data_ptr()), F.shape[0] if F.numel() else 0,
+                                      C.byref(cfg), _stream_ptr(None), C.byref(self._h)))
+        else:
+            V, F = _host_mesh(vertices, facets)
+            _check(L.fwn_build(V.ctypes.data_as(C.c_void_p), len(V),
+                               F.ctypes.data_as(C.c_void_p), len(F), C.byref(cfg),
+                               C.byref(self._h)))
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            library().fwn_destroy(self._h)
+            self._h = C.c_void_p(None)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    def info(self) -> dict:
+        i = fwn_info()
+        _check(library().fwn_get_info(self._h, C.byref(i)))
+        d = {k: getattr(i, k) for k, _ in fwn_info._fields_}
+        d["bbox_min"] = list(i.bbox_min)
+        d["bbox_max"] = list(i.bbox_max)
+        return d
+
+    # ---- queries -------------------------------------------------------------------------
+    def query(self, points, *, omega=True, inside=True, precision=None, traversal=None,
+              block_size=None, sort_queries=None, beta=None, omega_f64=False, stats=False,
+              stream=None):
+        """Returns (omega, inside[, omega_f64][, stats]) for a batch of points.
+
+        numpy input -> numpy outputs (host path, synchronous unless options are given, in which
+        case a device round trip through torch is used). CUDA tensor input -> CUDA tensors.
+        """
+        L = library()
+        o = _opts(precision, traversal, block_size, sort_queries, beta)
+        if _is_cuda_tensor(points):
+            import torch
+            Q = points.detach().to(torch.float32).contiguous().reshape(-1, 3)
+            n = Q.shape[0]
+            dev = Q.device
+            w = torch.empty(n, dtype=torch.float32, device=dev) if omega else None
+            ins = torch.empty(n, dtype=torch.uint8, device=dev) if inside else None
+            w64 = torch.empty(n, dtype=torch.float64, device=dev) if omega_f64 else None
+            st = fwn_query_stats() if stats else None
+            ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else None  # noqa: E731
+            _check(L.fwn_query_ex(self._h, C.byref(o), ptr(Q), n, ptr(w), ptr(ins), ptr(w64),
+                                  C.byref(st) if st is not None else None, _stream_ptr(stream)))
+            out = (w, ins)
+            if omega_f64:
+                out = out + (w64,)
+            if stats:
+                out = out + (st.as_dict(),)
+            return out
+        Q = np.ascontiguousarray(np.asarray(points), dtype=np.float32).reshape(-1, 3)
+        plain = all(v is None for v in (precision, traversal, block_size, sort_queries, beta)) \
+            and not omega_f64 and not stats
+        if plain:
+            n = len(Q)
+            w = np.empty(n, np.float32) if omega else None
+            ins = np.empty(n, np.uint8) if inside else None
+            pw = w.ctypes.data_as(C.c_void_p) if w is not None else None
+            pi = ins.ctypes.data_as(C.c_void_p) if ins is not None else None
+            _check(L.fwn_query_host(self._h, Q.ctypes.data_as(C.c_void_p), n, pw, pi))
+            return w, ins
+        import torch
+        res = self.query(torch.from_numpy(Q).cuda(), omega=omega, inside=inside,
+                         precision=precision, traversal=traversal, block_size=block_size,
+                         sort_queries=sort_queries, beta=beta, omega_f64=omega_f64, stats=stats,
+                         stream=stream)
+        torch.cuda.synchronize()
+        return tuple(r.cpu().numpy() if hasattr(r, "cpu") else r for r in res)
+
+    def solid_angle(self, points):
+        """Solid angle(s) in steradians (FastWindingNumber.cpp:69-76). A single point (3,)
+        returns a float, a batch (n,3) an array."""
+        single = np.ndim(points) == 1 and not _is_cuda_tensor(points)
+        w, _ = self.query(points, inside=False)
+        return float(w[0]) if single else w
+
+    def is_inside(self, points):
+        """Omega/(4 pi) > 0.5 (FastWindingNumber.cpp:60-67)."""
+        single = np.ndim(points) == 1 and not _is_cuda_tensor(points)
+        _, ins = self.query(points, omega=False)
+        return bool(ins[0]) if single else (ins.astype(bool) if isinstance(ins, np.ndarray) else ins)
+
+    # ---- inspection ------------------------------------------------------------------------
+    def export_tree(self) -> dict:
+        inf = self.info()
+        E, nf, M = inf["num_nodes"], inf["num_triangles"], inf["num_meshes"]
+        out = dict(skip=np.empty(E, np.int32), tri_begin=np.empty(E, np.int32),
+                   tri_count=np.empty(E, np.int32), center_radius=np.empty((E, 4), np.float64),
+                   sorted_tri=np.empty(nf, np.int32), mesh_root=np.empty((M, 2), np.int32))
+        p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+        _check(library().fwn_export_tree(self._h, p(out["skip"]), p(out["tri_begin"]),
+                                         p(out["tri_count"]), p(out["center_radius"]),
+                                         p(out["sorted_tri"]), p(out["mesh_root"])))
+        return out
+
+    def export_moments(self) -> np.ndarray:
+        E = self.info()["num_nodes"]
+        m = np.empty((E, 33), np.float64)
+        _check(library().fwn_export_moments(self._h, m.ctypes.data_as(C.c_void_p)))
+        return m
+
+
+class Forest(FastWindingNumber):
+    """Many meshes built and queried together (one launch per stage over all meshes)."""
+
+    def __init__(self, vertices, voff, facets, foff, *, config: fwn_config | None = None,
+                 **cfg_overrides):
+        self._h = C.c_void_p(None)
+        cfg = config if config is not None else config_default(**cfg_overrides)
+        self.voff = np.ascontiguousarray(voff, dtype=np.int64)
+        self.foff = np.ascontiguousarray(foff, dtype=np.int64)
+        self.nmeshes = len(self.voff) - 1
+        L = library()
+        if _is_cuda_tensor(vertices):
+            import torch
+            V = vertices.detach().to(torch.float32).contiguous()
+            F = facets.detach().to(torch.int32).contiguous()
+            _check(L.fwn_forest_build_device(C.c_void_p(V.data_ptr()),
+                                             self.voff.ctypes.data_as(C.c_void_p),
+                                             C.c_void_p(F.data_ptr()),
+                                             self.foff.ctypes.data_as(C.c_void_p), self.nmeshes,
+                                             C.byref(cfg), _stream_ptr(None), C.byref(self._h)))
+        else:
+            V = np.ascontiguousarray(vertices, dtype=np.float32)
+            F = np.ascontiguousarray(facets, dtype=np.int32)
+            _check(L.fwn_forest_build(V.ctypes.data_as(C.c_void_p),
+                                      self.voff.ctypes.data_as(C.c_void_p),
+                                      F.ctypes.data_as(C.c_void_p),
+                                      self.foff.ctypes.data_as(C.c_void_p), self.nmeshes,
+                                      C.byref(cfg), C.byref(self._h)))
+
+    def query_forest(self, points, qoff, *, precision=None, traversal=None, block_size=None,
+                     sort_queries=None, beta=None, stream=None):
+        """points: CUDA tensor [sum Q, 3]; qoff: host int64 offsets [M+1]."""
+        import torch
+        qoff = np.ascontiguousarray(qoff, dtype=np.int64)
+        Q = points.detach().to(torch.float32).contiguous().reshape(-1, 3)
+        n = Q.shape[0]
+        w = torch.empty(n, dtype=torch.float32, device=Q.device)
+        ins = torch.empty(n, dtype=torch.uint8, device=Q.device)
+        o = _opts(precision, traversal, block_size, sort_queries, beta)
+        _check(library().fwn_forest_query(self._h, C.c_void_p(Q.data_ptr()),
+                                          qoff.ctypes.data_as(C.c_void_p),
+                                          C.c_void_p(w.data_ptr()), C.c_void_p(ins.data_ptr()),
+                                          C.byref(o), _stream_ptr(stream)))
+        return w, ins

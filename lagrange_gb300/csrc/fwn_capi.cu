@@ -1,0 +1,350 @@
+// C ABI of the engine (declared in include/fwn_gb300.h). No exception crosses this boundary:
+// every entry point catches, stores the message in a thread-local slot and returns a status.
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "fwn_internal.cuh"
+
+namespace fwn {
+
+static thread_local std::string g_last_error;
+
+void set_last_error(const std::string& m) { g_last_error = m; }
+
+Engine::~Engine() {
+    if (nodes32) cudaFree(nodes32);
+    if (nodes64) cudaFree(nodes64);
+    if (tris) cudaFree(tris);
+    if (sorted_tri) cudaFree(sorted_tri);
+    if (meshes) cudaFree(meshes);
+    if (stage) cudaFree(stage);
+    delete[] meshes_h;
+    delete[] node_tri_begin_h;
+}
+
+namespace {
+
+template <class Fn> fwn_status guarded(Fn&& fn) {
+    try {
+        fn();
+        return FWN_OK;
+    } catch (const Error& e) {
+        set_last_error(e.what());
+        return e.status;
+    } catch (const std::bad_alloc&) {
+        set_last_error("host allocation failed");
+        return FWN_OOM;
+    } catch (const std::exception& e) {
+        set_last_error(e.what());
+        return FWN_INTERNAL;
+    } catch (...) {
+        set_last_error("unknown error");
+        return FWN_INTERNAL;
+    }
+}
+
+void validate_config(const fwn_config& c) {
+    if (!(c.beta > 0.f) || !std::isfinite(c.beta)) throw Error(FWN_INVALID_ARG, "beta must be finite and > 0");
+    if (c.leaf_size < 1 || c.leaf_size > 16) throw Error(FWN_INVALID_ARG, "leaf_size must be in [1, 16]");
+    if (!(c.records & (FWN_RECORDS_F32 | FWN_RECORDS_F64)))
+        throw Error(FWN_INVALID_ARG, "records must include FWN_RECORDS_F32 or FWN_RECORDS_F64");
+    if (c.precision != FWN_PRECISION_MIXED && c.precision != FWN_PRECISION_FP64)
+        throw Error(FWN_INVALID_ARG, "unknown precision");
+    if (c.traversal < FWN_TRAVERSAL_AUTO || c.traversal > FWN_TRAVERSAL_WARP)
+        throw Error(FWN_INVALID_ARG, "unknown traversal");
+    if (c.block_size < 0 || c.block_size > 1024 || c.block_size % 32 != 0)
+        throw Error(FWN_INVALID_ARG, "block_size must be 0 or a multiple of 32 <= 1024");
+    if (!(c.fp64_near_scale >= 0.f) || !std::isfinite(c.fp64_near_scale))
+        throw Error(FWN_INVALID_ARG, "fp64_near_scale must be finite and >= 0");
+}
+
+struct OwnedStream {
+    cudaStream_t s = nullptr;
+    OwnedStream() { FWN_CUDA_CHECK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking)); }
+    ~OwnedStream() {
+        if (s) cudaStreamDestroy(s);
+    }
+};
+
+Engine* engine_of(fwn_handle h) {
+    if (!h) throw Error(FWN_NOT_BUILT, "null handle (default-constructed or moved-from engine)");
+    return reinterpret_cast<Engine*>(h);
+}
+
+Engine* new_engine(const fwn_config* cfg) {
+    fwn_config c;
+    fwn_config_default(&c);
+    if (cfg) c = *cfg;
+    validate_config(c);
+    Engine* e = new Engine();
+    e->cfg = c;
+    FWN_CUDA_CHECK(cudaGetDevice(&e->device));
+    return e;
+}
+
+void build_into(Engine* e, const float* d_V, const int64_t* voff, const int32_t* d_F,
+                const int64_t* foff, int64_t nmeshes, cudaStream_t st) {
+    build_forest(*e, d_V, voff, d_F, foff, nmeshes, st);
+}
+
+void check_points(int64_t n, const void* p) {
+    if (n < 0) throw Error(FWN_INVALID_ARG, "number of points must be >= 0");
+    if (n > 0 && !p) throw Error(FWN_INVALID_ARG, "points pointer is null");
+    if (n > (int64_t)INT32_MAX) throw Error(FWN_INVALID_ARG, "at most 2^31-1 points per call");
+}
+
+void check_mesh_args(const void* V, int64_t nv, const void* F, int64_t nf) {
+    if (nv < 0 || nf < 0) throw Error(FWN_INVALID_ARG, "sizes must be >= 0");
+    if (nv > 0 && !V) throw Error(FWN_INVALID_ARG, "vertices pointer is null");
+    if (nf > 0 && !F) throw Error(FWN_INVALID_ARG, "triangles pointer is null");
+}
+
+}  // namespace
+}  // namespace fwn
+
+using namespace fwn;
+
+extern "C" {
+
+FWN_API void fwn_config_default(fwn_config* c) {
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->beta = 2.0f;
+    c->leaf_size = 4;
+    c->records = FWN_RECORDS_F32;
+    c->precision = FWN_PRECISION_MIXED;
+    c->traversal = FWN_TRAVERSAL_AUTO;
+    c->block_size = 0;
+    c->sort_queries = 1;
+    c->fp64_near_scale = 1e-3f;
+}
+
+FWN_API size_t fwn_last_error(char* buf, size_t n) {
+    const std::string& m = g_last_error;
+    if (buf && n) {
+        size_t k = m.size() < n - 1 ? m.size() : n - 1;
+        std::memcpy(buf, m.data(), k);
+        buf[k] = '\0';
+    }
+    return m.size();
+}
+
+FWN_API const char* fwn_version(void) { return "0.1.0 sm_103a"; }
+
+FWN_API fwn_status fwn_build(const float* V, int64_t nv, const int32_t* F, int64_t nf,
+                             const fwn_config* cfg, fwn_handle* out) {
+    return guarded([&] {
+        if (!out) throw Error(FWN_INVALID_ARG, "out is null");
+        *out = nullptr;
+        check_mesh_args(V, nv, F, nf);
+        std::unique_ptr<Engine> e(new_engine(cfg));
+        OwnedStream os;
+        Scratch dv(nv * 3 * sizeof(float), os.s), df(nf * 3 * sizeof(int32_t), os.s);
+        if (nv) FWN_CUDA_CHECK(cudaMemcpyAsync(dv.p, V, nv * 3 * sizeof(float), cudaMemcpyHostToDevice, os.s));
+        if (nf) FWN_CUDA_CHECK(cudaMemcpyAsync(df.p, F, nf * 3 * sizeof(int32_t), cudaMemcpyHostToDevice, os.s));
+        const int64_t voff[2] = {0, nv}, foff[2] = {0, nf};
+        build_into(e.get(), dv.as<float>(), voff, df.as<int32_t>(), foff, 1, os.s);
+        FWN_CUDA_CHECK(cudaStreamSynchronize(os.s));
+        *out = reinterpret_cast<fwn_handle>(e.release());
+    });
+}
+
+FWN_API fwn_status fwn_build_device(const float* d_V, int64_t nv, const int32_t* d_F, int64_t nf,
+                                    const fwn_config* cfg, void* stream, fwn_handle* out) {
+    return guarded([&] {
+        if (!out) throw Error(FWN_INVALID_ARG, "out is null");
+        *out = nullptr;
+        check_mesh_args(d_V, nv, d_F, nf);
+        std::unique_ptr<Engine> e(new_engine(cfg));
+        const int64_t voff[2] = {0, nv}, foff[2] = {0, nf};
+        build_into(e.get(), d_V, voff, d_F, foff, 1, static_cast<cudaStream_t>(stream));
+        *out = reinterpret_cast<fwn_handle>(e.release());
+    });
+}
+
+FWN_API fwn_status fwn_destroy(fwn_handle h) {
+    return guarded([&] {
+        if (!h) return;
+        delete reinterpret_cast<Engine*>(h);
+    });
+}
+
+FWN_API fwn_status fwn_get_info(fwn_handle h, fwn_info* info) {
+    return guarded([&] {
+        Engine* e = engine_of(h);
+        if (!info) throw Error(FWN_INVALID_ARG, "info is null");
+        std::memset(info, 0, sizeof(*info));
+        info->num_vertices = e->nv;
+        info->num_triangles = e->nf;
+        info->num_nodes = e->num_nodes;
+        info->num_leaves = e->num_leaves;
+        info->num_meshes = e->nmeshes;
+        info->device_bytes = e->device_bytes;
+        info->build_ms = e->build_ms;
+        for (int a = 0; a < 3; ++a) {
+            info->bbox_min[a] = e->meshes_h[0].lo[a];
+            info->bbox_max[a] = e->meshes_h[0].hi[a];
+        }
+        info->leaf_size = e->cfg.leaf_size;
+        info->records = e->cfg.records;
+    });
+}
+
+FWN_API fwn_status fwn_query(fwn_handle h, const float* d_points, int64_t n, float* d_omega,
+                             uint8_t* d_inside, void* stream) {
+    return fwn_query_ex(h, nullptr, d_points, n, d_omega, d_inside, nullptr, nullptr, stream);
+}
+
+FWN_API fwn_status fwn_query_ex(fwn_handle h, const fwn_query_opts* opts, const float* d_points,
+                                int64_t n, float* d_omega, uint8_t* d_inside, double* d_omega64,
+                                fwn_query_stats* stats, void* stream) {
+    return guarded([&] {
+        Engine* e = engine_of(h);
+        check_points(n, d_points);
+        if (e->nmeshes != 1) throw Error(FWN_INVALID_ARG, "forest handle: use fwn_forest_query");
+        QueryArgs a = resolve_query_args(*e, opts);
+        query_mesh(*e, 0, a, d_points, n, d_omega, d_inside, d_omega64, stats,
+                   static_cast<cudaStream_t>(stream));
+    });
+}
+
+FWN_API fwn_status fwn_query_host(fwn_handle h, const float* points, int64_t n, float* omega,
+                                  uint8_t* inside) {
+    return guarded([&] {
+        Engine* e = engine_of(h);
+        check_points(n, points);
+        if (e->nmeshes != 1) throw Error(FWN_INVALID_ARG, "forest handle: use fwn_forest_query");
+        if (n == 0) return;
+        QueryArgs a = resolve_query_args(*e, nullptr);
+        OwnedStream os;
+        Scratch dq(n * 3 * sizeof(float), os.s);
+        Scratch dw(omega ? n * sizeof(float) : 0, os.s);
+        Scratch di(inside ? n * sizeof(uint8_t) : 0, os.s);
+        FWN_CUDA_CHECK(cudaMemcpyAsync(dq.p, points, n * 3 * sizeof(float), cudaMemcpyHostToDevice, os.s));
+        query_mesh(*e, 0, a, dq.as<float>(), n, dw.as<float>(), di.as<uint8_t>(), nullptr, nullptr,
+                   os.s, /*check=*/true);
+        if (omega) FWN_CUDA_CHECK(cudaMemcpyAsync(omega, dw.p, n * sizeof(float), cudaMemcpyDeviceToHost, os.s));
+        if (inside) FWN_CUDA_CHECK(cudaMemcpyAsync(inside, di.p, n, cudaMemcpyDeviceToHost, os.s));
+        FWN_CUDA_CHECK(cudaStreamSynchronize(os.s));
+    });
+}
+
+FWN_API fwn_status fwn_export_tree(fwn_handle h, int32_t* skip, int32_t* tri_begin,
+                                   int32_t* tri_count, double* center_radius, int32_t* sorted_tri,
+                                   int32_t* mesh_root) {
+    return guarded([&] {
+        Engine* e = engine_of(h);
+        const int64_t E = e->num_nodes;
+        if (E > 0 && (skip || tri_begin || tri_count || center_radius)) {
+            if (e->nodes32) {
+                std::vector<NodeF32> nodes(E);
+                FWN_CUDA_CHECK(cudaMemcpy(nodes.data(), e->nodes32, E * sizeof(NodeF32), cudaMemcpyDeviceToHost));
+                for (int64_t i = 0; i < E; ++i) {
+                    if (skip) skip[i] = nodes[i].skip;
+                    if (tri_begin) tri_begin[i] = nodes[i].tri_begin;
+                    if (tri_count) tri_count[i] = nodes[i].tri_count;
+                    if (center_radius) {
+                        center_radius[4 * i + 0] = nodes[i].s0.x;
+                        center_radius[4 * i + 1] = nodes[i].s0.y;
+                        center_radius[4 * i + 2] = nodes[i].s0.z;
+                        center_radius[4 * i + 3] = nodes[i].s0.w;
+                    }
+                }
+            } else {
+                std::vector<NodeF64> nodes(E);
+                FWN_CUDA_CHECK(cudaMemcpy(nodes.data(), e->nodes64, E * sizeof(NodeF64), cudaMemcpyDeviceToHost));
+                for (int64_t i = 0; i < E; ++i) {
+                    if (skip) skip[i] = nodes[i].skip;
+                    if (tri_begin) tri_begin[i] = nodes[i].tri_begin;
+                    if (tri_count) tri_count[i] = nodes[i].tri_count;
+                    if (center_radius) {
+                        for (int a = 0; a < 3; ++a) center_radius[4 * i + a] = nodes[i].P[a];
+                        center_radius[4 * i + 3] = nodes[i].r;
+                    }
+                }
+            }
+        }
+        if (sorted_tri && e->nf > 0)
+            FWN_CUDA_CHECK(cudaMemcpy(sorted_tri, e->sorted_tri, e->nf * sizeof(int32_t), cudaMemcpyDeviceToHost));
+        if (mesh_root)
+            for (int64_t m = 0; m < e->nmeshes; ++m) {
+                mesh_root[2 * m] = e->meshes_h[m].root;
+                mesh_root[2 * m + 1] = e->meshes_h[m].end;
+            }
+    });
+}
+
+FWN_API fwn_status fwn_export_moments(fwn_handle h, double* moments) {
+    return guarded([&] {
+        Engine* e = engine_of(h);
+        if (!moments) throw Error(FWN_INVALID_ARG, "moments is null");
+        if (!e->stage && e->num_nodes > 0)
+            throw Error(FWN_INVALID_ARG, "engine was built without FWN_RECORDS_MOMENTS");
+        const int64_t E = e->num_nodes;
+        std::vector<StageRec> recs(E);
+        if (E) FWN_CUDA_CHECK(cudaMemcpy(recs.data(), e->stage, E * sizeof(StageRec), cudaMemcpyDeviceToHost));
+        for (int64_t i = 0; i < E; ++i) {
+            double* o = moments + 33 * i;
+            for (int a = 0; a < 3; ++a) o[a] = recs[i].P[a];
+            for (int a = 0; a < 3; ++a) o[3 + a] = recs[i].N[a];
+            for (int a = 0; a < 9; ++a) o[6 + a] = recs[i].M1[a];
+            for (int a = 0; a < 18; ++a) o[15 + a] = recs[i].M2[a];
+        }
+    });
+}
+
+FWN_API fwn_status fwn_forest_build(const float* V, const int64_t* voff, const int32_t* F,
+                                    const int64_t* foff, int64_t nmeshes, const fwn_config* cfg,
+                                    fwn_handle* out) {
+    return guarded([&] {
+        if (!out) throw Error(FWN_INVALID_ARG, "out is null");
+        *out = nullptr;
+        if (nmeshes < 1 || !voff || !foff) throw Error(FWN_INVALID_ARG, "bad forest offsets");
+        const int64_t nv = voff[nmeshes], nf = foff[nmeshes];
+        check_mesh_args(V, nv, F, nf);
+        std::unique_ptr<Engine> e(new_engine(cfg));
+        OwnedStream os;
+        Scratch dv(nv * 3 * sizeof(float), os.s), df(nf * 3 * sizeof(int32_t), os.s);
+        if (nv) FWN_CUDA_CHECK(cudaMemcpyAsync(dv.p, V, nv * 3 * sizeof(float), cudaMemcpyHostToDevice, os.s));
+        if (nf) FWN_CUDA_CHECK(cudaMemcpyAsync(df.p, F, nf * 3 * sizeof(int32_t), cudaMemcpyHostToDevice, os.s));
+        build_into(e.get(), dv.as<float>(), voff, df.as<int32_t>(), foff, nmeshes, os.s);
+        FWN_CUDA_CHECK(cudaStreamSynchronize(os.s));
+        *out = reinterpret_cast<fwn_handle>(e.release());
+    });
+}
+
+FWN_API fwn_status fwn_forest_build_device(const float* d_V, const int64_t* voff,
+                                           const int32_t* d_F, const int64_t* foff,
+                                           int64_t nmeshes, const fwn_config* cfg, void* stream,
+                                           fwn_handle* out) {
+    return guarded([&] {
+        if (!out) throw Error(FWN_INVALID_ARG, "out is null");
+        *out = nullptr;
+        if (nmeshes < 1 || !voff || !foff) throw Error(FWN_INVALID_ARG, "bad forest offsets");
+        check_mesh_args(d_V, voff[nmeshes], d_F, foff[nmeshes]);
+        std::unique_ptr<Engine> e(new_engine(cfg));
+        build_into(e.get(), d_V, voff, d_F, foff, nmeshes, static_cast<cudaStream_t>(stream));
+        *out = reinterpret_cast<fwn_handle>(e.release());
+    });
+}
+
+FWN_API fwn_status fwn_forest_query(fwn_handle h, const float* d_points, const int64_t* qoff,
+                                    float* d_omega, uint8_t* d_inside, const fwn_query_opts* opts,
+                                    void* stream) {
+    return guarded([&] {
+        Engine* e = engine_of(h);
+        if (!qoff) throw Error(FWN_INVALID_ARG, "query offsets are null");
+        if (qoff[0] != 0) throw Error(FWN_INVALID_ARG, "query offsets must start at 0");
+        for (int64_t m = 0; m < e->nmeshes; ++m)
+            if (qoff[m + 1] < qoff[m]) throw Error(FWN_INVALID_ARG, "query offsets must not decrease");
+        check_points(qoff[e->nmeshes], d_points);
+        QueryArgs a = resolve_query_args(*e, opts);
+        query_forest(*e, a, d_points, qoff, d_omega, d_inside, static_cast<cudaStream_t>(stream));
+    });
+}
+
+}  // extern "C"

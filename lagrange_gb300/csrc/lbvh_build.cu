@@ -1,0 +1,832 @@
+// LBVH build of the winding-number forest (replaces the tree + moment precompute done by
+// UT_SolidAngle<float,float>::init, called at modules/winding/src/FastWindingNumber.cpp:57).
+//
+// Stages (each ONE launch over all meshes of the forest):
+//   K0  per-mesh vertex bbox (ordered-int atomics), mesh info (Morton frame, FP64 radius)
+//   K1  triangle keys: (mesh id << 30) | 30-bit Morton code of the float centroid
+//   K2  device radix sort of (key, triangle id)                       (radix_sort.cu)
+//   K3  Karras 2012 binary radix tree over the sorted keys (equal keys tie-broken by index)
+//   K3b collapse subtrees of <= leaf_size triangles into leaves and assign DFS pre-order
+//       positions + escape ("skip") links with one scan:  pos(v) = base[first(v)] + rank(v),
+//       skip(v) = base[last(v)+1], where base = exclusive scan of #emitted nodes per first leaf
+//       and rank(v) = #ancestors sharing first(v)
+//   K4  bottom-up FP64 refit of order-0/1/2 moments (atomic-counter ascent; the second child to
+//       arrive combines), then conversion to 128 B FP32 / 256 B FP64 records in DFS order
+//
+// This translation unit is compiled with -fmad=false: every floating-point operation is
+// individually rounded, in the order written, so the CPU restatement of the same build
+// (oracle/fwn_oracle.c, compiled with -ffp-contract=off) reproduces keys, topology, centres and
+// radii bit for bit.
+#include <cmath>
+#include <vector>
+
+#include "fwn_internal.cuh"
+
+namespace fwn {
+namespace {
+
+constexpr int MORTON_BITS = 30;
+
+__device__ __forceinline__ unsigned enc_float(float f) {
+    unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__host__ __device__ __forceinline__ float dec_float(unsigned u) {
+    unsigned b = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+#ifdef __CUDA_ARCH__
+    return __uint_as_float(b);
+#else
+    float f;
+    memcpy(&f, &b, 4);
+    return f;
+#endif
+}
+
+// Spreads the low 10 bits of x so that bit k moves to bit 3k.
+__device__ __forceinline__ unsigned spread3(unsigned x) {
+    x &= 0x3ffu;
+    x = (x | (x << 16)) & 0x030000ffu;
+    x = (x | (x << 8)) & 0x0300f00fu;
+    x = (x | (x << 4)) & 0x030c30c3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+
+__device__ __forceinline__ unsigned quantize10(float c, float lo, float inv) {
+    float u = (c - lo) * inv;
+    float s = u * 1024.0f;
+    int q = (s >= 0.0f) ? (int)floorf(s) : 0;  // also maps NaN to 0
+    return (unsigned)min(q, 1023);
+}
+
+__device__ __forceinline__ int find_mesh(const int64_t* off, int nmeshes, int64_t x) {
+    // last m with off[m] <= x (offsets non-decreasing; empty meshes skipped naturally)
+    int lo = 0, hi = nmeshes - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= x) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// ---- K0: per-mesh vertex bbox -----------------------------------------------------------------
+__global__ void k_mesh_bbox(const float* __restrict__ V, const int64_t* __restrict__ voff,
+                            int chunk, unsigned* __restrict__ enc) {
+    const int m = blockIdx.y;
+    const int64_t v0 = voff[m] + (int64_t)blockIdx.x * chunk;
+    const int64_t v1 = min(voff[m + 1], v0 + chunk);
+    if (v0 >= v1) return;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int64_t v = v0 + threadIdx.x; v < v1; v += blockDim.x) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            float x = V[3 * v + a];
+            lo[a] = fminf(lo[a], x);  // fminf/fmaxf ignore NaN
+            hi[a] = fmaxf(hi[a], x);
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[a] = fminf(lo[a], __shfl_xor_sync(0xffffffffu, lo[a], o));
+            hi[a] = fmaxf(hi[a], __shfl_xor_sync(0xffffffffu, hi[a], o));
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            atomicMin(&enc[6 * m + a], enc_float(lo[a]));
+            atomicMax(&enc[6 * m + 3 + a], enc_float(hi[a]));
+        }
+    }
+}
+
+__global__ void k_init_bbox(unsigned* enc, int nmeshes) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 6 * nmeshes) enc[i] = (i % 6) < 3 ? 0xffffffffu : 0u;
+}
+
+__global__ void k_mesh_info(const unsigned* __restrict__ enc, const int64_t* __restrict__ voff,
+                            int nmeshes, float near_scale, MeshInfo* __restrict__ mi) {
+    int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nmeshes) return;
+    MeshInfo r;
+    r.root = -1;
+    r.end = -1;
+    r.pad = 0.f;
+    r.pad2 = 0.f;
+    const bool has = voff[m + 1] > voff[m];
+    float diag2 = 0.f;
+    for (int a = 0; a < 3; ++a) {
+        float lo = has ? dec_float(enc[6 * m + a]) : 0.f;
+        float hi = has ? dec_float(enc[6 * m + 3 + a]) : 0.f;
+        if (!(lo <= hi)) { lo = 0.f; hi = 0.f; }  // all-NaN axis
+        r.lo[a] = lo;
+        r.hi[a] = hi;
+        float ext = hi - lo;
+        r.inv_ext[a] = ext > 0.f ? 1.0f / ext : 0.f;
+        diag2 = diag2 + ext * ext;
+    }
+    r.tau = near_scale * sqrtf(diag2);
+    mi[m] = r;
+}
+
+// ---- K1: triangle keys ------------------------------------------------------------------------
+__global__ void k_tri_keys(const float* __restrict__ V, const int32_t* __restrict__ F,
+                           const int64_t* __restrict__ voff, const int64_t* __restrict__ foff,
+                           int nmeshes, int64_t nf, const MeshInfo* __restrict__ mi,
+                           uint64_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                           unsigned* __restrict__ status) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nf) return;
+    const int m = find_mesh(foff, nmeshes, t);
+    const int64_t nvm = voff[m + 1] - voff[m];
+    float c[3] = {0.f, 0.f, 0.f};
+    bool ok = true;
+    int32_t idx[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        idx[j] = F[3 * t + j];
+        if (idx[j] < 0 || (int64_t)idx[j] >= nvm) ok = false;
+    }
+    if (!ok) {
+        atomicOr(status, ST_BAD_INDEX);
+    } else {
+        float v[3][3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const float* p = V + 3 * (voff[m] + idx[j]);
+            v[j][0] = p[0];
+            v[j][1] = p[1];
+            v[j][2] = p[2];
+            if (!isfinite(v[j][0]) || !isfinite(v[j][1]) || !isfinite(v[j][2])) ok = false;
+        }
+        if (!ok) atomicOr(status, ST_NONFINITE);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) c[a] = ((v[0][a] + v[1][a]) + v[2][a]) / 3.0f;
+    }
+    const MeshInfo& M = mi[m];
+    unsigned code = (spread3(quantize10(c[0], M.lo[0], M.inv_ext[0])) << 2) |
+                    (spread3(quantize10(c[1], M.lo[1], M.inv_ext[1])) << 1) |
+                    spread3(quantize10(c[2], M.lo[2], M.inv_ext[2]));
+    keys[t] = ((uint64_t)m << MORTON_BITS) | code;
+    vals[t] = (uint32_t)t;
+}
+
+// ---- K3: Karras hierarchy ---------------------------------------------------------------------
+// Node ids: internal nodes 0..n-2, leaf k -> n-1+k. Root is 0 (internal 0, or leaf 0 if n==1).
+__device__ __forceinline__ int kdelta(const uint64_t* __restrict__ keys, int n, int i, int64_t j) {
+    if (j < 0 || j >= n) return -1;
+    uint64_t a = keys[i], b = keys[j];
+    if (a == b) return 64 + __clz((unsigned)(i ^ (int)j));
+    return __clzll(a ^ b);
+}
+
+__global__ void k_leaf_init(int n, int* __restrict__ first, int* __restrict__ last) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    first[n - 1 + k] = k;
+    last[n - 1 + k] = k;
+}
+
+__global__ void k_karras(const uint64_t* __restrict__ keys, int n, int* __restrict__ left,
+                         int* __restrict__ right, int* __restrict__ parent,
+                         int* __restrict__ first, int* __restrict__ last) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    const int d = (kdelta(keys, n, i, i + 1) - kdelta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+    const int dmin = kdelta(keys, n, i, i - d);
+    int64_t lmax = 2;
+    while (kdelta(keys, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int64_t t = lmax >> 1; t >= 1; t >>= 1)
+        if (kdelta(keys, n, i, i + (l + t) * d) > dmin) l += (int)t;
+    const int j = i + l * d;
+    const int dnode = kdelta(keys, n, i, j);
+    int s = 0, step = l;
+    do {
+        step = (step + 1) >> 1;
+        if (kdelta(keys, n, i, (int64_t)i + (int64_t)(s + step) * d) > dnode) s += step;
+    } while (step > 1);
+    const int g = i + s * d + min(d, 0);
+    const int lo = min(i, j), hi = max(i, j);
+    const int lc = (lo == g) ? (n - 1 + g) : g;
+    const int rc = (hi == g + 1) ? (n - 1 + g + 1) : g + 1;
+    left[i] = lc;
+    right[i] = rc;
+    parent[lc] = i;
+    parent[rc] = i;
+    first[i] = lo;
+    last[i] = hi;
+    if (i == 0) parent[0] = -1;
+}
+
+__device__ __forceinline__ bool is_cross(const uint64_t* keys, const int* first, const int* last,
+                                         int u) {
+    return (keys[first[u]] >> MORTON_BITS) != (keys[last[u]] >> MORTON_BITS);
+}
+// A node is "big" (never collapsed into a leaf) if it spans meshes or holds > K triangles.
+__device__ __forceinline__ bool is_big(const uint64_t* keys, const int* first, const int* last,
+                                       int u, int K) {
+    return is_cross(keys, first, last, u) || (last[u] - first[u] + 1) > K;
+}
+
+// ---- K3b: collapse + DFS layout ---------------------------------------------------------------
+// flags: bit0 emitted, bit1 leaf
+__global__ void k_emit_count(int n, int K, const uint64_t* __restrict__ keys,
+                             const int* __restrict__ parent, const int* __restrict__ first,
+                             const int* __restrict__ last, int* __restrict__ cnt_first,
+                             uint8_t* __restrict__ flags) {
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= 2 * n - 1) return;
+    const int pu = parent[u];
+    const bool emitted = (u == 0) || (pu >= 0 && is_big(keys, first, last, pu, K));
+    const bool leaf = (u >= n - 1) || !is_big(keys, first, last, u, K);
+    flags[u] = (uint8_t)((emitted ? 1 : 0) | (leaf ? 2 : 0));
+    if (emitted) atomicAdd(&cnt_first[first[u]], 1);
+}
+
+__global__ void k_positions(int n, const int* __restrict__ parent, const int* __restrict__ first,
+                            const int* __restrict__ last, const uint8_t* __restrict__ flags,
+                            const int* __restrict__ base, int* __restrict__ pos,
+                            int* __restrict__ skip) {
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= 2 * n - 1) return;
+    if (!(flags[u] & 1)) {
+        pos[u] = -1;
+        skip[u] = -1;
+        return;
+    }
+    const int f = first[u];
+    int rank = 0, v = u;
+    while (v != 0) {
+        const int p = parent[v];
+        if (p < 0 || first[p] != f) break;  // p < 0 only for an unlinked node (never)
+        ++rank;
+        v = p;
+    }
+    pos[u] = base[f] + rank;
+    skip[u] = base[last[u] + 1];
+}
+
+__global__ void k_mesh_roots(int nmeshes, const int64_t* __restrict__ foff, int n,
+                             const int* __restrict__ parent, const int* __restrict__ first,
+                             const int* __restrict__ last, const int* __restrict__ pos,
+                             const int* __restrict__ skip, MeshInfo* __restrict__ mi) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nmeshes) return;
+    const int64_t lo = foff[m], hi = foff[m + 1] - 1;
+    if (hi < lo) {
+        mi[m].root = -1;
+        mi[m].end = -1;
+        return;
+    }
+    int u = (n - 1) + (int)lo;
+    while (u != 0) {
+        const int p = parent[u];
+        if (p < 0 || first[p] < lo || last[p] > hi) break;
+        u = p;
+    }
+    mi[m].root = pos[u];
+    mi[m].end = skip[u];
+}
+
+// ---- K4: FP64 refit ---------------------------------------------------------------------------
+__device__ __forceinline__ double round_up_float(double x) {
+    float f = (float)x;
+    if ((double)f < x) f = nextafterf(f, INFINITY);
+    return (double)f;
+}
+
+__device__ __forceinline__ void load_tri_d(const float* __restrict__ V, const int32_t* __restrict__ F,
+                                           int64_t vbase, int64_t t, double v[3][3]) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        const int64_t vi = vbase + F[3 * t + j];
+        v[j][0] = (double)V[3 * vi + 0];
+        v[j][1] = (double)V[3 * vi + 1];
+        v[j][2] = (double)V[3 * vi + 2];
+    }
+}
+
+// Moments of the triangles in sorted slots [f, l] about their area-weighted centroid.
+// Per triangle t (vertices v0,v1,v2, area-weighted normal n = (v1-v0)x(v2-v0)/2, centroid c,
+// d = c - P):  N += n,  M1[i][j] += n_i d_j,
+// M2[i][jk] += n_i (d_j d_k + (1/12) sum_v (v-c)_j (v-c)_k)   (exact area integral of
+// (x-P)_j (x-P)_k over the triangle divided by its area).
+__device__ void leaf_moments(const float* __restrict__ V, const int32_t* __restrict__ F,
+                             const int64_t* __restrict__ voff, const uint64_t* __restrict__ keys,
+                             const uint32_t* __restrict__ tri_of_slot, int f, int l,
+                             StageRec& R) {
+    double A = 0.0, S[3] = {0.0, 0.0, 0.0}, Cs[3] = {0.0, 0.0, 0.0};
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int s = f; s <= l; ++s) {
+        const int64_t t = tri_of_slot[s];
+        const int m = (int)(keys[s] >> MORTON_BITS);
+        double v[3][3];
+        load_tri_d(V, F, voff[m], t, v);
+        double e1[3], e2[3], nn[3], c[3];
+        for (int a = 0; a < 3; ++a) {
+            e1[a] = v[1][a] - v[0][a];
+            e2[a] = v[2][a] - v[0][a];
+        }
+        nn[0] = 0.5 * (e1[1] * e2[2] - e1[2] * e2[1]);
+        nn[1] = 0.5 * (e1[2] * e2[0] - e1[0] * e2[2]);
+        nn[2] = 0.5 * (e1[0] * e2[1] - e1[1] * e2[0]);
+        const double a_t = sqrt(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
+        for (int a = 0; a < 3; ++a) {
+            c[a] = ((v[0][a] + v[1][a]) + v[2][a]) / 3.0;
+            S[a] = S[a] + a_t * c[a];
+            Cs[a] = Cs[a] + c[a];
+        }
+        A = A + a_t;
+        for (int j = 0; j < 3; ++j)
+            for (int a = 0; a < 3; ++a) {
+                const float x = (float)v[j][a];
+                lo[a] = fminf(lo[a], x);
+                hi[a] = fmaxf(hi[a], x);
+            }
+    }
+    const double cnt = (double)(l - f + 1);
+    double P[3];
+    for (int a = 0; a < 3; ++a) {
+        const double pe = A > 0.0 ? S[a] / A : Cs[a] / cnt;
+        P[a] = (double)(float)pe;
+    }
+    double N[3] = {0, 0, 0}, M1[9], M2[18], r2 = 0.0;
+    for (int i = 0; i < 9; ++i) M1[i] = 0.0;
+    for (int i = 0; i < 18; ++i) M2[i] = 0.0;
+    for (int s = f; s <= l; ++s) {
+        const int64_t t = tri_of_slot[s];
+        const int m = (int)(keys[s] >> MORTON_BITS);
+        double v[3][3];
+        load_tri_d(V, F, voff[m], t, v);
+        double e1[3], e2[3], nn[3], c[3], d[3];
+        for (int a = 0; a < 3; ++a) {
+            e1[a] = v[1][a] - v[0][a];
+            e2[a] = v[2][a] - v[0][a];
+        }
+        nn[0] = 0.5 * (e1[1] * e2[2] - e1[2] * e2[1]);
+        nn[1] = 0.5 * (e1[2] * e2[0] - e1[0] * e2[2]);
+        nn[2] = 0.5 * (e1[0] * e2[1] - e1[1] * e2[0]);
+        for (int a = 0; a < 3; ++a) {
+            c[a] = ((v[0][a] + v[1][a]) + v[2][a]) / 3.0;
+            d[a] = c[a] - P[a];
+        }
+        double w[3][3];  // vertex offsets from the centroid
+        for (int j = 0; j < 3; ++j)
+            for (int a = 0; a < 3; ++a) w[j][a] = v[j][a] - c[a];
+        const int SJ[6] = {0, 1, 2, 0, 0, 1};
+        const int SK[6] = {0, 1, 2, 1, 2, 2};
+        double Q[6];
+        for (int q = 0; q < 6; ++q) {
+            const int j = SJ[q], k = SK[q];
+            const double cov = ((w[0][j] * w[0][k] + w[1][j] * w[1][k]) + w[2][j] * w[2][k]) / 12.0;
+            Q[q] = d[j] * d[k] + cov;
+        }
+        for (int i = 0; i < 3; ++i) {
+            N[i] = N[i] + nn[i];
+            for (int j = 0; j < 3; ++j) M1[3 * i + j] = M1[3 * i + j] + nn[i] * d[j];
+            for (int q = 0; q < 6; ++q) M2[6 * i + q] = M2[6 * i + q] + nn[i] * Q[q];
+        }
+        for (int j = 0; j < 3; ++j) {
+            const double dx = v[j][0] - P[0], dy = v[j][1] - P[1], dz = v[j][2] - P[2];
+            const double q2 = (dx * dx + dy * dy) + dz * dz;
+            r2 = fmax(r2, q2);
+        }
+    }
+    for (int a = 0; a < 3; ++a) {
+        R.P[a] = P[a];
+        R.N[a] = N[a];
+        R.lo[a] = lo[a];
+        R.hi[a] = hi[a];
+    }
+    for (int i = 0; i < 9; ++i) R.M1[i] = M1[i];
+    for (int i = 0; i < 18; ++i) R.M2[i] = M2[i];
+    R.area = A;
+    R.r = round_up_float(sqrt(r2));
+}
+
+__device__ __forceinline__ double ldcg_d(const double* p) { return __ldcg(p); }
+__device__ __forceinline__ float ldcg_f(const float* p) { return __ldcg(p); }
+
+__device__ void combine_moments(const StageRec* __restrict__ a_, const StageRec* __restrict__ b_,
+                                StageRec& R) {
+    // children were written by other threads: read through L2 (ld.global.cg)
+    double Pa[3], Pb[3], Na[3], Nb[3], M1a[9], M1b[9];
+    const double Aa = ldcg_d(&a_->area), Ab = ldcg_d(&b_->area);
+    for (int i = 0; i < 3; ++i) {
+        Pa[i] = ldcg_d(&a_->P[i]);
+        Pb[i] = ldcg_d(&b_->P[i]);
+        Na[i] = ldcg_d(&a_->N[i]);
+        Nb[i] = ldcg_d(&b_->N[i]);
+    }
+    for (int i = 0; i < 9; ++i) {
+        M1a[i] = ldcg_d(&a_->M1[i]);
+        M1b[i] = ldcg_d(&b_->M1[i]);
+    }
+    const double A = Aa + Ab;
+    double P[3], ea[3], eb[3];
+    for (int i = 0; i < 3; ++i) {
+        const double pe = A > 0.0 ? (Aa * Pa[i] + Ab * Pb[i]) / A : (Pa[i] + Pb[i]) * 0.5;
+        P[i] = (double)(float)pe;
+        ea[i] = Pa[i] - P[i];
+        eb[i] = Pb[i] - P[i];
+    }
+    for (int i = 0; i < 3; ++i) {
+        R.P[i] = P[i];
+        R.N[i] = Na[i] + Nb[i];
+        for (int j = 0; j < 3; ++j)
+            R.M1[3 * i + j] = (M1a[3 * i + j] + Na[i] * ea[j]) + (M1b[3 * i + j] + Nb[i] * eb[j]);
+    }
+    const int SJ[6] = {0, 1, 2, 0, 0, 1};
+    const int SK[6] = {0, 1, 2, 1, 2, 2};
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const int j = SJ[q], k = SK[q];
+            const double ta = ((ldcg_d(&a_->M2[6 * i + q]) + M1a[3 * i + j] * ea[k]) +
+                               M1a[3 * i + k] * ea[j]) + Na[i] * (ea[j] * ea[k]);
+            const double tb = ((ldcg_d(&b_->M2[6 * i + q]) + M1b[3 * i + j] * eb[k]) +
+                               M1b[3 * i + k] * eb[j]) + Nb[i] * (eb[j] * eb[k]);
+            R.M2[6 * i + q] = ta + tb;
+        }
+    double lo[3], hi[3];
+    for (int a = 0; a < 3; ++a) {
+        const float la = fminf(ldcg_f(&a_->lo[a]), ldcg_f(&b_->lo[a]));
+        const float ha = fmaxf(ldcg_f(&a_->hi[a]), ldcg_f(&b_->hi[a]));
+        R.lo[a] = la;
+        R.hi[a] = ha;
+        lo[a] = la;
+        hi[a] = ha;
+    }
+    R.area = A;
+    // radius: min of (a) the sphere around both child spheres, (b) farthest bbox corner
+    const double ra = ldcg_d(&a_->r), rb = ldcg_d(&b_->r);
+    const double da = sqrt((ea[0] * ea[0] + ea[1] * ea[1]) + ea[2] * ea[2]) + ra;
+    const double db = sqrt((eb[0] * eb[0] + eb[1] * eb[1]) + eb[2] * eb[2]) + rb;
+    double c2 = 0.0;
+    for (int a = 0; a < 3; ++a) {
+        const double x = fmax(fabs(P[a] - lo[a]), fabs(P[a] - hi[a]));
+        c2 = c2 + x * x;
+    }
+    R.r = round_up_float(fmin(fmax(da, db), sqrt(c2)));
+}
+
+__device__ __forceinline__ void store_rec(StageRec* dst, const StageRec& R) {
+    // plain stores: they reach L2 before the __threadfence of the ascent
+    *dst = R;
+}
+
+__global__ void k_refit(int n, int K, const uint64_t* __restrict__ keys,
+                        const int* __restrict__ parent, const int* __restrict__ first,
+                        const int* __restrict__ last, const int* __restrict__ left,
+                        const int* __restrict__ right, const int* __restrict__ pos,
+                        const uint32_t* __restrict__ tri_of_slot, const float* __restrict__ V,
+                        const int32_t* __restrict__ F, const int64_t* __restrict__ voff,
+                        StageRec* __restrict__ stage, int* __restrict__ visit,
+                        unsigned* __restrict__ status) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int e = (n - 1) + k;
+    while (e != 0) {
+        const int p = parent[e];
+        if (p < 0) {  // unlinked node: cannot happen for a Karras tree
+            atomicOr(status, ST_REFIT_ORPHAN);
+            return;
+        }
+        if (is_big(keys, first, last, p, K)) break;
+        e = p;
+    }
+    if (first[e] != k) return;  // the leaf is handled by the thread of its first slot
+    StageRec R;
+    leaf_moments(V, F, voff, keys, tri_of_slot, first[e], last[e], R);
+    store_rec(&stage[pos[e]], R);
+    int v = e;
+    int guard = 0;
+    while (v != 0) {
+        const int p = parent[v];
+        if (p < 0) {
+            atomicOr(status, ST_REFIT_ORPHAN);
+            return;
+        }
+        if (is_cross(keys, first, last, p)) break;  // v is a mesh root
+        __threadfence();
+        if (atomicAdd(&visit[p], 1) == 0) return;  // first arrival: the sibling continues
+        __threadfence();
+        const int pl = pos[left[p]], pr = pos[right[p]];
+        if (pl < 0 || pr < 0) {
+            atomicOr(status, ST_REFIT_ORPHAN);
+            return;
+        }
+        combine_moments(&stage[pl], &stage[pr], R);
+        store_rec(&stage[pos[p]], R);
+        v = p;
+        if (++guard > 4 * 64 + 64) {  // depth is bounded by key bits + index bits
+            atomicOr(status, ST_REFIT_ORPHAN);
+            return;
+        }
+    }
+}
+
+// ---- K4b: records -------------------------------------------------------------------------------
+struct Coeffs {
+    double trM1, N[3], W[3], C[6], D[10];
+};
+
+__device__ void derive_coeffs(const StageRec& R, Coeffs& c) {
+    const double* M1 = R.M1;
+    const double* M2 = R.M2;  // [i*6 + s], s: xx yy zz xy xz yz
+    c.trM1 = (M1[0] + M1[4]) + M1[8];
+    for (int i = 0; i < 3; ++i) c.N[i] = R.N[i];
+    // C = -3 sym(M1): d^T C d with off-diagonals doubled
+    c.C[0] = -3.0 * M1[0];
+    c.C[1] = -3.0 * M1[4];
+    c.C[2] = -3.0 * M1[8];
+    c.C[3] = -3.0 * (M1[1] + M1[3]);
+    c.C[4] = -3.0 * (M1[2] + M1[6]);
+    c.C[5] = -3.0 * (M1[5] + M1[7]);
+    // u_k = sum_i M2[i][ik], v_i = sum_j M2[i][jj]; W = -1.5 (2u + v)
+    auto m2 = [&](int i, int j, int k) -> double {
+        // symmetric pair (j,k) -> slot
+        int a = j < k ? j : k, b = j < k ? k : j;
+        int s = (a == b) ? a : (a == 0 ? (b == 1 ? 3 : 4) : 5);
+        return M2[6 * i + s];
+    };
+    for (int k = 0; k < 3; ++k) {
+        const double u = (m2(0, 0, k) + m2(1, 1, k)) + m2(2, 2, k);
+        const double v = (m2(k, 0, 0) + m2(k, 1, 1)) + m2(k, 2, 2);
+        c.W[k] = -1.5 * (2.0 * u + v);
+    }
+    // D = 7.5 * coefficients of the cubic sum_ijk M2_ijk d_i d_j d_k per monomial
+    const double xxx = m2(0, 0, 0), yyy = m2(1, 1, 1), zzz = m2(2, 2, 2);
+    const double xxy = 2.0 * m2(0, 0, 1) + m2(1, 0, 0);
+    const double xxz = 2.0 * m2(0, 0, 2) + m2(2, 0, 0);
+    const double xyy = 2.0 * m2(1, 0, 1) + m2(0, 1, 1);
+    const double yyz = 2.0 * m2(1, 1, 2) + m2(2, 1, 1);
+    const double xzz = 2.0 * m2(2, 0, 2) + m2(0, 2, 2);
+    const double yzz = 2.0 * m2(2, 1, 2) + m2(1, 2, 2);
+    const double xyz = 2.0 * ((m2(0, 1, 2) + m2(1, 0, 2)) + m2(2, 0, 1));
+    const double mono[10] = {xxx, yyy, zzz, xxy, xxz, xyy, yyz, xzz, yzz, xyz};
+    for (int i = 0; i < 10; ++i) c.D[i] = 7.5 * mono[i];
+}
+
+__global__ void k_convert(int n, const uint64_t* __restrict__ keys, const int* __restrict__ first,
+                          const int* __restrict__ last, const uint8_t* __restrict__ flags,
+                          const int* __restrict__ pos, const int* __restrict__ skip,
+                          const StageRec* __restrict__ stage, NodeF32* __restrict__ n32,
+                          NodeF64* __restrict__ n64, int* __restrict__ leaf_count) {
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= 2 * n - 1) return;
+    const uint8_t fl = flags[u];
+    if (!(fl & 1)) return;
+    const int i = pos[u];
+    const bool cross = is_cross(keys, first, last, u);
+    const bool leaf = (fl & 2) && !cross;
+    const int tb = first[u];
+    const int tc = leaf ? (last[u] - first[u] + 1) : 0;
+    if (leaf) atomicAdd(leaf_count, 1);
+    Coeffs c;
+    StageRec R;
+    if (!cross) {
+        R = stage[i];
+        derive_coeffs(R, c);
+    } else {
+        memset(&R, 0, sizeof(R));
+        memset(&c, 0, sizeof(c));
+    }
+    if (n32) {
+        NodeF32 o;
+        o.s0 = make_float4((float)R.P[0], (float)R.P[1], (float)R.P[2], (float)R.r);
+        o.skip = skip[u];
+        o.tri_begin = tb;
+        o.tri_count = tc;
+        o.trM1 = (float)c.trM1;
+        o.m0 = make_float4((float)c.N[0], (float)c.N[1], (float)c.N[2], (float)c.W[0]);
+        o.m1 = make_float4((float)c.W[1], (float)c.W[2], (float)c.C[0], (float)c.C[1]);
+        o.m2 = make_float4((float)c.C[2], (float)c.C[3], (float)c.C[4], (float)c.C[5]);
+        o.m3 = make_float4((float)c.D[0], (float)c.D[1], (float)c.D[2], (float)c.D[3]);
+        o.m4 = make_float4((float)c.D[4], (float)c.D[5], (float)c.D[6], (float)c.D[7]);
+        o.m5 = make_float4((float)c.D[8], (float)c.D[9], 0.f, 0.f);
+        n32[i] = o;
+    }
+    if (n64) {
+        NodeF64 o;
+        for (int a = 0; a < 3; ++a) {
+            o.P[a] = R.P[a];
+            o.N[a] = c.N[a];
+            o.W[a] = c.W[a];
+        }
+        o.r = R.r;
+        o.skip = skip[u];
+        o.tri_begin = tb;
+        o.tri_count = tc;
+        o.pad0 = 0;
+        o.trM1 = c.trM1;
+        for (int a = 0; a < 6; ++a) o.C[a] = c.C[a];
+        for (int a = 0; a < 10; ++a) o.D[a] = c.D[a];
+        o.pad1[0] = o.pad1[1] = o.pad1[2] = 0.0;
+        n64[i] = o;
+    }
+}
+
+__global__ void k_tri_records(int n, const uint32_t* __restrict__ tri_of_slot,
+                              const uint64_t* __restrict__ keys, const float* __restrict__ V,
+                              const int32_t* __restrict__ F, const int64_t* __restrict__ voff,
+                              TriF32* __restrict__ tris, int* __restrict__ sorted_tri) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const int64_t t = tri_of_slot[s];
+    const int m = (int)(keys[s] >> MORTON_BITS);
+    float v[3][3];
+    for (int j = 0; j < 3; ++j) {
+        const int64_t vi = voff[m] + F[3 * t + j];
+        v[j][0] = V[3 * vi];
+        v[j][1] = V[3 * vi + 1];
+        v[j][2] = V[3 * vi + 2];
+    }
+    float c[3];
+    for (int a = 0; a < 3; ++a) c[a] = ((v[0][a] + v[1][a]) + v[2][a]) / 3.0f;
+    float rt = 0.f;
+    for (int j = 0; j < 3; ++j) {
+        const float dx = v[j][0] - c[0], dy = v[j][1] - c[1], dz = v[j][2] - c[2];
+        rt = fmaxf(rt, sqrtf(dx * dx + dy * dy + dz * dz));
+    }
+    rt = rt * 1.0000010f + 1e-30f;  // conservative: the bound only selects the FP64 near field
+    const float e1x = v[1][0] - v[0][0], e1y = v[1][1] - v[0][1], e1z = v[1][2] - v[0][2];
+    const float e2x = v[2][0] - v[0][0], e2y = v[2][1] - v[0][1], e2z = v[2][2] - v[0][2];
+    const float nx = e1y * e2z - e1z * e2y, ny = e1z * e2x - e1x * e2z, nz = e1x * e2y - e1y * e2x;
+    const float nl = sqrtf(nx * nx + ny * ny + nz * nz);
+    TriF32 o;
+    o.t0 = make_float4(v[0][0], v[0][1], v[0][2], v[1][0]);
+    o.t1 = make_float4(v[1][1], v[1][2], v[2][0], v[2][1]);
+    o.t2 = make_float4(v[2][2], rt, nl > 0.f ? 1.0f / nl : 0.f, 0.f);
+    tris[s] = o;
+    sorted_tri[s] = (int)t;
+}
+
+template <class T> T* dalloc(size_t count, cudaStream_t s) {
+    void* p = nullptr;
+    if (count) FWN_CUDA_CHECK(cudaMallocAsync(&p, count * sizeof(T), s));
+    return static_cast<T*>(p);
+}
+
+inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
+
+}  // namespace
+
+void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int32_t* d_F,
+                  const int64_t* foff_h, int64_t nmeshes, cudaStream_t st) {
+    if (nmeshes <= 0 || nmeshes > 65535)
+        throw Error(FWN_INVALID_ARG, "number of meshes must be in [1, 65535]");
+    for (int64_t m = 0; m < nmeshes; ++m) {
+        if (voff_h[m + 1] < voff_h[m] || foff_h[m + 1] < foff_h[m] || voff_h[0] != 0 ||
+            foff_h[0] != 0)
+            throw Error(FWN_INVALID_ARG, "vertex/triangle offsets must start at 0 and not decrease");
+    }
+    const int64_t nv = voff_h[nmeshes], nf = foff_h[nmeshes];
+    if (nf > (int64_t)0x3fffffff)
+        throw Error(FWN_INVALID_ARG, "at most 2^30-1 triangles per forest");
+    e.nv = nv;
+    e.nf = nf;
+    e.nmeshes = nmeshes;
+    const int K = e.cfg.leaf_size;
+
+    cudaEvent_t ev0, ev1;
+    FWN_CUDA_CHECK(cudaEventCreate(&ev0));
+    FWN_CUDA_CHECK(cudaEventCreate(&ev1));
+    FWN_CUDA_CHECK(cudaEventRecord(ev0, st));
+
+    int64_t* voff = dalloc<int64_t>(nmeshes + 1, st);
+    int64_t* foff = dalloc<int64_t>(nmeshes + 1, st);
+    FWN_CUDA_CHECK(cudaMemcpyAsync(voff, voff_h, (nmeshes + 1) * sizeof(int64_t),
+                                   cudaMemcpyHostToDevice, st));
+    FWN_CUDA_CHECK(cudaMemcpyAsync(foff, foff_h, (nmeshes + 1) * sizeof(int64_t),
+                                   cudaMemcpyHostToDevice, st));
+    FWN_CUDA_CHECK(cudaMalloc(&e.meshes, nmeshes * sizeof(MeshInfo)));
+    e.meshes_h = new MeshInfo[nmeshes];
+    unsigned* enc = dalloc<unsigned>(6 * nmeshes, st);
+    unsigned* status = dalloc<unsigned>(1, st);
+    FWN_CUDA_CHECK(cudaMemsetAsync(status, 0, sizeof(unsigned), st));
+    k_init_bbox<<<grid_for(6 * nmeshes, 256), 256, 0, st>>>(enc, (int)nmeshes);
+    int64_t maxv = 0;
+    for (int64_t m = 0; m < nmeshes; ++m) maxv = std::max(maxv, voff_h[m + 1] - voff_h[m]);
+    if (maxv > 0) {
+        const int chunk = 16384;
+        dim3 g((unsigned)((maxv + chunk - 1) / chunk), (unsigned)nmeshes);
+        k_mesh_bbox<<<g, 256, 0, st>>>(d_V, voff, chunk, enc);
+    }
+    k_mesh_info<<<grid_for(nmeshes, 128), 128, 0, st>>>(enc, voff, (int)nmeshes,
+                                                        e.cfg.fp64_near_scale, e.meshes);
+    FWN_CUDA_CHECK(cudaGetLastError());
+
+    struct TmpList {  // stream-ordered frees on every exit path
+        std::vector<void*> v;
+        cudaStream_t s;
+        ~TmpList() {
+            for (void* p : v) cudaFreeAsync(p, s);
+        }
+    } tmp{{}, st};
+    auto track = [&](void* p) { tmp.v.push_back(p); return p; };
+    track(voff);
+    track(foff);
+    track(enc);
+    track(status);
+
+    if (nf > 0) {
+        const int n = (int)nf;
+        int mesh_bits = 0;
+        while ((1ll << mesh_bits) < nmeshes) ++mesh_bits;
+        uint64_t* keys_a = (uint64_t*)track(dalloc<uint64_t>(n, st));
+        uint64_t* keys_b = (uint64_t*)track(dalloc<uint64_t>(n, st));
+        uint32_t* vals_a = (uint32_t*)track(dalloc<uint32_t>(n, st));
+        uint32_t* vals_b = (uint32_t*)track(dalloc<uint32_t>(n, st));
+        void* sort_tmp = track(dalloc<char>(radix_sort_temp_bytes(n, 8), st));
+        k_tri_keys<<<grid_for(n, 256), 256, 0, st>>>(d_V, d_F, voff, foff, (int)nmeshes, nf,
+                                                     e.meshes, keys_a, vals_a, status);
+        FWN_CUDA_CHECK(cudaGetLastError());
+        unsigned st_h = 0;
+        FWN_CUDA_CHECK(cudaMemcpyAsync(&st_h, status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        FWN_CUDA_CHECK(cudaStreamSynchronize(st));
+        if (st_h & ST_BAD_INDEX) throw Error(FWN_INVALID_ARG, "triangle vertex index out of range");
+        if (st_h & ST_NONFINITE)
+            throw Error(FWN_INVALID_ARG, "non-finite vertex coordinate referenced by a triangle");
+        const bool in_b = radix_sort_u64(keys_a, vals_a, keys_b, vals_b, n,
+                                         MORTON_BITS + mesh_bits, sort_tmp, st);
+        const uint64_t* keys = in_b ? keys_b : keys_a;
+        const uint32_t* tri_of_slot = in_b ? vals_b : vals_a;
+
+        const int nn = 2 * n - 1;
+        int* parent = (int*)track(dalloc<int>(nn, st));
+        int* first = (int*)track(dalloc<int>(nn, st));
+        int* last = (int*)track(dalloc<int>(nn, st));
+        int* left = (int*)track(dalloc<int>(std::max(n - 1, 1), st));
+        int* right = (int*)track(dalloc<int>(std::max(n - 1, 1), st));
+        int* cnt = (int*)track(dalloc<int>(n + 1, st));
+        uint8_t* flags = (uint8_t*)track(dalloc<uint8_t>(nn, st));
+        int* pos = (int*)track(dalloc<int>(nn, st));
+        int* skip = (int*)track(dalloc<int>(nn, st));
+        void* scan_tmp = track(dalloc<char>(exclusive_scan_temp_bytes(n + 1), st));
+        int* visit = (int*)track(dalloc<int>(std::max(n - 1, 1), st));
+        int* leaf_count = (int*)track(dalloc<int>(1, st));
+
+        FWN_CUDA_CHECK(cudaMemsetAsync(parent, 0xff, (size_t)nn * sizeof(int), st));  // -1
+        k_leaf_init<<<grid_for(n, 256), 256, 0, st>>>(n, first, last);
+        if (n == 1) {
+            int m1 = -1;
+            FWN_CUDA_CHECK(cudaMemcpyAsync(parent, &m1, sizeof(int), cudaMemcpyHostToDevice, st));
+        } else {
+            k_karras<<<grid_for(n - 1, 256), 256, 0, st>>>(keys, n, left, right, parent, first, last);
+        }
+        FWN_CUDA_CHECK(cudaMemsetAsync(cnt, 0, (n + 1) * sizeof(int), st));
+        k_emit_count<<<grid_for(nn, 256), 256, 0, st>>>(n, K, keys, parent, first, last, cnt, flags);
+        exclusive_scan_i32(cnt, n + 1, scan_tmp, st);
+        k_positions<<<grid_for(nn, 256), 256, 0, st>>>(n, parent, first, last, flags, cnt, pos, skip);
+        k_mesh_roots<<<grid_for(nmeshes, 128), 128, 0, st>>>((int)nmeshes, foff, n, parent, first,
+                                                             last, pos, skip, e.meshes);
+        int E = 0;
+        FWN_CUDA_CHECK(cudaMemcpyAsync(&E, cnt + n, sizeof(int), cudaMemcpyDeviceToHost, st));
+        FWN_CUDA_CHECK(cudaStreamSynchronize(st));
+        e.num_nodes = E;
+
+        StageRec* stage = dalloc<StageRec>(E, st);
+        if (!(e.cfg.records & FWN_RECORDS_MOMENTS)) track(stage);
+        else e.stage = stage;
+        FWN_CUDA_CHECK(cudaMemsetAsync(visit, 0, std::max(n - 1, 1) * sizeof(int), st));
+        FWN_CUDA_CHECK(cudaMemsetAsync(leaf_count, 0, sizeof(int), st));
+        k_refit<<<grid_for(n, 128), 128, 0, st>>>(n, K, keys, parent, first, last, left, right, pos,
+                                                  tri_of_slot, d_V, d_F, voff, stage, visit, status);
+        FWN_CUDA_CHECK(cudaGetLastError());
+        if (e.cfg.records & FWN_RECORDS_F32) FWN_CUDA_CHECK(cudaMalloc(&e.nodes32, E * sizeof(NodeF32)));
+        if (e.cfg.records & FWN_RECORDS_F64) FWN_CUDA_CHECK(cudaMalloc(&e.nodes64, E * sizeof(NodeF64)));
+        k_convert<<<grid_for(nn, 128), 128, 0, st>>>(n, keys, first, last, flags, pos, skip, stage,
+                                                     e.nodes32, e.nodes64, leaf_count);
+        FWN_CUDA_CHECK(cudaMalloc(&e.tris, (size_t)n * sizeof(TriF32)));
+        FWN_CUDA_CHECK(cudaMalloc(&e.sorted_tri, (size_t)n * sizeof(int)));
+        k_tri_records<<<grid_for(n, 256), 256, 0, st>>>(n, tri_of_slot, keys, d_V, d_F, voff,
+                                                        e.tris, e.sorted_tri);
+        FWN_CUDA_CHECK(cudaGetLastError());
+        int lc = 0;
+        FWN_CUDA_CHECK(cudaMemcpyAsync(&lc, leaf_count, sizeof(int), cudaMemcpyDeviceToHost, st));
+        FWN_CUDA_CHECK(cudaMemcpyAsync(&st_h, status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        FWN_CUDA_CHECK(cudaStreamSynchronize(st));
+        e.num_leaves = lc;
+        if (st_h & ST_REFIT_ORPHAN) throw Error(FWN_INTERNAL, "refit ascent found an inconsistent tree");
+    }
+    FWN_CUDA_CHECK(cudaEventRecord(ev1, st));
+    FWN_CUDA_CHECK(cudaMemcpyAsync(e.meshes_h, e.meshes, nmeshes * sizeof(MeshInfo),
+                                   cudaMemcpyDeviceToHost, st));
+    FWN_CUDA_CHECK(cudaStreamSynchronize(st));
+    float ms = 0.f;
+    FWN_CUDA_CHECK(cudaEventElapsedTime(&ms, ev0, ev1));
+    e.build_ms = ms;
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
+    e.device_bytes = (int64_t)e.num_nodes * ((e.nodes32 ? sizeof(NodeF32) : 0) +
+                                             (e.nodes64 ? sizeof(NodeF64) : 0) +
+                                             (e.stage ? sizeof(StageRec) : 0)) +
+                     (int64_t)nf * (sizeof(TriF32) + sizeof(int)) + nmeshes * sizeof(MeshInfo);
+}
+
+}  // namespace fwn

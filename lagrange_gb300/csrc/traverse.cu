@@ -1,0 +1,541 @@
+// Winding-number traversal (replaces UT_SolidAngle::computeSolidAngle, called per point at
+// modules/winding/src/FastWindingNumber.cpp:66 and :75).
+//
+// Tree walk: nodes are in DFS pre-order with escape links, so the walk is stackless:
+//   far  (|P-q| > beta*r)      -> add the order-2 Taylor term, jump to skip
+//   near leaf                   -> add exact triangle solid angles, jump to skip
+//   near internal               -> step to i+1 (the first child)
+// The cursor strictly increases, so every walk ends in at most num_nodes steps.
+//
+// Forms:
+//   mixed / thread : one thread per query, FP32 far field and near field with a Kahan sum;
+//                    far tests inside a 1e-5 guard band are re-decided with the exact FP64
+//                    expression the FP64 form uses (so both forms take identical branches);
+//                    triangles within tau = fp64_near_scale * bbox diagonal get det and the
+//                    Van Oosterom denominator in FP64.
+//   mixed / warp   : 32 queries share one cursor (warp-uniform node loads, lanes inactive until
+//                    the cursor reaches their own resume index); the leaf's triangles are staged
+//                    in shared memory once per warp.
+//   fp64           : the plain comparison form, FP64 everywhere (including atan2).
+#include <climits>
+#include <cmath>
+
+#include "fwn_internal.cuh"
+
+namespace fwn {
+namespace {
+
+constexpr double TWO_PI_D = 6.283185307179586476925286766559;  // Omega/(4 pi) > 0.5 <=> Omega > 2 pi
+constexpr float GUARD = 1e-5f;
+
+struct QCounters {
+    unsigned nodes = 0, far = 0, tri = 0, tri64 = 0, test64 = 0;
+};
+
+__device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
+    const float y = x - c;
+    const float t = s + y;
+    c = (t - s) - y;
+    s = t;
+}
+
+// Exact-order FP64 far test shared by the mixed and FP64 forms (P, r are float values).
+__device__ __forceinline__ bool far_test_f64(double qx, double qy, double qz, double px,
+                                             double py, double pz, double r, double beta) {
+    const double dx = __dsub_rn(px, qx), dy = __dsub_rn(py, qy), dz = __dsub_rn(pz, qz);
+    const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    const double br = __dmul_rn(beta, r);
+    return d2 > __dmul_rn(br, br);
+}
+
+// Order-2 far-field term of a node (coefficients pre-scaled, see NodeF32), d = P - q.
+__device__ __forceinline__ float taylor_f32(const float4 m0, const float4 m1, const float4 m2,
+                                            const float4 m3, const float4 m4, const float4 m5,
+                                            float dx, float dy, float dz, float d2, float trM1) {
+    const float rinv = rsqrtf(d2);
+    const float rinv2 = rinv * rinv;
+    const float rinv3 = rinv * rinv2;
+    const float xx = dx * dx, yy = dy * dy, zz = dz * dz;
+    const float xy = dx * dy, xz = dx * dz, yz = dy * dz;
+    const float t0 = fmaf(dx, m0.x, fmaf(dy, m0.y, fmaf(dz, m0.z, trM1)));
+    float t1 = m0.w * dx;
+    t1 = fmaf(m1.x, dy, t1);
+    t1 = fmaf(m1.y, dz, t1);
+    t1 = fmaf(m1.z, xx, t1);
+    t1 = fmaf(m1.w, yy, t1);
+    t1 = fmaf(m2.x, zz, t1);
+    t1 = fmaf(m2.y, xy, t1);
+    t1 = fmaf(m2.z, xz, t1);
+    t1 = fmaf(m2.w, yz, t1);
+    const float gx = fmaf(m3.x, dx, fmaf(m3.w, dy, m4.x * dz));  // xxx xxy xxz
+    const float gy = fmaf(m4.y, dx, fmaf(m3.y, dy, m4.z * dz));  // xyy yyy yyz
+    const float gz = fmaf(m4.w, dx, fmaf(m5.x, dy, m3.z * dz));  // xzz yzz zzz
+    const float t2 = fmaf(xx, gx, fmaf(yy, gy, fmaf(zz, gz, m5.y * xy * dz)));
+    return rinv3 * fmaf(rinv2, fmaf(rinv2, t2, t1), t0);
+}
+
+__device__ __forceinline__ double taylor_f64(const NodeF64* __restrict__ nd, double dx, double dy,
+                                             double dz, double d2) {
+    const double rinv = 1.0 / sqrt(d2);
+    const double rinv2 = rinv * rinv;
+    const double rinv3 = rinv * rinv2;
+    const double xx = dx * dx, yy = dy * dy, zz = dz * dz;
+    const double xy = dx * dy, xz = dx * dz, yz = dy * dz;
+    const double t0 = dx * nd->N[0] + dy * nd->N[1] + dz * nd->N[2] + nd->trM1;
+    const double t1 = nd->W[0] * dx + nd->W[1] * dy + nd->W[2] * dz + nd->C[0] * xx +
+                      nd->C[1] * yy + nd->C[2] * zz + nd->C[3] * xy + nd->C[4] * xz +
+                      nd->C[5] * yz;
+    const double* D = nd->D;  // xxx yyy zzz xxy xxz xyy yyz xzz yzz xyz
+    const double t2 = xx * (D[0] * dx + D[3] * dy + D[4] * dz) +
+                      yy * (D[5] * dx + D[1] * dy + D[6] * dz) +
+                      zz * (D[7] * dx + D[8] * dy + D[2] * dz) + D[9] * xy * dz;
+    return rinv3 * (t0 + rinv2 * (t1 + rinv2 * t2));
+}
+
+// Van Oosterom & Strackee (1983): tan(Omega/2) = a.(b x c) /
+//   (|a||b||c| + (a.b)|c| + (b.c)|a| + (c.a)|b|),  a,b,c = vertices - q.
+// A query on a vertex, or in the triangle's plane (det == 0), contributes 0.
+__device__ __forceinline__ double tri_omega_f64(double ax, double ay, double az, double bx,
+                                                double by, double bz, double cx, double cy,
+                                                double cz) {
+    const double la = sqrt(ax * ax + ay * ay + az * az);
+    const double lb = sqrt(bx * bx + by * by + bz * bz);
+    const double lc = sqrt(cx * cx + cy * cy + cz * cz);
+    if (la == 0.0 || lb == 0.0 || lc == 0.0) return 0.0;
+    const double det = ax * (by * cz - bz * cy) + ay * (bz * cx - bx * cz) + az * (bx * cy - by * cx);
+    if (det == 0.0) return 0.0;
+    const double D = la * lb * lc + (ax * bx + ay * by + az * bz) * lc +
+                     (bx * cx + by * cy + bz * cz) * la + (cx * ax + cy * ay + cz * az) * lb;
+    return 2.0 * atan2(det, D);
+}
+
+// Mixed-form near field in FP64: det and the denominator in FP64 (the cancellation-prone part),
+// then atan2 in FP32 on the exponent-normalised pair (atan2 is well conditioned in its inputs).
+__device__ __noinline__ float tri_omega_near64(float v0x, float v0y, float v0z, float v1x,
+                                               float v1y, float v1z, float v2x, float v2y,
+                                               float v2z, float qx, float qy, float qz) {
+    const double ax = (double)v0x - (double)qx, ay = (double)v0y - (double)qy,
+                 az = (double)v0z - (double)qz;
+    const double bx = (double)v1x - (double)qx, by = (double)v1y - (double)qy,
+                 bz = (double)v1z - (double)qz;
+    const double cx = (double)v2x - (double)qx, cy = (double)v2y - (double)qy,
+                 cz = (double)v2z - (double)qz;
+    const double la = sqrt(ax * ax + ay * ay + az * az);
+    const double lb = sqrt(bx * bx + by * by + bz * bz);
+    const double lc = sqrt(cx * cx + cy * cy + cz * cz);
+    if (la == 0.0 || lb == 0.0 || lc == 0.0) return 0.f;
+    const double det = ax * (by * cz - bz * cy) + ay * (bz * cx - bx * cz) + az * (bx * cy - by * cx);
+    if (det == 0.0) return 0.f;
+    const double D = la * lb * lc + (ax * bx + ay * by + az * bz) * lc +
+                     (bx * cx + by * cy + bz * cz) * la + (cx * ax + cy * ay + cz * az) * lb;
+    const double m = fmax(fabs(det), fabs(D));
+    const int ex = max(-1000, min(1000, ((__double2hiint(m) >> 20) & 0x7ff) - 1023));
+    const double sc = __hiloint2double((1023 - ex) << 20, 0);  // 2^-ex, exact scaling
+    return 2.0f * atan2f((float)(det * sc), (float)(D * sc));
+}
+
+template <bool STATS>
+__device__ __forceinline__ float tri_omega_mixed(float v0x, float v0y, float v0z, float v1x,
+                                                 float v1y, float v1z, float v2x, float v2y,
+                                                 float v2z, float rt, float inv_nlen, float qx,
+                                                 float qy, float qz, float tau, QCounters& qc) {
+    const float ax = v0x - qx, ay = v0y - qy, az = v0z - qz;
+    const float bx = v1x - qx, by = v1y - qy, bz = v1z - qz;
+    const float cx = v2x - qx, cy = v2y - qy, cz = v2z - qz;
+    const float det = ax * (by * cz - bz * cy) + ay * (bz * cx - bx * cz) + az * (bx * cy - by * cx);
+    // lower bound of dist(q, triangle): max(plane distance, centroid distance - Rt)
+    const float h = fabsf(det) * inv_nlen;
+    const float sx = ax + bx + cx, sy = ay + by + cy, sz = az + bz + cz;
+    const float dc = sqrtf(sx * sx + sy * sy + sz * sz) * (1.0f / 3.0f);
+    if (h < tau && dc - rt < tau) {
+        if (STATS) ++qc.tri64;
+        return tri_omega_near64(v0x, v0y, v0z, v1x, v1y, v1z, v2x, v2y, v2z, qx, qy, qz);
+    }
+    const float la = sqrtf(ax * ax + ay * ay + az * az);
+    const float lb = sqrtf(bx * bx + by * by + bz * bz);
+    const float lc = sqrtf(cx * cx + cy * cy + cz * cz);
+    if (la == 0.f || lb == 0.f || lc == 0.f || det == 0.f) return 0.f;
+    const float D = la * lb * lc + (ax * bx + ay * by + az * bz) * lc +
+                    (bx * cx + by * cy + bz * cz) * la + (cx * ax + cy * ay + cz * az) * lb;
+    return 2.0f * atan2f(det, D);
+}
+
+__device__ __forceinline__ void flush_stats(const QCounters& c, unsigned long long* stats) {
+    // warp-aggregated: all lanes of the warp call this (no early exits in STATS kernels)
+    unsigned v[5] = {c.nodes, c.far, c.tri, c.tri64, c.test64};
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        unsigned s = __reduce_add_sync(0xffffffffu, v[i]);
+        if ((threadIdx.x & 31) == 0 && s) atomicAdd(&stats[i], (unsigned long long)s);
+    }
+}
+
+// ---- mixed, one thread per query --------------------------------------------------------------
+template <bool STATS>
+__global__ void __launch_bounds__(256)
+k_query_thread(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
+               const MeshInfo mi, const float* __restrict__ Q, const uint32_t* __restrict__ order,
+               int64_t n, float beta, float* __restrict__ omega, uint8_t* __restrict__ inside,
+               unsigned* __restrict__ status, unsigned long long* __restrict__ stats) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = k < n;
+    if (!STATS && !valid) return;
+    QCounters qc;
+    if (valid) {
+        const int64_t qi = order ? (int64_t)order[k] : k;
+        const float qx = Q[3 * qi], qy = Q[3 * qi + 1], qz = Q[3 * qi + 2];
+        const double qxd = qx, qyd = qy, qzd = qz;
+        float s = 0.f, c = 0.f;
+        int i = mi.root;
+        const int end = mi.end;
+        const float tau = mi.tau;
+        while (i < end) {
+            const NodeF32* nd = nodes + i;
+            const float4 a = __ldg(&nd->s0);
+            const int4 b = __ldg(reinterpret_cast<const int4*>(&nd->skip));
+            const float dx = a.x - qx, dy = a.y - qy, dz = a.z - qz;
+            const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            const float br = beta * a.w;
+            const float br2 = br * br;
+            bool far = d2 > br2;
+            if (fabsf(d2 - br2) <= GUARD * br2) {
+                far = far_test_f64(qxd, qyd, qzd, a.x, a.y, a.z, a.w, beta);
+                if (STATS) ++qc.test64;
+            }
+            if (STATS) ++qc.nodes;
+            int next;
+            if (far) {
+                const float t = taylor_f32(__ldg(&nd->m0), __ldg(&nd->m1), __ldg(&nd->m2),
+                                           __ldg(&nd->m3), __ldg(&nd->m4), __ldg(&nd->m5), dx, dy,
+                                           dz, d2, __int_as_float(b.w));
+                kahan_add(s, c, t);
+                if (STATS) ++qc.far;
+                next = b.x;
+            } else if (b.z > 0) {
+                const TriF32* T = tris + b.y;
+                for (int t = 0; t < b.z; ++t) {
+                    const float4 t0 = __ldg(&T[t].t0), t1 = __ldg(&T[t].t1), t2 = __ldg(&T[t].t2);
+                    const float w = tri_omega_mixed<STATS>(t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z,
+                                                           t1.w, t2.x, t2.y, t2.z, qx, qy, qz, tau, qc);
+                    kahan_add(s, c, w);
+                }
+                if (STATS) qc.tri += b.z;
+                next = b.x;
+            } else {
+                next = i + 1;
+            }
+            if (next <= i) {
+                atomicOr(status, ST_BAD_LINK);
+                break;
+            }
+            i = next;
+        }
+        const float res = s - c;
+        if (omega) omega[qi] = res;
+        if (inside) inside[qi] = (double)res > TWO_PI_D ? 1 : 0;
+    }
+    if (STATS) flush_stats(qc, stats);
+}
+
+// ---- mixed, warp-shared cursor ------------------------------------------------------------------
+constexpr int WARP_LEAF_MAX = 16;
+
+template <bool STATS>
+__global__ void __launch_bounds__(128)
+k_query_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
+             const MeshInfo mi, const float* __restrict__ Q, const uint32_t* __restrict__ order,
+             int64_t n, float beta, float* __restrict__ omega, uint8_t* __restrict__ inside,
+             unsigned* __restrict__ status, unsigned long long* __restrict__ stats) {
+    __shared__ float4 leafbuf[128 / 32][WARP_LEAF_MAX * 3];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t warp_first = k - lane;
+    if (warp_first >= n) return;  // whole warp out of range (warp-uniform)
+    const bool valid = k < n;
+    QCounters qc;
+    float qx = 0.f, qy = 0.f, qz = 0.f;
+    int64_t qi = 0;
+    if (valid) {
+        qi = order ? (int64_t)order[k] : k;
+        qx = Q[3 * qi];
+        qy = Q[3 * qi + 1];
+        qz = Q[3 * qi + 2];
+    }
+    const double qxd = qx, qyd = qy, qzd = qz;
+    const float tau = mi.tau;
+    const int end = mi.end;
+    float s = 0.f, c = 0.f;
+    int resume = valid ? mi.root : INT_MAX;
+    int cursor = __reduce_min_sync(0xffffffffu, resume);
+    while (cursor < end) {
+        const NodeF32* nd = nodes + cursor;
+        const float4 a = __ldg(&nd->s0);
+        const int4 b = __ldg(reinterpret_cast<const int4*>(&nd->skip));
+        const bool active = resume == cursor;
+        bool need_leaf = false;
+        if (active) {
+            const float dx = a.x - qx, dy = a.y - qy, dz = a.z - qz;
+            const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+            const float br = beta * a.w;
+            const float br2 = br * br;
+            bool far = d2 > br2;
+            if (fabsf(d2 - br2) <= GUARD * br2) {
+                far = far_test_f64(qxd, qyd, qzd, a.x, a.y, a.z, a.w, beta);
+                if (STATS) ++qc.test64;
+            }
+            if (STATS) ++qc.nodes;
+            if (far) {
+                const float t = taylor_f32(__ldg(&nd->m0), __ldg(&nd->m1), __ldg(&nd->m2),
+                                           __ldg(&nd->m3), __ldg(&nd->m4), __ldg(&nd->m5), dx, dy,
+                                           dz, d2, __int_as_float(b.w));
+                kahan_add(s, c, t);
+                if (STATS) ++qc.far;
+                resume = b.x;
+            } else if (b.z > 0) {
+                need_leaf = true;
+                resume = b.x;
+            } else {
+                resume = cursor + 1;
+            }
+        }
+        if (__any_sync(0xffffffffu, need_leaf)) {
+            const int cnt = b.z;  // warp-uniform (same node for all lanes)
+            const float4* src = reinterpret_cast<const float4*>(tris + b.y);
+            for (int j = lane; j < 3 * cnt; j += 32) leafbuf[w][j] = __ldg(src + j);
+            __syncwarp();
+            if (need_leaf) {
+                for (int t = 0; t < cnt; ++t) {
+                    const float4 t0 = leafbuf[w][3 * t], t1 = leafbuf[w][3 * t + 1],
+                                 t2 = leafbuf[w][3 * t + 2];
+                    const float wv = tri_omega_mixed<STATS>(t0.x, t0.y, t0.z, t0.w, t1.x, t1.y,
+                                                            t1.z, t1.w, t2.x, t2.y, t2.z, qx, qy,
+                                                            qz, tau, qc);
+                    kahan_add(s, c, wv);
+                }
+                if (STATS) qc.tri += cnt;
+            }
+            __syncwarp();
+        }
+        const int nc = __reduce_min_sync(0xffffffffu, resume);
+        if (nc <= cursor) {  // cannot happen for a well-formed tree
+            if (lane == 0) atomicOr(status, ST_BAD_LINK);
+            break;
+        }
+        cursor = nc;
+    }
+    if (valid) {
+        const float res = s - c;
+        if (omega) omega[qi] = res;
+        if (inside) inside[qi] = (double)res > TWO_PI_D ? 1 : 0;
+    }
+    if (STATS) flush_stats(qc, stats);
+}
+
+// ---- plain FP64 form ----------------------------------------------------------------------------
+template <bool STATS>
+__global__ void __launch_bounds__(128)
+k_query_f64(const NodeF64* __restrict__ nodes, const TriF32* __restrict__ tris, const MeshInfo mi,
+            const float* __restrict__ Q, const uint32_t* __restrict__ order, int64_t n,
+            float beta, float* __restrict__ omega, uint8_t* __restrict__ inside,
+            double* __restrict__ omega64, unsigned* __restrict__ status,
+            unsigned long long* __restrict__ stats) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = k < n;
+    if (!STATS && !valid) return;
+    QCounters qc;
+    if (valid) {
+        const int64_t qi = order ? (int64_t)order[k] : k;
+        const double qx = Q[3 * qi], qy = Q[3 * qi + 1], qz = Q[3 * qi + 2];
+        const double betad = beta;
+        double s = 0.0;
+        int i = mi.root;
+        const int end = mi.end;
+        while (i < end) {
+            const NodeF64* nd = nodes + i;
+            const double px = nd->P[0], py = nd->P[1], pz = nd->P[2];
+            const bool far = far_test_f64(qx, qy, qz, px, py, pz, nd->r, betad);
+            if (STATS) ++qc.nodes;
+            int next;
+            const int skip = nd->skip, tc = nd->tri_count;
+            if (far) {
+                const double dx = px - qx, dy = py - qy, dz = pz - qz;
+                s += taylor_f64(nd, dx, dy, dz, dx * dx + dy * dy + dz * dz);
+                if (STATS) ++qc.far;
+                next = skip;
+            } else if (tc > 0) {
+                const TriF32* T = tris + nd->tri_begin;
+                for (int t = 0; t < tc; ++t) {
+                    const float4 t0 = T[t].t0, t1 = T[t].t1, t2 = T[t].t2;
+                    s += tri_omega_f64((double)t0.x - qx, (double)t0.y - qy, (double)t0.z - qz,
+                                       (double)t0.w - qx, (double)t1.x - qy, (double)t1.y - qz,
+                                       (double)t1.z - qx, (double)t1.w - qy, (double)t2.x - qz);
+                }
+                if (STATS) qc.tri += tc;
+                next = skip;
+            } else {
+                next = i + 1;
+            }
+            if (next <= i) {
+                atomicOr(status, ST_BAD_LINK);
+                break;
+            }
+            i = next;
+        }
+        const float res = (float)s;
+        if (omega) omega[qi] = res;
+        if (omega64) omega64[qi] = s;
+        if (inside) inside[qi] = (double)res > TWO_PI_D ? 1 : 0;
+    }
+    if (STATS) flush_stats(qc, stats);
+}
+
+// ---- query Morton keys -----------------------------------------------------------------------
+__device__ __forceinline__ unsigned spread3q(unsigned x) {
+    x &= 0x3ffu;
+    x = (x | (x << 16)) & 0x030000ffu;
+    x = (x | (x << 8)) & 0x0300f00fu;
+    x = (x | (x << 4)) & 0x030c30c3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+
+__global__ void k_query_keys(const float* __restrict__ Q, int64_t n, const MeshInfo mi,
+                             uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    unsigned code = 0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        // frame: mesh bbox grown by 25% per side
+        const float ext = mi.hi[a] - mi.lo[a];
+        const float lo = mi.lo[a] - 0.25f * ext;
+        const float inv = ext > 0.f ? 1.0f / (1.5f * ext) : 0.f;
+        const float u = (Q[3 * k + a] - lo) * inv * 1024.0f;
+        const int qv = u >= 0.f ? (int)fminf(u, 1023.0f) : 0;  // NaN -> 0
+        code |= spread3q((unsigned)qv) << (2 - a);
+    }
+    keys[k] = code;
+    vals[k] = (uint32_t)k;
+}
+
+__global__ void k_fill_zero(float* omega, uint8_t* inside, double* omega64, int64_t n) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    if (omega) omega[k] = 0.f;
+    if (inside) inside[k] = 0;
+    if (omega64) omega64[k] = 0.0;
+}
+
+inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
+
+}  // namespace
+
+QueryArgs resolve_query_args(const Engine& e, const fwn_query_opts* o) {
+    QueryArgs a;
+    a.precision = e.cfg.precision;
+    a.traversal = e.cfg.traversal;
+    a.block_size = e.cfg.block_size;
+    a.sort_queries = e.cfg.sort_queries;
+    a.beta = e.cfg.beta;
+    if (o) {
+        if (o->precision >= 0) a.precision = o->precision;
+        if (o->traversal >= 0) a.traversal = o->traversal;
+        if (o->block_size > 0) a.block_size = o->block_size;
+        if (o->sort_queries >= 0) a.sort_queries = o->sort_queries;
+        if (o->beta > 0.f) a.beta = o->beta;
+    }
+    if (a.precision != FWN_PRECISION_MIXED && a.precision != FWN_PRECISION_FP64)
+        throw Error(FWN_INVALID_ARG, "unknown precision");
+    if (a.traversal == FWN_TRAVERSAL_AUTO) a.traversal = FWN_TRAVERSAL_THREAD;
+    if (a.traversal != FWN_TRAVERSAL_THREAD && a.traversal != FWN_TRAVERSAL_WARP)
+        throw Error(FWN_INVALID_ARG, "unknown traversal");
+    if (a.block_size <= 0) a.block_size = 128;
+    if (a.block_size % 32 != 0 || a.block_size > 1024)
+        throw Error(FWN_INVALID_ARG, "block_size must be a multiple of 32 and <= 1024");
+    if (a.traversal == FWN_TRAVERSAL_WARP) a.block_size = 128;
+    if (!(a.beta > 0.f) || !std::isfinite(a.beta)) throw Error(FWN_INVALID_ARG, "beta must be > 0");
+    return a;
+}
+
+void query_mesh(const Engine& e, int mesh, const QueryArgs& a, const float* d_points, int64_t n,
+                float* d_omega, uint8_t* d_inside, double* d_omega64, fwn_query_stats* stats,
+                cudaStream_t st, bool check) {
+    if (n <= 0) return;
+    if (a.precision == FWN_PRECISION_FP64 && !e.nodes64 && e.num_nodes > 0)
+        throw Error(FWN_INVALID_ARG, "engine was built without FP64 records (FWN_RECORDS_F64)");
+    if (a.precision == FWN_PRECISION_MIXED && !e.nodes32 && e.num_nodes > 0)
+        throw Error(FWN_INVALID_ARG, "engine was built without FP32 records (FWN_RECORDS_F32)");
+    if (d_omega64 && a.precision != FWN_PRECISION_FP64)
+        throw Error(FWN_INVALID_ARG, "FP64 solid-angle output needs the FP64 form");
+    const MeshInfo& mi = e.meshes_h[mesh];
+    Scratch status(sizeof(unsigned) + 8 * sizeof(unsigned long long), st);
+    unsigned* d_status = status.as<unsigned>();
+    unsigned long long* d_stats = reinterpret_cast<unsigned long long*>(status.as<char>() + 8);
+    FWN_CUDA_CHECK(cudaMemsetAsync(status.p, 0, sizeof(unsigned) + 8 * sizeof(unsigned long long), st));
+    if (mi.root < 0) {
+        k_fill_zero<<<grid_for(n, 256), 256, 0, st>>>(d_omega, d_inside, d_omega64, n);
+        FWN_CUDA_CHECK(cudaGetLastError());
+        if (stats) *stats = fwn_query_stats{0, 0, 0, 0, 0};
+        return;
+    }
+    const uint32_t* order = nullptr;
+    const bool do_sort = a.sort_queries && n > 1;
+    Scratch sortbuf(do_sort ? 4 * (size_t)n * sizeof(uint32_t) + radix_sort_temp_bytes(n, 4) + 256 : 0, st);
+    if (do_sort) {
+        uint32_t* ka = sortbuf.as<uint32_t>();
+        uint32_t* va = ka + n;
+        uint32_t* kb = va + n;
+        uint32_t* vb = kb + n;
+        void* tmp = vb + n;
+        k_query_keys<<<grid_for(n, 256), 256, 0, st>>>(d_points, n, mi, ka, va);
+        const bool in_b = radix_sort_u32(ka, va, kb, vb, n, 30, tmp, st);
+        order = in_b ? vb : va;
+    }
+    const bool want_stats = stats != nullptr;
+    const int bs = a.block_size;
+    if (a.precision == FWN_PRECISION_FP64) {
+        if (want_stats)
+            k_query_f64<true><<<grid_for(n, 128), 128, 0, st>>>(e.nodes64, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_omega64, d_status, d_stats);
+        else
+            k_query_f64<false><<<grid_for(n, 128), 128, 0, st>>>(e.nodes64, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_omega64, d_status, d_stats);
+    } else if (a.traversal == FWN_TRAVERSAL_WARP) {
+        if (want_stats)
+            k_query_warp<true><<<grid_for(n, 128), 128, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, d_stats);
+        else
+            k_query_warp<false><<<grid_for(n, 128), 128, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, d_stats);
+    } else {
+        if (want_stats)
+            k_query_thread<true><<<grid_for(n, bs), bs, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, d_stats);
+        else
+            k_query_thread<false><<<grid_for(n, bs), bs, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, d_stats);
+    }
+    FWN_CUDA_CHECK(cudaGetLastError());
+    if (want_stats || check) {
+        unsigned long long h[8];
+        unsigned sh = 0;
+        FWN_CUDA_CHECK(cudaMemcpyAsync(h, d_stats, sizeof(h), cudaMemcpyDeviceToHost, st));
+        FWN_CUDA_CHECK(cudaMemcpyAsync(&sh, d_status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        FWN_CUDA_CHECK(cudaStreamSynchronize(st));
+        if (stats) {
+            stats->nodes_tested = h[0];
+            stats->far_evals = h[1];
+            stats->tri_evals = h[2];
+            stats->tri_evals_fp64 = h[3];
+            stats->far_tests_fp64 = h[4];
+        }
+        if (sh & ST_BAD_LINK) throw Error(FWN_INTERNAL, "traversal met a non-advancing skip link");
+    }
+}
+
+void query_forest(const Engine& e, const QueryArgs& a, const float* d_points,
+                  const int64_t* query_offsets, float* d_omega, uint8_t* d_inside,
+                  cudaStream_t st) {
+    for (int64_t m = 0; m < e.nmeshes; ++m) {
+        const int64_t q0 = query_offsets[m], q1 = query_offsets[m + 1];
+        if (q1 <= q0) continue;
+        query_mesh(e, (int)m, a, d_points + 3 * q0, q1 - q0, d_omega ? d_omega + q0 : nullptr,
+                   d_inside ? d_inside + q0 : nullptr, nullptr, nullptr, st);
+    }
+}
+
+}  // namespace fwn

@@ -1,0 +1,84 @@
+"""C-ABI surface without a GPU: the library loads, exports every entry point declared in
+include/fwn_gb300.h, and rejects invalid arguments before touching the device."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import lagrange_gb300 as fwn
+
+HEADER = Path(__file__).resolve().parent.parent / "include" / "fwn_gb300.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"FWN_API\s+[\w\s\*]+?\b(fwn_\w+)\s*\(", text)))
+
+
+def test_header_declares_expected_entry_points():
+    names = declared_functions()
+    assert set(fwn.EXPORTS) == set(names), (set(fwn.EXPORTS) ^ set(names))
+
+
+def test_library_exports_every_declared_symbol(engine_lib):
+    for name in declared_functions():
+        assert hasattr(engine_lib, name), name
+    assert engine_lib.fwn_version().decode().endswith("sm_103a")
+
+
+def test_config_defaults(engine_lib):
+    c = fwn.config_default()
+    assert c.beta == 2.0 and c.leaf_size == 4 and c.sort_queries == 1
+    assert c.records == fwn.RECORDS_F32 and c.precision == fwn.PRECISION_MIXED
+    assert abs(c.fp64_near_scale - 1e-3) < 1e-9
+
+
+def _build_status(V, nv, F, nf, cfg=None):
+    h = C.c_void_p()
+    st = fwn.library().fwn_build(V, nv, F, nf, C.byref(cfg) if cfg is not None else None,
+                                 C.byref(h))
+    buf = C.create_string_buffer(256)
+    fwn.library().fwn_last_error(buf, 256)
+    return st, buf.value.decode(), h
+
+
+def test_invalid_arguments_rejected_on_host(engine_lib):
+    st, msg, h = _build_status(None, -1, None, 0)
+    assert st == 1 and "sizes" in msg and not h.value
+    st, msg, _ = _build_status(None, 3, None, 0)
+    assert st == 1 and "vertices pointer" in msg
+    V = np.zeros((3, 3), np.float32)
+    st, msg, _ = _build_status(V.ctypes.data_as(C.c_void_p), 3, None, 1)
+    assert st == 1 and "triangles pointer" in msg
+    for field, val, frag in (("beta", 0.0, "beta"), ("leaf_size", 17, "leaf_size"),
+                             ("leaf_size", 0, "leaf_size"), ("records", 4, "records"),
+                             ("block_size", 48, "block_size"), ("precision", 7, "precision"),
+                             ("fp64_near_scale", -1.0, "fp64_near_scale")):
+        cfg = fwn.config_default(**{field: val})
+        st, msg, _ = _build_status(V.ctypes.data_as(C.c_void_p), 3, None, 0, cfg)
+        assert st == 1 and frag in msg, (field, msg)
+
+
+def test_null_handle_is_not_built(engine_lib):
+    st = engine_lib.fwn_query_host(None, None, 0, None, None)
+    assert st == 6
+    eng = fwn.FastWindingNumber()
+    with pytest.raises(fwn.WindingError) as e:
+        eng.solid_angle(np.zeros(3, np.float32))
+    assert e.value.status == 6
+
+
+def test_last_error_truncates(engine_lib):
+    _build_status(None, -1, None, 0)
+    buf = C.create_string_buffer(4)
+    n = engine_lib.fwn_last_error(buf, 4)
+    assert n > 3 and len(buf.value) == 3
+
+
+def test_host_mesh_validation():
+    with pytest.raises(fwn.WindingError, match="3D"):
+        fwn.FastWindingNumber(np.zeros((4, 2), np.float32), np.zeros((1, 3), np.int32))
+    with pytest.raises(fwn.WindingError, match="triangle"):
+        fwn.FastWindingNumber(np.zeros((4, 3), np.float32), np.zeros((1, 4), np.int32))

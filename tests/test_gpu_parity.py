@@ -1,0 +1,219 @@
+"""GPU parity of the engine against the oracle, through the C ABI (ctypes).
+
+Tolerances (w = Omega / 4 pi):
+  * build topology / skip links / leaf ranges / triangle order / centres / radii: bit-exact
+    against the CPU restatement of the build (O3); FP64 moments within 1e-12 relative.
+  * plain FP64 form vs O3 FP64 traversal of the same tree: |dw| <= 1e-10.
+  * mixed form vs plain FP64 form (same tree, same beta): |dw| <= 1e-4 (the workload gate);
+    observed values are far smaller and are asserted at <= 2e-6 on these inputs.
+  * beta -> infinity (every triangle exact): FP64 form vs O1 brute force |dw| <= 1e-10,
+    mixed vs O1 |dw| <= 1e-5.
+  * is_inside agrees with the FP64 oracle on every point with |w - 0.5| > 1e-3.
+"""
+import math
+import threading
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import lagrange_gb300 as fwn
+from lagrange_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+GOLDEN = Path(__file__).resolve().parent / "golden"
+FOUR_PI = 4 * math.pi
+BOTH = fwn.RECORDS_F32 | fwn.RECORDS_F64
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    import torch
+    torch.cuda.set_device(0)
+    return torch
+
+
+def _q(eng, torch, Q, **kw):
+    res = eng.query(torch.from_numpy(np.ascontiguousarray(Q, np.float32)).cuda(), **kw)
+    torch.cuda.synchronize()
+    return [r.cpu().numpy() if hasattr(r, "cpu") else r for r in res]
+
+
+def _engine(V, F, **kw):
+    kw.setdefault("records", BOTH | fwn.RECORDS_MOMENTS)
+    return fwn.FastWindingNumber(V, F, **kw)
+
+
+@pytest.mark.parametrize("leaf", [1, 4, 7, 16])
+def test_build_matches_cpu_restatement(torch_cuda, oracle_mod, leaf):
+    g = np.load(GOLDEN / "displaced.npz")
+    eng = _engine(g["V"], g["F"], leaf_size=leaf)
+    got = eng.export_tree()
+    ref = oracle_mod.LbvhTree(g["V"], g["F"], leaf_size=leaf).export()
+    for k in ("skip", "tri_begin", "tri_count", "sorted_tri", "mesh_root"):
+        np.testing.assert_array_equal(got[k], ref[k], err_msg=k)
+    np.testing.assert_array_equal(got["center_radius"], ref["center_radius"])
+    m = eng.export_moments()
+    scale = np.max(np.abs(ref["moments"]), axis=0) + 1e-300
+    assert np.max(np.abs(m - ref["moments"]) / scale) <= 1e-12
+
+
+def test_golden_uv_sphere(torch_cuda, oracle_mod):
+    g = np.load(GOLDEN / "uv_sphere.npz")
+    eng = _engine(g["V"], g["F"])
+    w_mix, ins = _q(eng, torch_cuda, g["Q"])
+    w32, _, w64 = _q(eng, torch_cuda, g["Q"], precision=fwn.PRECISION_FP64, omega_f64=True)
+    np.testing.assert_allclose(w64, g["omega_lbvh_beta2"], rtol=0, atol=1e-10 * FOUR_PI)
+    assert np.max(np.abs(w_mix - w64)) / FOUR_PI <= 2e-6
+    we = g["omega_exact"] / FOUR_PI
+    band = np.abs(we - 0.5) > 1e-3
+    np.testing.assert_array_equal(ins[band].astype(bool), we[band] > 0.5)
+    np.testing.assert_array_equal(ins[band], g["inside_ref"][band])
+    # beta -> infinity: every triangle evaluated exactly
+    _, _, x64 = _q(eng, torch_cuda, g["Q"], precision=fwn.PRECISION_FP64, omega_f64=True, beta=1e30)
+    np.testing.assert_allclose(x64, g["omega_exact"], rtol=0, atol=1e-10 * FOUR_PI)
+    xm, _ = _q(eng, torch_cuda, g["Q"], beta=1e30)
+    assert np.max(np.abs(xm - g["omega_exact"])) / FOUR_PI <= 1e-5
+
+
+@pytest.mark.parametrize("leaf", [1, 4, 16])
+def test_displaced_near_surface(torch_cuda, oracle_mod, leaf):
+    g = np.load(GOLDEN / "displaced.npz")
+    eng = _engine(g["V"], g["F"], leaf_size=leaf)
+    ref = oracle_mod.LbvhTree(g["V"], g["F"], leaf_size=leaf).query_f64(g["Q"], beta=2.0)
+    _, _, w64 = _q(eng, torch_cuda, g["Q"], precision=fwn.PRECISION_FP64, omega_f64=True)
+    np.testing.assert_allclose(w64, ref, rtol=0, atol=1e-10 * FOUR_PI)
+    for trav in (fwn.TRAVERSAL_THREAD, fwn.TRAVERSAL_WARP):
+        wm, ins, st = _q(eng, torch_cuda, g["Q"], traversal=trav, stats=True)
+        assert np.max(np.abs(wm - w64)) / FOUR_PI <= 2e-6
+        assert st["tri_evals_fp64"] > 0      # near-surface queries use the FP64 near field
+        assert st["far_evals"] > 0 and st["nodes_tested"] >= st["far_evals"]
+    we = g["omega_exact"] / FOUR_PI
+    band = np.abs(we - 0.5) > 1e-3
+    _, ins = _q(eng, torch_cuda, g["Q"])
+    np.testing.assert_array_equal(ins[band].astype(bool), we[band] > 0.5)
+
+
+def test_schedules_and_sorting_bit_identical(torch_cuda):
+    wl = W.displaced_icosphere_workload(nu=40, n_queries=20000)
+    eng = _engine(wl.V, wl.F)
+    a, ia = _q(eng, torch_cuda, wl.Q, traversal=fwn.TRAVERSAL_THREAD)
+    b, ib = _q(eng, torch_cuda, wl.Q, traversal=fwn.TRAVERSAL_WARP)
+    c, ic = _q(eng, torch_cuda, wl.Q, sort_queries=0)
+    d, _ = _q(eng, torch_cuda, wl.Q, block_size=256)
+    np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(a, c)
+    np.testing.assert_array_equal(a, d)
+    np.testing.assert_array_equal(ia, ib)
+    np.testing.assert_array_equal(ia, ic)
+    # host (C-ABI copy-in/copy-out) path == device path
+    h, hi = eng.query(wl.Q)
+    np.testing.assert_array_equal(h, a)
+    np.testing.assert_array_equal(hi, ia)
+
+
+def test_edge_cases(torch_cuda, oracle_mod):
+    # empty mesh: Omega = 0 everywhere
+    e0 = fwn.FastWindingNumber(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.int32))
+    w, ins = e0.query(np.array([[0, 0, 0], [1, 2, 3]], np.float32))
+    assert np.all(w == 0) and np.all(ins == 0)
+    # single triangle, query on a vertex / in its plane / above
+    V = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    F = np.array([[0, 1, 2]], np.int32)
+    e1 = _engine(V, F)
+    Q = np.array([[1, 0, 0], [2, 2, 0], [0.25, 0.25, 1], [0.25, 0.25, -1]], np.float32)
+    w, _ = e1.query(Q)
+    ref = oracle_mod.brute_f64(V, F, Q)
+    assert np.all(np.isfinite(w))
+    np.testing.assert_allclose(w, ref, atol=1e-6)
+    # degenerate and duplicated triangles contribute as in the oracle
+    Vd, Fd = W.uv_sphere(16, 8)
+    Fd2 = np.concatenate([Fd, Fd[:5], [[0, 0, 1], [3, 3, 3]]]).astype(np.int32)
+    e2 = _engine(Vd, Fd2)
+    Q = np.random.default_rng(3).uniform(-1.5, 1.5, (2000, 3)).astype(np.float32)
+    _, _, w64 = _q(e2, torch_cuda, Q, precision=fwn.PRECISION_FP64, omega_f64=True)
+    np.testing.assert_allclose(w64, oracle_mod.LbvhTree(Vd, Fd2).query_f64(Q), atol=1e-9)
+    # zero queries
+    w, ins = e2.query(np.zeros((0, 3), np.float32))
+    assert len(w) == 0 and len(ins) == 0
+    # queries exactly on vertices: finite
+    w, _ = e2.query(Vd[:50])
+    assert np.all(np.isfinite(w))
+
+
+def test_invalid_meshes(torch_cuda):
+    V, F = W.uv_sphere(8, 4)
+    Fb = F.copy()
+    Fb[2, 2] = len(V)
+    with pytest.raises(fwn.WindingError, match="out of range") as e:
+        fwn.FastWindingNumber(V, Fb)
+    assert e.value.status == 1
+    Fn = F.copy()
+    Fn[0, 0] = -1
+    with pytest.raises(fwn.WindingError, match="out of range"):
+        fwn.FastWindingNumber(V, Fn)
+    Vn = V.copy()
+    Vn[F[4, 1], 2] = np.inf
+    with pytest.raises(fwn.WindingError, match="non-finite"):
+        fwn.FastWindingNumber(Vn, F)
+    # unreferenced NaN vertex is fine (not part of any triangle)
+    Vx = np.concatenate([V, [[np.nan, 0, 0]]]).astype(np.float32)
+    eng = fwn.FastWindingNumber(Vx, F)
+    w, ins = eng.query(np.zeros((1, 3), np.float32))
+    assert ins[0] == 1
+    # FP64 form on an engine without FP64 records
+    e32 = fwn.FastWindingNumber(V, F)
+    with pytest.raises(fwn.WindingError, match="FP64 records"):
+        e32.query(np.zeros((1, 3), np.float32), precision=fwn.PRECISION_FP64)
+
+
+def test_concurrent_queries_one_handle(torch_cuda):
+    wl = W.displaced_icosphere_workload(nu=20, n_queries=5000)
+    eng = _engine(wl.V, wl.F)
+    ref, _ = eng.query(wl.Q)
+    out = [None] * 8
+    errs = []
+
+    def run(i):
+        try:
+            out[i] = eng.query(wl.Q)[0]
+        except Exception as ex:  # pragma: no cover
+            errs.append(ex)
+
+    ts = [threading.Thread(target=run, args=(i,)) for i in range(8)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert not errs
+    for o in out:
+        np.testing.assert_array_equal(o, ref)
+
+
+def test_forest_matches_cpu_restatement(torch_cuda, oracle_mod):
+    fo = W.batched_forest_workload(n_meshes=9, seed=11, f_lo=100, f_hi=20000, q_lo=50, q_hi=3000)
+    # add an empty mesh in the middle
+    voff = np.insert(fo.voff, 4, fo.voff[4])
+    foff = np.insert(fo.foff, 4, fo.foff[4])
+    qoff = np.insert(fo.qoff, 4, fo.qoff[4])
+    forest = fwn.Forest(fo.V, voff, fo.F, foff, records=BOTH)
+    got = forest.export_tree()
+    lb = oracle_mod.LbvhTree(fo.V, fo.F, leaf_size=4, voff=voff, foff=foff)
+    ref = lb.export()
+    for k in ("skip", "tri_begin", "tri_count", "sorted_tri", "mesh_root"):
+        np.testing.assert_array_equal(got[k], ref[k], err_msg=k)
+    np.testing.assert_array_equal(got["center_radius"], ref["center_radius"])
+    import torch
+    Qd = torch.from_numpy(fo.Q).cuda()
+    w, ins = forest.query_forest(Qd, qoff)
+    w64, _ = forest.query_forest(Qd, qoff, precision=fwn.PRECISION_FP64)
+    torch.cuda.synchronize()
+    w, w64, ins = w.cpu().numpy(), w64.cpu().numpy(), ins.cpu().numpy()
+    qmesh = np.repeat(np.arange(len(qoff) - 1), np.diff(qoff)).astype(np.int32)
+    r = lb.query_f64(fo.Q, beta=2.0, qmesh=qmesh)
+    np.testing.assert_allclose(w64, r, rtol=0, atol=1e-6)  # float output of the FP64 form
+    assert np.max(np.abs(w - w64)) / FOUR_PI <= 2e-6
+    # closed meshes: inside flags match the FP64 oracle's
+    wr = r / FOUR_PI
+    band = np.abs(wr - 0.5) > 1e-3
+    np.testing.assert_array_equal(ins[band].astype(bool), wr[band] > 0.5)
