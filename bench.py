@@ -61,8 +61,8 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--nu", type=int, default=316)
     p.add_argument("--queries", type=int, default=10_000_000)
-    p.add_argument("--leaf", type=int, default=4)
-    p.add_argument("--traversal", default="thread", choices=["thread", "warp"])
+    p.add_argument("--leaf", type=int, default=8)
+    p.add_argument("--traversal", default="warp", choices=["thread", "warp"])
     p.add_argument("--block", type=int, default=128)
     p.add_argument("--fp64-steps", type=int, default=2)
     p.add_argument("--cpu-sample", type=int, default=100_000)

@@ -59,7 +59,7 @@ enum {
 
 /* Traversal schedules of the mixed form. */
 enum {
-    FWN_TRAVERSAL_AUTO = 0,   /* autotuned choice (thread schedule until tuned) */
+    FWN_TRAVERSAL_AUTO = 0,   /* autotuned choice (warp schedule until tuned) */
     FWN_TRAVERSAL_THREAD = 1, /* one thread per query, stackless skip-link walk */
     FWN_TRAVERSAL_WARP = 2    /* warp-shared cursor over 32 queries, leaf triangles in smem */
 };
@@ -73,14 +73,17 @@ enum {
 
 typedef struct fwn_config {
     float beta;            /* far-field accuracy scale: node is far if |q-P| > beta*r. Default 2 */
-    int32_t leaf_size;     /* max triangles per tree leaf, 1..16. Default 4 */
+    int32_t leaf_size;     /* max triangles per tree leaf, 1..16. Default 8 */
     int32_t records;       /* FWN_RECORDS_* mask. Default FWN_RECORDS_F32 */
     int32_t precision;     /* default query form, FWN_PRECISION_*. Default MIXED */
     int32_t traversal;     /* default schedule, FWN_TRAVERSAL_*. Default AUTO */
     int32_t block_size;    /* query kernel block size (multiple of 32, <= 1024); 0 = tuned */
     int32_t sort_queries;  /* 1: Morton-sort queries before traversal (default), 0: input order */
     float fp64_near_scale; /* FP64 near field if triangle is within scale*bbox_diagonal. 1e-3 */
-    int32_t reserved[8];
+    float fp64_cond;       /* ... and its FP32 evaluation is ill-conditioned: |a||b||c| >
+                              fp64_cond * |(det, D)|, or det is within rounding of 0 with D <= 0.
+                              0 = every triangle within the distance. Default 4 */
+    int32_t reserved[7];
 } fwn_config;
 
 /* Per-query options (override the handle's defaults; pass NULL for defaults). */
@@ -90,7 +93,8 @@ typedef struct fwn_query_opts {
     int32_t block_size;    /* 0 = handle default */
     int32_t sort_queries;  /* -1 = handle default */
     float beta;            /* <= 0: handle default */
-    int32_t reserved[7];
+    int32_t tuning;        /* schedule-specific variant for the autotuner (0 = default) */
+    int32_t reserved[6];
 } fwn_query_opts;
 
 /* Work counters of one query call (filled when a non-NULL pointer is passed to fwn_query_ex). */
@@ -100,6 +104,8 @@ typedef struct fwn_query_stats {
     uint64_t tri_evals;        /* exact triangle solid angles (all precisions) */
     uint64_t tri_evals_fp64;   /* of which evaluated in FP64 (mixed form only) */
     uint64_t far_tests_fp64;   /* far tests re-decided in FP64 inside the guard band */
+    uint64_t warp_steps;       /* node steps summed over warps (max over the warp's lanes);
+                                  nodes_tested / (32 * warp_steps) = lane utilisation */
 } fwn_query_stats;
 
 typedef struct fwn_info {

@@ -43,18 +43,19 @@ class fwn_config(C.Structure):
     _fields_ = [("beta", C.c_float), ("leaf_size", C.c_int32), ("records", C.c_int32),
                 ("precision", C.c_int32), ("traversal", C.c_int32), ("block_size", C.c_int32),
                 ("sort_queries", C.c_int32), ("fp64_near_scale", C.c_float),
-                ("reserved", C.c_int32 * 8)]
+                ("fp64_cond", C.c_float), ("reserved", C.c_int32 * 7)]
 
 
 class fwn_query_opts(C.Structure):
     _fields_ = [("precision", C.c_int32), ("traversal", C.c_int32), ("block_size", C.c_int32),
-                ("sort_queries", C.c_int32), ("beta", C.c_float), ("reserved", C.c_int32 * 7)]
+                ("sort_queries", C.c_int32), ("beta", C.c_float), ("tuning", C.c_int32),
+                ("reserved", C.c_int32 * 6)]
 
 
 class fwn_query_stats(C.Structure):
     _fields_ = [("nodes_tested", C.c_uint64), ("far_evals", C.c_uint64),
                 ("tri_evals", C.c_uint64), ("tri_evals_fp64", C.c_uint64),
-                ("far_tests_fp64", C.c_uint64)]
+                ("far_tests_fp64", C.c_uint64), ("warp_steps", C.c_uint64)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}
@@ -133,13 +134,15 @@ def config_default(**overrides) -> fwn_config:
     return c
 
 
-def _opts(precision=None, traversal=None, block_size=None, sort_queries=None, beta=None):
+def _opts(precision=None, traversal=None, block_size=None, sort_queries=None, beta=None,
+          tuning=None):
     o = fwn_query_opts()
     o.precision = -1 if precision is None else int(precision)
     o.traversal = -1 if traversal is None else int(traversal)
     o.block_size = 0 if block_size is None else int(block_size)
     o.sort_queries = -1 if sort_queries is None else int(sort_queries)
     o.beta = 0.0 if beta is None else float(beta)
+    o.tuning = 0 if tuning is None else int(tuning)
     return o
 
 

@@ -60,6 +60,8 @@ void validate_config(const fwn_config& c) {
         throw Error(FWN_INVALID_ARG, "block_size must be 0 or a multiple of 32 <= 1024");
     if (!(c.fp64_near_scale >= 0.f) || !std::isfinite(c.fp64_near_scale))
         throw Error(FWN_INVALID_ARG, "fp64_near_scale must be finite and >= 0");
+    if (!(c.fp64_cond >= 0.f) || !std::isfinite(c.fp64_cond))
+        throw Error(FWN_INVALID_ARG, "fp64_cond must be finite and >= 0");
 }
 
 struct OwnedStream {
@@ -114,13 +116,14 @@ FWN_API void fwn_config_default(fwn_config* c) {
     if (!c) return;
     std::memset(c, 0, sizeof(*c));
     c->beta = 2.0f;
-    c->leaf_size = 4;
+    c->leaf_size = 8;
     c->records = FWN_RECORDS_F32;
     c->precision = FWN_PRECISION_MIXED;
     c->traversal = FWN_TRAVERSAL_AUTO;
     c->block_size = 0;
     c->sort_queries = 1;
     c->fp64_near_scale = 1e-3f;
+    c->fp64_cond = 4.0f;
 }
 
 FWN_API size_t fwn_last_error(char* buf, size_t n) {

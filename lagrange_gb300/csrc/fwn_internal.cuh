@@ -79,7 +79,7 @@ struct MeshInfo {
     int root;          // first node of the mesh's subtree (-1: empty mesh)
     int end;           // escape index of the root (one past the subtree)
     float tau;         // FP64 near-field distance: fp64_near_scale * bbox diagonal
-    float pad;
+    float cond;        // FP64 near-field condition threshold (fwn_config::fp64_cond)
     float lo[3];       // vertex bbox
     float hi[3];
     float inv_ext[3];  // 1/(hi-lo) per axis (0 for flat axes), Morton normalisation
@@ -196,6 +196,7 @@ struct QueryArgs {
     int block_size = 128;
     int sort_queries = 1;
     float beta = 2.0f;
+    int tuning = 0;
 };
 // `check` (or a non-null `stats`) synchronises the stream and turns device status bits into
 // errors.

@@ -108,13 +108,14 @@ __global__ void k_init_bbox(unsigned* enc, int nmeshes) {
 }
 
 __global__ void k_mesh_info(const unsigned* __restrict__ enc, const int64_t* __restrict__ voff,
-                            int nmeshes, float near_scale, MeshInfo* __restrict__ mi) {
+                            int nmeshes, float near_scale, float cond,
+                            MeshInfo* __restrict__ mi) {
     int m = blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= nmeshes) return;
     MeshInfo r;
     r.root = -1;
     r.end = -1;
-    r.pad = 0.f;
+    r.cond = cond;
     r.pad2 = 0.f;
     const bool has = voff[m + 1] > voff[m];
     float diag2 = 0.f;
@@ -718,7 +719,8 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
         k_mesh_bbox<<<g, 256, 0, st>>>(d_V, voff, chunk, enc);
     }
     k_mesh_info<<<grid_for(nmeshes, 128), 128, 0, st>>>(enc, voff, (int)nmeshes,
-                                                        e.cfg.fp64_near_scale, e.meshes);
+                                                        e.cfg.fp64_near_scale, e.cfg.fp64_cond,
+                                                        e.meshes);
     FWN_CUDA_CHECK(cudaGetLastError());
 
     struct TmpList {  // stream-ordered frees on every exit path

@@ -28,8 +28,14 @@ namespace {
 constexpr double TWO_PI_D = 6.283185307179586476925286766559;  // Omega/(4 pi) > 0.5 <=> Omega > 2 pi
 constexpr float GUARD = 1e-5f;
 
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
 struct QCounters {
-    unsigned nodes = 0, far = 0, tri = 0, tri64 = 0, test64 = 0;
+    unsigned nodes = 0, far = 0, tri = 0, tri64 = 0, test64 = 0, steps = 0;
 };
 
 __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
@@ -138,25 +144,37 @@ template <bool STATS>
 __device__ __forceinline__ float tri_omega_mixed(float v0x, float v0y, float v0z, float v1x,
                                                  float v1y, float v1z, float v2x, float v2y,
                                                  float v2z, float rt, float inv_nlen, float qx,
-                                                 float qy, float qz, float tau, QCounters& qc) {
+                                                 float qy, float qz, float tau, float cond,
+                                                 QCounters& qc) {
     const float ax = v0x - qx, ay = v0y - qy, az = v0z - qz;
     const float bx = v1x - qx, by = v1y - qy, bz = v1z - qz;
     const float cx = v2x - qx, cy = v2y - qy, cz = v2z - qz;
     const float det = ax * (by * cz - bz * cy) + ay * (bz * cx - bx * cz) + az * (bx * cy - by * cx);
-    // lower bound of dist(q, triangle): max(plane distance, centroid distance - Rt)
-    const float h = fabsf(det) * inv_nlen;
-    const float sx = ax + bx + cx, sy = ay + by + cy, sz = az + bz + cz;
-    const float dc = sqrtf(sx * sx + sy * sy + sz * sz) * (1.0f / 3.0f);
-    if (h < tau && dc - rt < tau) {
-        if (STATS) ++qc.tri64;
-        return tri_omega_near64(v0x, v0y, v0z, v1x, v1y, v1z, v2x, v2y, v2z, qx, qy, qz);
-    }
     const float la = sqrtf(ax * ax + ay * ay + az * az);
     const float lb = sqrtf(bx * bx + by * by + bz * bz);
     const float lc = sqrtf(cx * cx + cy * cy + cz * cz);
-    if (la == 0.f || lb == 0.f || lc == 0.f || det == 0.f) return 0.f;
     const float D = la * lb * lc + (ax * bx + ay * by + az * bz) * lc +
                     (bx * cx + by * cy + bz * cz) * la + (cx * ax + cy * ay + cz * az) * lb;
+    // FP64 near field: the triangle is within tau of q (lower bound of the distance:
+    // max(plane distance, centroid distance - Rt)) AND its FP32 evaluation is ill-conditioned.
+    // The FP32 rounding errors of det and D are ~eps*|a||b||c| each, so the angle error is
+    // ~eps*kappa with kappa = |a||b||c| / |(det, D)|; and when D <= 0, a det within its rounding
+    // error may carry the wrong sign, i.e. the wrong side of atan2's branch cut (+-pi).
+    const float h = fabsf(det) * inv_nlen;
+    if (h < tau) {
+        const float sx = ax + bx + cx, sy = ay + by + cy, sz = az + bz + cz;
+        const float dc = sqrtf(sx * sx + sy * sy + sz * sz) * (1.0f / 3.0f);
+        if (dc - rt < tau) {
+            const float prod = la * lb * lc;
+            const bool ill = prod > cond * sqrtf(fmaf(det, det, D * D)) ||
+                             (D <= 0.f && fabsf(det) <= 1e-6f * prod);
+            if (ill) {
+                if (STATS) ++qc.tri64;
+                return tri_omega_near64(v0x, v0y, v0z, v1x, v1y, v1z, v2x, v2y, v2z, qx, qy, qz);
+            }
+        }
+    }
+    if (la == 0.f || lb == 0.f || lc == 0.f || det == 0.f) return 0.f;
     return 2.0f * atan2f(det, D);
 }
 
@@ -168,9 +186,68 @@ __device__ __forceinline__ void flush_stats(const QCounters& c, unsigned long lo
         unsigned s = __reduce_add_sync(0xffffffffu, v[i]);
         if ((threadIdx.x & 31) == 0 && s) atomicAdd(&stats[i], (unsigned long long)s);
     }
+    // warp steps: the warp runs as many steps as its longest lane (per-lane step counts) or
+    // as its shared cursor (all lanes hold the same count)
+    const unsigned ws = __reduce_max_sync(0xffffffffu, c.steps);
+    if ((threadIdx.x & 31) == 0 && ws) atomicAdd(&stats[5], (unsigned long long)ws);
+}
+
+// ---- 256-bit record loads ----------------------------------------------------------------------
+// A NodeF32 is four 32 B sectors: sector 0 = (P, r, skip, tri_begin, tri_count, trM1), sectors
+// 1-3 = far-field coefficients. One ld.global.nc.v8 per sector halves the load instructions (and
+// the L1 wavefronts when lanes sit on different nodes) compared with float4 loads.
+__device__ __forceinline__ void ld_v8(const void* p, float4& lo, float4& hi) {
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(lo.x), "=f"(lo.y), "=f"(lo.z), "=f"(lo.w), "=f"(hi.x), "=f"(hi.y), "=f"(hi.z),
+          "=f"(hi.w)
+        : "l"(p));
+}
+
+__device__ __forceinline__ void load_sector0(const NodeF32* nd, float4& a, int4& b) {
+    float4 h;
+    ld_v8(nd, a, h);
+    b = make_int4(__float_as_int(h.x), __float_as_int(h.y), __float_as_int(h.z),
+                  __float_as_int(h.w));
+}
+
+__device__ __forceinline__ float taylor_node(const NodeF32* nd, float dx, float dy, float dz,
+                                             float d2, float trM1) {
+    float4 m0, m1, m2, m3, m4, m5;
+    ld_v8(&nd->m0, m0, m1);
+    ld_v8(&nd->m2, m2, m3);
+    ld_v8(&nd->m4, m4, m5);
+    return taylor_f32(m0, m1, m2, m3, m4, m5, dx, dy, dz, d2, trM1);
+}
+
+// far test: FP32 decision, re-decided with the exact FP64 expression inside the guard band
+template <bool STATS>
+__device__ __forceinline__ bool far_test(const float4 a, float qx, float qy, float qz, float beta,
+                                         float& dx, float& dy, float& dz, float& d2,
+                                         QCounters& qc) {
+    dx = a.x - qx;
+    dy = a.y - qy;
+    dz = a.z - qz;
+    d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float br = beta * a.w;
+    const float br2 = br * br;
+    bool far = d2 > br2;
+    if (fabsf(d2 - br2) <= GUARD * br2) {
+        far = far_test_f64(qx, qy, qz, a.x, a.y, a.z, a.w, beta);
+        if (STATS) ++qc.test64;
+    }
+    if (STATS) ++qc.nodes;
+    return far;
 }
 
 // ---- mixed, one thread per query --------------------------------------------------------------
+// "Advance, then evaluate" rounds keep the warp converged on the two expensive blocks:
+//   1. every lane walks its own path through cheap near-internal steps until it reaches its next
+//      far node; near leaves met on the way are queued (two slots per lane) and skipped;
+//   2. the lanes holding a far node evaluate its Taylor term together;
+//   3. queued leaf triangles are evaluated in a batch once half the warp holds one (or a lane's
+//      slots are full, or a lane has finished its walk), one triangle per lane per iteration.
+constexpr int LEAF_BATCH = 16;
+
 template <bool STATS>
 __global__ void __launch_bounds__(256)
 k_query_thread(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
@@ -178,58 +255,96 @@ k_query_thread(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tri
                int64_t n, float beta, float* __restrict__ omega, uint8_t* __restrict__ inside,
                unsigned* __restrict__ status, unsigned long long* __restrict__ stats) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k - (threadIdx.x & 31) >= n) return;  // whole warp out of range (warp-uniform)
     const bool valid = k < n;
-    if (!STATS && !valid) return;
     QCounters qc;
+    int64_t qi = 0;
+    float qx = 0.f, qy = 0.f, qz = 0.f;
     if (valid) {
-        const int64_t qi = order ? (int64_t)order[k] : k;
-        const float qx = Q[3 * qi], qy = Q[3 * qi + 1], qz = Q[3 * qi + 2];
-        const double qxd = qx, qyd = qy, qzd = qz;
-        float s = 0.f, c = 0.f;
-        int i = mi.root;
-        const int end = mi.end;
-        const float tau = mi.tau;
+        qi = order ? (int64_t)order[k] : k;
+        qx = Q[3 * qi];
+        qy = Q[3 * qi + 1];
+        qz = Q[3 * qi + 2];
+    }
+    const int end = mi.end;
+    const float tau = mi.tau;
+    const float cond = mi.cond;
+    float s = 0.f, c = 0.f;
+    int i = valid ? mi.root : end;
+    int pb0 = 0, pc0 = 0, pb1 = 0, pc1 = 0;  // queued leaf triangle runs
+    bool bad = false;
+    while (true) {
+        bool far = false;
+        float dx = 0.f, dy = 0.f, dz = 0.f, d2 = 1.f, trM1 = 0.f;
+        int skipf = 0;
         while (i < end) {
-            const NodeF32* nd = nodes + i;
-            const float4 a = __ldg(&nd->s0);
-            const int4 b = __ldg(reinterpret_cast<const int4*>(&nd->skip));
-            const float dx = a.x - qx, dy = a.y - qy, dz = a.z - qz;
-            const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            const float br = beta * a.w;
-            const float br2 = br * br;
-            bool far = d2 > br2;
-            if (fabsf(d2 - br2) <= GUARD * br2) {
-                far = far_test_f64(qxd, qyd, qzd, a.x, a.y, a.z, a.w, beta);
-                if (STATS) ++qc.test64;
-            }
-            if (STATS) ++qc.nodes;
-            int next;
+            float4 a;
+            int4 b;
+            load_sector0(nodes + i, a, b);
+            far = far_test<STATS>(a, qx, qy, qz, beta, dx, dy, dz, d2, qc);
             if (far) {
-                const float t = taylor_f32(__ldg(&nd->m0), __ldg(&nd->m1), __ldg(&nd->m2),
-                                           __ldg(&nd->m3), __ldg(&nd->m4), __ldg(&nd->m5), dx, dy,
-                                           dz, d2, __int_as_float(b.w));
-                kahan_add(s, c, t);
-                if (STATS) ++qc.far;
-                next = b.x;
-            } else if (b.z > 0) {
-                const TriF32* T = tris + b.y;
-                for (int t = 0; t < b.z; ++t) {
-                    const float4 t0 = __ldg(&T[t].t0), t1 = __ldg(&T[t].t1), t2 = __ldg(&T[t].t2);
-                    const float w = tri_omega_mixed<STATS>(t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z,
-                                                           t1.w, t2.x, t2.y, t2.z, qx, qy, qz, tau, qc);
-                    kahan_add(s, c, w);
-                }
-                if (STATS) qc.tri += b.z;
-                next = b.x;
-            } else {
-                next = i + 1;
-            }
-            if (next <= i) {
-                atomicOr(status, ST_BAD_LINK);
+                trM1 = __int_as_float(b.w);
+                skipf = b.x;
                 break;
             }
-            i = next;
+            if (b.z > 0) {
+                if (pc0 == 0) {
+                    pb0 = b.y;
+                    pc0 = b.z;
+                } else if (pc1 == 0) {
+                    pb1 = b.y;
+                    pc1 = b.z;
+                } else {
+                    break;  // both slots full: stay on this leaf until the batch below runs
+                }
+                if (b.x <= i) {
+                    bad = true;
+                    i = end;
+                    break;
+                }
+                i = b.x;
+            } else {
+                i = i + 1;
+            }
         }
+        const bool blocked = (i < end) && !far;
+        if (far) {
+            kahan_add(s, c, taylor_node(nodes + i, dx, dy, dz, d2, trM1));
+            if (STATS) ++qc.far;
+            if (skipf <= i) {
+                bad = true;
+                i = end;
+            } else {
+                i = skipf;
+            }
+        }
+        if (STATS) ++qc.steps;
+        const bool pend = pc0 > 0;
+        const bool done = i >= end;
+        const unsigned pm = __ballot_sync(0xffffffffu, pend);
+        if (__any_sync(0xffffffffu, blocked || (done && pend)) || __popc(pm) >= LEAF_BATCH) {
+            while (__any_sync(0xffffffffu, pc0 > 0)) {
+                if (pc0 > 0) {
+                    const TriF32* T = tris + pb0;
+                    const float4 t0 = __ldg(&T->t0), t1 = __ldg(&T->t1), t2 = __ldg(&T->t2);
+                    const float w = tri_omega_mixed<STATS>(t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z,
+                                                           t1.w, t2.x, t2.y, t2.z, qx, qy, qz, tau,
+                                                           cond, qc);
+                    kahan_add(s, c, w);
+                    if (STATS) ++qc.tri;
+                    ++pb0;
+                    if (--pc0 == 0) {
+                        pb0 = pb1;
+                        pc0 = pc1;
+                        pc1 = 0;
+                    }
+                }
+            }
+        }
+        if (__all_sync(0xffffffffu, i >= end && pc0 == 0)) break;
+    }
+    if (bad) atomicOr(status, ST_BAD_LINK);
+    if (valid) {
         const float res = s - c;
         if (omega) omega[qi] = res;
         if (inside) inside[qi] = (double)res > TWO_PI_D ? 1 : 0;
@@ -238,19 +353,30 @@ k_query_thread(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tri
 }
 
 // ---- mixed, warp-shared cursor ------------------------------------------------------------------
+// 32 queries share one cursor over the DFS node order: the cursor is the smallest "resume" index
+// of the warp's lanes, and a lane takes part in a step only when the cursor equals its own resume
+// index. Node loads are therefore warp-uniform (one L1 wavefront each), while every lane still
+// visits exactly its own path, in DFS order (so the result does not depend on which queries share
+// the warp). The walk is software-pipelined: the next cursor is reduced right after the far test
+// and its 32 B test sector is loaded before this step's Taylor / leaf work, and the coefficient
+// sectors of the current node are requested before its far test.
+// Near leaves: the (query, triangle) pairs of the leaf under the cursor are spread over all 32
+// lanes (triangles staged in shared memory) and each owner adds its results in triangle order.
 constexpr int WARP_LEAF_MAX = 16;
+constexpr int WARP_BLOCK = 128;
 
-template <bool STATS>
-__global__ void __launch_bounds__(128)
+template <bool STATS, int MINB>
+__global__ void __launch_bounds__(WARP_BLOCK, MINB)
 k_query_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
              const MeshInfo mi, const float* __restrict__ Q, const uint32_t* __restrict__ order,
              int64_t n, float beta, float* __restrict__ omega, uint8_t* __restrict__ inside,
              unsigned* __restrict__ status, unsigned long long* __restrict__ stats) {
-    __shared__ float4 leafbuf[128 / 32][WARP_LEAF_MAX * 3];
+    __shared__ float4 leafbuf[WARP_BLOCK / 32][WARP_LEAF_MAX * 3];
+    __shared__ float4 qbuf[WARP_BLOCK / 32][32];
+    __shared__ float resbuf[WARP_BLOCK / 32][32 * WARP_LEAF_MAX];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t warp_first = k - lane;
-    if (warp_first >= n) return;  // whole warp out of range (warp-uniform)
+    if (k - lane >= n) return;  // whole warp out of range (warp-uniform)
     const bool valid = k < n;
     QCounters qc;
     float qx = 0.f, qy = 0.f, qz = 0.f;
@@ -261,35 +387,27 @@ k_query_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
         qy = Q[3 * qi + 1];
         qz = Q[3 * qi + 2];
     }
-    const double qxd = qx, qyd = qy, qzd = qz;
     const float tau = mi.tau;
+    const float cond = mi.cond;
     const int end = mi.end;
+    const unsigned lt = lanemask_lt();
     float s = 0.f, c = 0.f;
     int resume = valid ? mi.root : INT_MAX;
     int cursor = __reduce_min_sync(0xffffffffu, resume);
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+    int4 b = make_int4(0, 0, 0, 0);
+    if (cursor < end) load_sector0(nodes + cursor, a, b);
     while (cursor < end) {
         const NodeF32* nd = nodes + cursor;
-        const float4 a = __ldg(&nd->s0);
-        const int4 b = __ldg(reinterpret_cast<const int4*>(&nd->skip));
-        const bool active = resume == cursor;
-        bool need_leaf = false;
-        if (active) {
-            const float dx = a.x - qx, dy = a.y - qy, dz = a.z - qz;
-            const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            const float br = beta * a.w;
-            const float br2 = br * br;
-            bool far = d2 > br2;
-            if (fabsf(d2 - br2) <= GUARD * br2) {
-                far = far_test_f64(qxd, qyd, qzd, a.x, a.y, a.z, a.w, beta);
-                if (STATS) ++qc.test64;
-            }
-            if (STATS) ++qc.nodes;
+        float4 m0, m1, m2, m3, m4, m5;
+        ld_v8(&nd->m0, m0, m1);
+        ld_v8(&nd->m2, m2, m3);
+        ld_v8(&nd->m4, m4, m5);
+        bool far = false, need_leaf = false;
+        float dx = 0.f, dy = 0.f, dz = 0.f, d2 = 1.f;
+        if (resume == cursor) {
+            far = far_test<STATS>(a, qx, qy, qz, beta, dx, dy, dz, d2, qc);
             if (far) {
-                const float t = taylor_f32(__ldg(&nd->m0), __ldg(&nd->m1), __ldg(&nd->m2),
-                                           __ldg(&nd->m3), __ldg(&nd->m4), __ldg(&nd->m5), dx, dy,
-                                           dz, d2, __int_as_float(b.w));
-                kahan_add(s, c, t);
-                if (STATS) ++qc.far;
                 resume = b.x;
             } else if (b.z > 0) {
                 need_leaf = true;
@@ -298,30 +416,53 @@ k_query_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
                 resume = cursor + 1;
             }
         }
-        if (__any_sync(0xffffffffu, need_leaf)) {
-            const int cnt = b.z;  // warp-uniform (same node for all lanes)
+        const int nc = __reduce_min_sync(0xffffffffu, resume);
+        float4 an = a;
+        int4 bn = b;
+        if (nc < end) load_sector0(nodes + nc, an, bn);  // next step's test sector, in flight now
+        if (far) {
+            kahan_add(s, c, taylor_f32(m0, m1, m2, m3, m4, m5, dx, dy, dz, d2, __int_as_float(b.w)));
+            if (STATS) ++qc.far;
+        }
+        const unsigned lm = __ballot_sync(0xffffffffu, need_leaf);
+        if (lm) {
+            const int cnt = b.z;  // warp-uniform (same node for all lanes), <= WARP_LEAF_MAX
+            const int nl = __popc(lm);
             const float4* src = reinterpret_cast<const float4*>(tris + b.y);
             for (int j = lane; j < 3 * cnt; j += 32) leafbuf[w][j] = __ldg(src + j);
+            if (need_leaf) qbuf[w][__popc(lm & lt)] = make_float4(qx, qy, qz, 0.f);
             __syncwarp();
-            if (need_leaf) {
-                for (int t = 0; t < cnt; ++t) {
+            const int np = nl * cnt;
+            const float inv = 1.0f / (float)cnt;
+            for (int base = 0; base < np; base += 32) {
+                const int p = base + lane;
+                if (p < np) {
+                    const int r = (int)(((float)p + 0.5f) * inv);  // p = r * cnt + t
+                    const int t = p - r * cnt;
+                    const float4 qq = qbuf[w][r];
                     const float4 t0 = leafbuf[w][3 * t], t1 = leafbuf[w][3 * t + 1],
                                  t2 = leafbuf[w][3 * t + 2];
-                    const float wv = tri_omega_mixed<STATS>(t0.x, t0.y, t0.z, t0.w, t1.x, t1.y,
-                                                            t1.z, t1.w, t2.x, t2.y, t2.z, qx, qy,
-                                                            qz, tau, qc);
-                    kahan_add(s, c, wv);
+                    resbuf[w][p] = tri_omega_mixed<STATS>(t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z,
+                                                          t1.w, t2.x, t2.y, t2.z, qq.x, qq.y, qq.z,
+                                                          tau, cond, qc);
                 }
+            }
+            __syncwarp();
+            if (need_leaf) {
+                const int r = __popc(lm & lt);
+                for (int t = 0; t < cnt; ++t) kahan_add(s, c, resbuf[w][r * cnt + t]);
                 if (STATS) qc.tri += cnt;
             }
             __syncwarp();
         }
-        const int nc = __reduce_min_sync(0xffffffffu, resume);
         if (nc <= cursor) {  // cannot happen for a well-formed tree
             if (lane == 0) atomicOr(status, ST_BAD_LINK);
             break;
         }
+        if (STATS) ++qc.steps;
         cursor = nc;
+        a = an;
+        b = bn;
     }
     if (valid) {
         const float res = s - c;
@@ -354,7 +495,7 @@ k_query_f64(const NodeF64* __restrict__ nodes, const TriF32* __restrict__ tris, 
             const NodeF64* nd = nodes + i;
             const double px = nd->P[0], py = nd->P[1], pz = nd->P[2];
             const bool far = far_test_f64(qx, qy, qz, px, py, pz, nd->r, betad);
-            if (STATS) ++qc.nodes;
+            if (STATS) { ++qc.nodes; ++qc.steps; }
             int next;
             const int skip = nd->skip, tc = nd->tri_count;
             if (far) {
@@ -443,10 +584,11 @@ QueryArgs resolve_query_args(const Engine& e, const fwn_query_opts* o) {
         if (o->block_size > 0) a.block_size = o->block_size;
         if (o->sort_queries >= 0) a.sort_queries = o->sort_queries;
         if (o->beta > 0.f) a.beta = o->beta;
+        if (o->tuning > 0) a.tuning = o->tuning;
     }
     if (a.precision != FWN_PRECISION_MIXED && a.precision != FWN_PRECISION_FP64)
         throw Error(FWN_INVALID_ARG, "unknown precision");
-    if (a.traversal == FWN_TRAVERSAL_AUTO) a.traversal = FWN_TRAVERSAL_THREAD;
+    if (a.traversal == FWN_TRAVERSAL_AUTO) a.traversal = FWN_TRAVERSAL_WARP;
     if (a.traversal != FWN_TRAVERSAL_THREAD && a.traversal != FWN_TRAVERSAL_WARP)
         throw Error(FWN_INVALID_ARG, "unknown traversal");
     if (a.block_size <= 0) a.block_size = 128;
@@ -468,10 +610,12 @@ void query_mesh(const Engine& e, int mesh, const QueryArgs& a, const float* d_po
     if (d_omega64 && a.precision != FWN_PRECISION_FP64)
         throw Error(FWN_INVALID_ARG, "FP64 solid-angle output needs the FP64 form");
     const MeshInfo& mi = e.meshes_h[mesh];
-    Scratch status(sizeof(unsigned) + 8 * sizeof(unsigned long long), st);
+    // layout: [status u32 | pad to 8 B | 8 x u64 counters]
+    constexpr size_t kStatusBytes = 8 + 8 * sizeof(unsigned long long);
+    Scratch status(kStatusBytes, st);
     unsigned* d_status = status.as<unsigned>();
     unsigned long long* d_stats = reinterpret_cast<unsigned long long*>(status.as<char>() + 8);
-    FWN_CUDA_CHECK(cudaMemsetAsync(status.p, 0, sizeof(unsigned) + 8 * sizeof(unsigned long long), st));
+    FWN_CUDA_CHECK(cudaMemsetAsync(status.p, 0, kStatusBytes, st));
     if (mi.root < 0) {
         k_fill_zero<<<grid_for(n, 256), 256, 0, st>>>(d_omega, d_inside, d_omega64, n);
         FWN_CUDA_CHECK(cudaGetLastError());
@@ -499,10 +643,15 @@ void query_mesh(const Engine& e, int mesh, const QueryArgs& a, const float* d_po
         else
             k_query_f64<false><<<grid_for(n, 128), 128, 0, st>>>(e.nodes64, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_omega64, d_status, d_stats);
     } else if (a.traversal == FWN_TRAVERSAL_WARP) {
+        const dim3 g = grid_for(n, WARP_BLOCK);
+        // default: register cap of 64 (8 blocks = 32 warps per SM); tuning 2: no cap (more
+        // registers, fewer resident warps)
         if (want_stats)
-            k_query_warp<true><<<grid_for(n, 128), 128, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, d_stats);
+            k_query_warp<true, 1><<<g, WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, d_stats);
+        else if (a.tuning == 2)
+            k_query_warp<false, 1><<<g, WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, d_stats);
         else
-            k_query_warp<false><<<grid_for(n, 128), 128, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, d_stats);
+            k_query_warp<false, 8><<<g, WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, d_stats);
     } else {
         if (want_stats)
             k_query_thread<true><<<grid_for(n, bs), bs, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, d_stats);
@@ -522,6 +671,7 @@ void query_mesh(const Engine& e, int mesh, const QueryArgs& a, const float* d_po
             stats->tri_evals = h[2];
             stats->tri_evals_fp64 = h[3];
             stats->far_tests_fp64 = h[4];
+            stats->warp_steps = h[5];
         }
         if (sh & ST_BAD_LINK) throw Error(FWN_INTERNAL, "traversal met a non-advancing skip link");
     }

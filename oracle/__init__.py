@@ -134,7 +134,7 @@ class RefTree:
 class LbvhTree:
     """O3: CPU restatement of the device LBVH build and of the plain FP64 traversal."""
 
-    def __init__(self, V, F, leaf_size: int = 4, near_scale: float = 1e-3, voff=None, foff=None):
+    def __init__(self, V, F, leaf_size: int = 8, near_scale: float = 1e-3, voff=None, foff=None):
         self._V, self._F = _f32(V), _i32(F)
         if voff is None:
             voff = [0, len(self._V)]

@@ -30,7 +30,7 @@ def test_library_exports_every_declared_symbol(engine_lib):
 
 def test_config_defaults(engine_lib):
     c = fwn.config_default()
-    assert c.beta == 2.0 and c.leaf_size == 4 and c.sort_queries == 1
+    assert c.beta == 2.0 and c.leaf_size == 8 and c.sort_queries == 1
     assert c.records == fwn.RECORDS_F32 and c.precision == fwn.PRECISION_MIXED
     assert abs(c.fp64_near_scale - 1e-3) < 1e-9
 

@@ -60,7 +60,7 @@ def test_build_matches_cpu_restatement(torch_cuda, oracle_mod, leaf):
 
 def test_golden_uv_sphere(torch_cuda, oracle_mod):
     g = np.load(GOLDEN / "uv_sphere.npz")
-    eng = _engine(g["V"], g["F"])
+    eng = _engine(g["V"], g["F"], leaf_size=4)  # the fixture was made with leaf 4
     w_mix, ins = _q(eng, torch_cuda, g["Q"])
     w32, _, w64 = _q(eng, torch_cuda, g["Q"], precision=fwn.PRECISION_FP64, omega_f64=True)
     np.testing.assert_allclose(w64, g["omega_lbvh_beta2"], rtol=0, atol=1e-10 * FOUR_PI)
@@ -94,22 +94,32 @@ def test_displaced_near_surface(torch_cuda, oracle_mod, leaf):
     np.testing.assert_array_equal(ins[band].astype(bool), we[band] > 0.5)
 
 
-def test_schedules_and_sorting_bit_identical(torch_cuda):
+def test_schedules_and_sorting(torch_cuda):
+    """Every schedule computes the same terms; only the Kahan summation order may differ (both
+    schedules defer work in warp-dependent batches, so the Morton sort changes the order; the
+    block size does not change warp composition, so it changes nothing)."""
     wl = W.displaced_icosphere_workload(nu=40, n_queries=20000)
     eng = _engine(wl.V, wl.F)
     a, ia = _q(eng, torch_cuda, wl.Q, traversal=fwn.TRAVERSAL_THREAD)
     b, ib = _q(eng, torch_cuda, wl.Q, traversal=fwn.TRAVERSAL_WARP)
-    c, ic = _q(eng, torch_cuda, wl.Q, sort_queries=0)
-    d, _ = _q(eng, torch_cuda, wl.Q, block_size=256)
-    np.testing.assert_array_equal(a, b)
-    np.testing.assert_array_equal(a, c)
+    b2, _ = _q(eng, torch_cuda, wl.Q, traversal=fwn.TRAVERSAL_WARP, sort_queries=0)
+    b3, _ = _q(eng, torch_cuda, wl.Q, traversal=fwn.TRAVERSAL_WARP)
+    c, ic = _q(eng, torch_cuda, wl.Q, traversal=fwn.TRAVERSAL_THREAD, sort_queries=0)
+    d, _ = _q(eng, torch_cuda, wl.Q, traversal=fwn.TRAVERSAL_THREAD, block_size=256)
+    np.testing.assert_array_equal(b, b3)  # deterministic run to run
     np.testing.assert_array_equal(a, d)
-    np.testing.assert_array_equal(ia, ib)
-    np.testing.assert_array_equal(ia, ic)
-    # host (C-ABI copy-in/copy-out) path == device path
+    assert np.max(np.abs(b - b2)) / FOUR_PI <= 1e-6
+    assert np.max(np.abs(a - b)) / FOUR_PI <= 1e-6
+    assert np.max(np.abs(a - c)) / FOUR_PI <= 1e-6
+    w = a / FOUR_PI
+    band = np.abs(w - 0.5) > 1e-3
+    np.testing.assert_array_equal(ia[band], ib[band])
+    np.testing.assert_array_equal(ia[band], ic[band])
+    # host (C-ABI copy-in/copy-out) path == device path with the same defaults
+    dflt, idflt = _q(eng, torch_cuda, wl.Q)
     h, hi = eng.query(wl.Q)
-    np.testing.assert_array_equal(h, a)
-    np.testing.assert_array_equal(hi, ia)
+    np.testing.assert_array_equal(h, dflt)
+    np.testing.assert_array_equal(hi, idflt)
 
 
 def test_edge_cases(torch_cuda, oracle_mod):
@@ -196,9 +206,9 @@ def test_forest_matches_cpu_restatement(torch_cuda, oracle_mod):
     voff = np.insert(fo.voff, 4, fo.voff[4])
     foff = np.insert(fo.foff, 4, fo.foff[4])
     qoff = np.insert(fo.qoff, 4, fo.qoff[4])
-    forest = fwn.Forest(fo.V, voff, fo.F, foff, records=BOTH)
+    forest = fwn.Forest(fo.V, voff, fo.F, foff, records=BOTH, leaf_size=8)
     got = forest.export_tree()
-    lb = oracle_mod.LbvhTree(fo.V, fo.F, leaf_size=4, voff=voff, foff=foff)
+    lb = oracle_mod.LbvhTree(fo.V, fo.F, leaf_size=8, voff=voff, foff=foff)
     ref = lb.export()
     for k in ("skip", "tri_begin", "tri_count", "sorted_tri", "mesh_root"):
         np.testing.assert_array_equal(got[k], ref[k], err_msg=k)
