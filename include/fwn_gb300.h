@@ -167,6 +167,19 @@ FWN_API fwn_status fwn_query_ex(fwn_handle h, const fwn_query_opts* opts,
 FWN_API fwn_status fwn_query_host(fwn_handle h, const float* points, int64_t n,
                                   float* omega, uint8_t* inside);
 
+/* No counterpart in the reference. Same result as fwn_query with the handle's defaults, but it
+ * allocates nothing: for callers that must not allocate device memory while they query (a
+ * voxelizer or renderer working under a fixed per-frame device budget, or code where a
+ * cudaMalloc/cudaFree could fail or would synchronize the device). Its sort buffers live in one
+ * fixed region built into the library (about 16.3 MB per GPU that loads it, held until exit),
+ * which limits a call to FWN_NOALLOC_MAX_POINTS points (larger n: FWN_INVALID_ARG; split the
+ * batch). All calls share that region: calls whose GPU work overlaps (other streams or host
+ * threads) race and must be serialized. The first call on each device looks up the region's
+ * device address; make it before any stream capture. Asynchronous on `stream`. */
+#define FWN_NOALLOC_MAX_POINTS (1 << 20)
+FWN_API fwn_status fwn_query_noalloc(fwn_handle h, const float* d_points, int64_t n,
+                                     float* d_omega, uint8_t* d_inside, void* stream);
+
 /* Exports the tree for inspection/tests into HOST arrays (any may be NULL):
  *   skip [num_nodes] int32, tri_begin [num_nodes] int32, tri_count [num_nodes] int32
  *   (0 for internal nodes), center_radius [num_nodes x 4] double (P.xyz, r) from the FP64

@@ -75,7 +75,7 @@ _lib = None
 EXPORTS = ["fwn_config_default", "fwn_last_error", "fwn_version", "fwn_build", "fwn_build_device",
            "fwn_destroy", "fwn_get_info", "fwn_query", "fwn_query_ex", "fwn_query_host",
            "fwn_export_tree", "fwn_export_moments", "fwn_forest_build",
-           "fwn_forest_build_device", "fwn_forest_query"]
+           "fwn_forest_build_device", "fwn_forest_query", "fwn_query_noalloc"]
 
 
 def library():
@@ -109,9 +109,11 @@ def library():
     L.fwn_forest_build_device.argtypes = [P, P, P, P, i64, C.POINTER(fwn_config), P,
                                           C.POINTER(P)]
     L.fwn_forest_query.argtypes = [P, P, P, P, P, C.POINTER(fwn_query_opts), P]
+    L.fwn_query_noalloc.argtypes = [P, P, i64, P, P, P]
     for name in ("fwn_build", "fwn_build_device", "fwn_destroy", "fwn_get_info", "fwn_query",
                  "fwn_query_ex", "fwn_query_host", "fwn_export_tree", "fwn_export_moments",
-                 "fwn_forest_build", "fwn_forest_build_device", "fwn_forest_query"):
+                 "fwn_forest_build", "fwn_forest_build_device", "fwn_forest_query",
+                 "fwn_query_noalloc"):
         getattr(L, name).restype = st
     _lib = L
     return L

@@ -33,6 +33,7 @@ SOURCES = [
     ("traverse.cu", []),
     ("forest.cu", []),
     ("fwn_capi.cu", []),
+    ("noalloc.cu", []),
 ]
 
 

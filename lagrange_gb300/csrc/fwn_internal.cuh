@@ -209,4 +209,11 @@ void query_forest(const Engine& e, const QueryArgs& a, const float* d_points,
 
 QueryArgs resolve_query_args(const Engine& e, const fwn_query_opts* opts);
 
+// Query with caller-provided device scratch (no allocation): `scratch` holds the status word and
+// the Morton-sort buffers, at least query_prealloc_bytes(n) bytes, 256-byte aligned. Async.
+size_t query_prealloc_bytes(int64_t n);
+void query_mesh_prealloc(const Engine& e, int mesh, const QueryArgs& a, const float* d_points,
+                         int64_t n, float* d_omega, uint8_t* d_inside, void* scratch,
+                         size_t scratch_bytes, cudaStream_t stream);
+
 }  // namespace fwn

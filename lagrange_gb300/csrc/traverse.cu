@@ -688,4 +688,56 @@ void query_forest(const Engine& e, const QueryArgs& a, const float* d_points,
     }
 }
 
+// Scratch layout of query_mesh_prealloc: [status word, 256 B][4 x n u32 sort keys/values]
+// [radix-sort histogram].
+size_t query_prealloc_bytes(int64_t n) {
+    return 256 + 4 * (size_t)n * sizeof(uint32_t) + radix_sort_temp_bytes(n, 4);
+}
+
+void query_mesh_prealloc(const Engine& e, int mesh, const QueryArgs& a, const float* d_points,
+                         int64_t n, float* d_omega, uint8_t* d_inside, void* scratch,
+                         size_t scratch_bytes, cudaStream_t st) {
+    if (n <= 0) return;
+    if (query_prealloc_bytes(n) > scratch_bytes)
+        throw Error(FWN_INTERNAL, "scratch region smaller than the query needs");
+    if (a.precision == FWN_PRECISION_FP64 && !e.nodes64 && e.num_nodes > 0)
+        throw Error(FWN_INVALID_ARG, "engine was built without FP64 records (FWN_RECORDS_F64)");
+    if (a.precision == FWN_PRECISION_MIXED && !e.nodes32 && e.num_nodes > 0)
+        throw Error(FWN_INVALID_ARG, "engine was built without FP32 records (FWN_RECORDS_F32)");
+    const MeshInfo& mi = e.meshes_h[mesh];
+    char* base = static_cast<char*>(scratch);
+    unsigned* d_status = reinterpret_cast<unsigned*>(base);
+    // the previous call's status bits are still in the shared region: clear them
+    FWN_CUDA_CHECK(cudaMemsetAsync(d_status, 0, sizeof(unsigned), st));
+    if (mi.root < 0) {
+        k_fill_zero<<<grid_for(n, 256), 256, 0, st>>>(d_omega, d_inside, nullptr, n);
+        FWN_CUDA_CHECK(cudaGetLastError());
+        return;
+    }
+    const uint32_t* order = nullptr;
+    if (a.sort_queries && n > 1) {
+        uint32_t* ka = reinterpret_cast<uint32_t*>(base + 256);
+        uint32_t* va = ka + n;
+        uint32_t* kb = va + n;
+        uint32_t* vb = kb + n;
+        void* tmp = vb + n;  // histogram: every entry is written by each pass before it is read
+        k_query_keys<<<grid_for(n, 256), 256, 0, st>>>(d_points, n, mi, ka, va);
+        const bool in_b = radix_sort_u32(ka, va, kb, vb, n, 30, tmp, st);
+        order = in_b ? vb : va;
+    }
+    const int bs = a.block_size;
+    if (a.precision == FWN_PRECISION_FP64) {
+        k_query_f64<false><<<grid_for(n, 128), 128, 0, st>>>(e.nodes64, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, nullptr, d_status, nullptr);
+    } else if (a.traversal == FWN_TRAVERSAL_WARP) {
+        const dim3 g = grid_for(n, WARP_BLOCK);
+        if (a.tuning == 2)
+            k_query_warp<false, 1><<<g, WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, nullptr);
+        else
+            k_query_warp<false, 8><<<g, WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, nullptr);
+    } else {
+        k_query_thread<false><<<grid_for(n, bs), bs, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, nullptr);
+    }
+    FWN_CUDA_CHECK(cudaGetLastError());
+}
+
 }  // namespace fwn
