@@ -104,6 +104,21 @@ def max_over_ranks(dist, x: float, device=None) -> float:
     return float(t.item())
 
 
+def rank_queries(Q, near_mask, rank: int):
+    """The query set a rank answers (weak scaling: every rank has a full-size set). Rank 0 uses
+    the workload as generated; rank r > 0 a seeded shuffle of it (different points per warp,
+    same distribution)."""
+    if rank == 0:
+        return Q, near_mask
+    perm = np.random.default_rng(1000 + rank).permutation(len(Q))
+    return Q[perm], near_mask[perm]
+
+
+def job_value(per_rank_units: int, world: int, max_seconds: float) -> float:
+    """Whole-job throughput: the units all ranks processed over the slowest rank's time."""
+    return world * per_rank_units / max_seconds
+
+
 # ---------------------------------------------------------------------------------------------
 class Clocks:
     """nvidia-smi sampling (200 ms) during the timed region."""
@@ -232,10 +247,7 @@ def run_ours(args, rank, world, local):
     from lagrange_gb300 import workloads as W
 
     wl = W.displaced_icosphere_workload(nu=args.nu, n_queries=args.queries)
-    if world > 1 and rank > 0:  # each rank answers its own shuffle of the queries on its replica
-        perm = np.random.default_rng(1000 + rank).permutation(len(wl.Q))
-        wl.Q = wl.Q[perm]
-        wl.near_mask = wl.near_mask[perm]
+    wl.Q, wl.near_mask = rank_queries(wl.Q, wl.near_mask, rank)
     n = len(wl.Q)
     trav = fwn.TRAVERSAL_WARP if args.traversal == "warp" else fwn.TRAVERSAL_THREAD
     Vd = torch.from_numpy(wl.V).to(dev)
@@ -288,7 +300,7 @@ def run_ours(args, rank, world, local):
     step_ms = [a.elapsed_time(b) for a, b in ev]
     ms = sum(step_ms) / args.steps
     ms = max_over_ranks(dist, ms, dev)
-    value = world * n / (ms / 1e3)
+    value = job_value(n, world, ms / 1e3)
     clocks = clk.summary()
 
     result = {
@@ -381,7 +393,7 @@ def run_ours(args, rank, world, local):
             e2e_call()
             ts.append(time.perf_counter() - t0)
         e2e_s = max_over_ranks(dist, sum(ts) / len(ts), dev)
-        result["e2e"] = {"value": world * n / e2e_s, "unit": "queries/s",
+        result["e2e"] = {"value": job_value(n, world, e2e_s), "unit": "queries/s",
                          "h2d_bytes_per_step": n * 12, "d2h_bytes_per_step": n * 5,
                          "ms_per_step": e2e_s * 1e3, "api": "fwn_query_host (pinned host buffers)"}
 
