@@ -238,7 +238,8 @@ __device__ __forceinline__ bool is_big(const uint64_t* keys, const int* first, c
 __global__ void k_emit_count(int n, int K, const uint64_t* __restrict__ keys,
                              const int* __restrict__ parent, const int* __restrict__ first,
                              const int* __restrict__ last, int* __restrict__ cnt_first,
-                             uint8_t* __restrict__ flags) {
+                             uint8_t* __restrict__ flags, int* __restrict__ leaf_list,
+                             int* __restrict__ leaf_list_len) {
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= 2 * n - 1) return;
     const int pu = parent[u];
@@ -246,6 +247,10 @@ __global__ void k_emit_count(int n, int K, const uint64_t* __restrict__ keys,
     const bool leaf = (u >= n - 1) || !is_big(keys, first, last, u, K);
     flags[u] = (uint8_t)((emitted ? 1 : 0) | (leaf ? 2 : 0));
     if (emitted) atomicAdd(&cnt_first[first[u]], 1);
+    // emitted leaves (never a node spanning meshes: such a node is "big") feed the refit, one
+    // thread each; the list order does not matter (each node's arithmetic is fixed)
+    if (emitted && leaf && !is_cross(keys, first, last, u))
+        leaf_list[atomicAdd(leaf_list_len, 1)] = u;
 }
 
 __global__ void k_positions(int n, const int* __restrict__ parent, const int* __restrict__ first,
@@ -311,23 +316,34 @@ __device__ __forceinline__ void load_tri_d(const float* __restrict__ V, const in
     }
 }
 
-// Moments of the triangles in sorted slots [f, l] about their area-weighted centroid.
+// Moments of the triangles in sorted slots [f, l] about their area-weighted centroid P.
 // Per triangle t (vertices v0,v1,v2, area-weighted normal n = (v1-v0)x(v2-v0)/2, centroid c,
-// d = c - P):  N += n,  M1[i][j] += n_i d_j,
+// d = c - X about a point X):  N += n,  M1[i][j] += n_i d_j,
 // M2[i][jk] += n_i (d_j d_k + (1/12) sum_v (v-c)_j (v-c)_k)   (exact area integral of
-// (x-P)_j (x-P)_k over the triangle divided by its area).
+// (x-X)_j (x-X)_k over the triangle divided by its area).
+// One pass accumulates the moments about X = the first triangle's centroid c0 together with the
+// area-weighted centroid; they are then moved to P with the same recentring formulas a parent
+// uses for its children (e = c0 - P). A second, vertex-only pass gives r = max |v - P|.
+constexpr double kThird = 1.0 / 3.0;
+constexpr double kTwelfth = 1.0 / 12.0;
+
 __device__ void leaf_moments(const float* __restrict__ V, const int32_t* __restrict__ F,
                              const int64_t* __restrict__ voff, const uint64_t* __restrict__ keys,
                              const uint32_t* __restrict__ tri_of_slot, int f, int l,
                              StageRec& R) {
-    double A = 0.0, S[3] = {0.0, 0.0, 0.0}, Cs[3] = {0.0, 0.0, 0.0};
+    double A = 0.0, S[3] = {0.0, 0.0, 0.0}, Cs[3] = {0.0, 0.0, 0.0}, c0[3] = {0.0, 0.0, 0.0};
+    double N[3] = {0.0, 0.0, 0.0}, M1[9], M2[18];
+    for (int i = 0; i < 9; ++i) M1[i] = 0.0;
+    for (int i = 0; i < 18; ++i) M2[i] = 0.0;
     float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    const int SJ[6] = {0, 1, 2, 0, 0, 1};
+    const int SK[6] = {0, 1, 2, 1, 2, 2};
     for (int s = f; s <= l; ++s) {
         const int64_t t = tri_of_slot[s];
         const int m = (int)(keys[s] >> MORTON_BITS);
         double v[3][3];
         load_tri_d(V, F, voff[m], t, v);
-        double e1[3], e2[3], nn[3], c[3];
+        double e1[3], e2[3], nn[3], c[3], d[3], w[3][3], Q[6];
         for (int a = 0; a < 3; ++a) {
             e1[a] = v[1][a] - v[0][a];
             e2[a] = v[2][a] - v[0][a];
@@ -336,12 +352,29 @@ __device__ void leaf_moments(const float* __restrict__ V, const int32_t* __restr
         nn[1] = 0.5 * (e1[2] * e2[0] - e1[0] * e2[2]);
         nn[2] = 0.5 * (e1[0] * e2[1] - e1[1] * e2[0]);
         const double a_t = sqrt(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
+        for (int a = 0; a < 3; ++a) c[a] = ((v[0][a] + v[1][a]) + v[2][a]) * kThird;
+        if (s == f)
+            for (int a = 0; a < 3; ++a) c0[a] = c[a];
         for (int a = 0; a < 3; ++a) {
-            c[a] = ((v[0][a] + v[1][a]) + v[2][a]) / 3.0;
             S[a] = S[a] + a_t * c[a];
             Cs[a] = Cs[a] + c[a];
+            d[a] = c[a] - c0[a];
         }
         A = A + a_t;
+        for (int j = 0; j < 3; ++j)
+            for (int a = 0; a < 3; ++a) w[j][a] = v[j][a] - c[a];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const int j = SJ[q], k = SK[q];
+            const double cov = ((w[0][j] * w[0][k] + w[1][j] * w[1][k]) + w[2][j] * w[2][k]) * kTwelfth;
+            Q[q] = d[j] * d[k] + cov;
+        }
+        for (int i = 0; i < 3; ++i) {
+            N[i] = N[i] + nn[i];
+            for (int j = 0; j < 3; ++j) M1[3 * i + j] = M1[3 * i + j] + nn[i] * d[j];
+#pragma unroll
+            for (int q = 0; q < 6; ++q) M2[6 * i + q] = M2[6 * i + q] + nn[i] * Q[q];
+        }
         for (int j = 0; j < 3; ++j)
             for (int a = 0; a < 3; ++a) {
                 const float x = (float)v[j][a];
@@ -350,51 +383,30 @@ __device__ void leaf_moments(const float* __restrict__ V, const int32_t* __restr
             }
     }
     const double cnt = (double)(l - f + 1);
-    double P[3];
+    double P[3], e[3];
     for (int a = 0; a < 3; ++a) {
         const double pe = A > 0.0 ? S[a] / A : Cs[a] / cnt;
         P[a] = (double)(float)pe;
+        e[a] = c0[a] - P[a];
     }
-    double N[3] = {0, 0, 0}, M1[9], M2[18], r2 = 0.0;
-    for (int i = 0; i < 9; ++i) M1[i] = 0.0;
-    for (int i = 0; i < 18; ++i) M2[i] = 0.0;
+    for (int i = 0; i < 3; ++i) {
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const int j = SJ[q], k = SK[q];
+            R.M2[6 * i + q] = ((M2[6 * i + q] + M1[3 * i + j] * e[k]) + M1[3 * i + k] * e[j]) +
+                              N[i] * (e[j] * e[k]);
+        }
+        for (int j = 0; j < 3; ++j) R.M1[3 * i + j] = M1[3 * i + j] + N[i] * e[j];
+    }
+    double r2 = 0.0;
     for (int s = f; s <= l; ++s) {
         const int64_t t = tri_of_slot[s];
         const int m = (int)(keys[s] >> MORTON_BITS);
         double v[3][3];
         load_tri_d(V, F, voff[m], t, v);
-        double e1[3], e2[3], nn[3], c[3], d[3];
-        for (int a = 0; a < 3; ++a) {
-            e1[a] = v[1][a] - v[0][a];
-            e2[a] = v[2][a] - v[0][a];
-        }
-        nn[0] = 0.5 * (e1[1] * e2[2] - e1[2] * e2[1]);
-        nn[1] = 0.5 * (e1[2] * e2[0] - e1[0] * e2[2]);
-        nn[2] = 0.5 * (e1[0] * e2[1] - e1[1] * e2[0]);
-        for (int a = 0; a < 3; ++a) {
-            c[a] = ((v[0][a] + v[1][a]) + v[2][a]) / 3.0;
-            d[a] = c[a] - P[a];
-        }
-        double w[3][3];  // vertex offsets from the centroid
-        for (int j = 0; j < 3; ++j)
-            for (int a = 0; a < 3; ++a) w[j][a] = v[j][a] - c[a];
-        const int SJ[6] = {0, 1, 2, 0, 0, 1};
-        const int SK[6] = {0, 1, 2, 1, 2, 2};
-        double Q[6];
-        for (int q = 0; q < 6; ++q) {
-            const int j = SJ[q], k = SK[q];
-            const double cov = ((w[0][j] * w[0][k] + w[1][j] * w[1][k]) + w[2][j] * w[2][k]) / 12.0;
-            Q[q] = d[j] * d[k] + cov;
-        }
-        for (int i = 0; i < 3; ++i) {
-            N[i] = N[i] + nn[i];
-            for (int j = 0; j < 3; ++j) M1[3 * i + j] = M1[3 * i + j] + nn[i] * d[j];
-            for (int q = 0; q < 6; ++q) M2[6 * i + q] = M2[6 * i + q] + nn[i] * Q[q];
-        }
         for (int j = 0; j < 3; ++j) {
             const double dx = v[j][0] - P[0], dy = v[j][1] - P[1], dz = v[j][2] - P[2];
-            const double q2 = (dx * dx + dy * dy) + dz * dz;
-            r2 = fmax(r2, q2);
+            r2 = fmax(r2, (dx * dx + dy * dy) + dz * dz);
         }
     }
     for (int a = 0; a < 3; ++a) {
@@ -403,8 +415,6 @@ __device__ void leaf_moments(const float* __restrict__ V, const int32_t* __restr
         R.lo[a] = lo[a];
         R.hi[a] = hi[a];
     }
-    for (int i = 0; i < 9; ++i) R.M1[i] = M1[i];
-    for (int i = 0; i < 18; ++i) R.M2[i] = M2[i];
     R.area = A;
     R.r = round_up_float(sqrt(r2));
 }
@@ -480,7 +490,8 @@ __device__ __forceinline__ void store_rec(StageRec* dst, const StageRec& R) {
     *dst = R;
 }
 
-__global__ void k_refit(int n, int K, const uint64_t* __restrict__ keys,
+__global__ void k_refit(int num_leaves, const int* __restrict__ leaf_list,
+                        const uint64_t* __restrict__ keys,
                         const int* __restrict__ parent, const int* __restrict__ first,
                         const int* __restrict__ last, const int* __restrict__ left,
                         const int* __restrict__ right, const int* __restrict__ pos,
@@ -489,18 +500,8 @@ __global__ void k_refit(int n, int K, const uint64_t* __restrict__ keys,
                         StageRec* __restrict__ stage, int* __restrict__ visit,
                         unsigned* __restrict__ status) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n) return;
-    int e = (n - 1) + k;
-    while (e != 0) {
-        const int p = parent[e];
-        if (p < 0) {  // unlinked node: cannot happen for a Karras tree
-            atomicOr(status, ST_REFIT_ORPHAN);
-            return;
-        }
-        if (is_big(keys, first, last, p, K)) break;
-        e = p;
-    }
-    if (first[e] != k) return;  // the leaf is handled by the thread of its first slot
+    if (k >= num_leaves) return;
+    const int e = leaf_list[k];  // one emitted leaf per thread
     StageRec R;
     leaf_moments(V, F, voff, keys, tri_of_slot, first[e], last[e], R);
     store_rec(&stage[pos[e]], R);
@@ -771,6 +772,8 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
         int* skip = (int*)track(dalloc<int>(nn, st));
         void* scan_tmp = track(dalloc<char>(exclusive_scan_temp_bytes(n + 1), st));
         int* visit = (int*)track(dalloc<int>(std::max(n - 1, 1), st));
+        int* leaf_list = (int*)track(dalloc<int>(n, st));
+        int* leaf_list_len = (int*)track(dalloc<int>(1, st));
         int* leaf_count = (int*)track(dalloc<int>(1, st));
 
         FWN_CUDA_CHECK(cudaMemsetAsync(parent, 0xff, (size_t)nn * sizeof(int), st));  // -1
@@ -782,13 +785,16 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
             k_karras<<<grid_for(n - 1, 256), 256, 0, st>>>(keys, n, left, right, parent, first, last);
         }
         FWN_CUDA_CHECK(cudaMemsetAsync(cnt, 0, (n + 1) * sizeof(int), st));
-        k_emit_count<<<grid_for(nn, 256), 256, 0, st>>>(n, K, keys, parent, first, last, cnt, flags);
+        FWN_CUDA_CHECK(cudaMemsetAsync(leaf_list_len, 0, sizeof(int), st));
+        k_emit_count<<<grid_for(nn, 256), 256, 0, st>>>(n, K, keys, parent, first, last, cnt, flags,
+                                                        leaf_list, leaf_list_len);
         exclusive_scan_i32(cnt, n + 1, scan_tmp, st);
         k_positions<<<grid_for(nn, 256), 256, 0, st>>>(n, parent, first, last, flags, cnt, pos, skip);
         k_mesh_roots<<<grid_for(nmeshes, 128), 128, 0, st>>>((int)nmeshes, foff, n, parent, first,
                                                              last, pos, skip, e.meshes);
-        int E = 0;
+        int E = 0, NL = 0;
         FWN_CUDA_CHECK(cudaMemcpyAsync(&E, cnt + n, sizeof(int), cudaMemcpyDeviceToHost, st));
+        FWN_CUDA_CHECK(cudaMemcpyAsync(&NL, leaf_list_len, sizeof(int), cudaMemcpyDeviceToHost, st));
         FWN_CUDA_CHECK(cudaStreamSynchronize(st));
         e.num_nodes = E;
 
@@ -797,8 +803,10 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
         else e.stage = stage;
         FWN_CUDA_CHECK(cudaMemsetAsync(visit, 0, std::max(n - 1, 1) * sizeof(int), st));
         FWN_CUDA_CHECK(cudaMemsetAsync(leaf_count, 0, sizeof(int), st));
-        k_refit<<<grid_for(n, 128), 128, 0, st>>>(n, K, keys, parent, first, last, left, right, pos,
-                                                  tri_of_slot, d_V, d_F, voff, stage, visit, status);
+        if (NL > 0)
+            k_refit<<<grid_for(NL, 128), 128, 0, st>>>(NL, leaf_list, keys, parent, first, last, left,
+                                                       right, pos, tri_of_slot, d_V, d_F, voff,
+                                                       stage, visit, status);
         FWN_CUDA_CHECK(cudaGetLastError());
         if (e.cfg.records & FWN_RECORDS_F32) FWN_CUDA_CHECK(cudaMalloc(&e.nodes32, E * sizeof(NodeF32)));
         if (e.cfg.records & FWN_RECORDS_F64) FWN_CUDA_CHECK(cudaMalloc(&e.nodes64, E * sizeof(NodeF64)));

@@ -467,41 +467,16 @@ static void lb_tri_d(const lb_tree* T, int64_t s, double v[3][3]) {
         for (int a = 0; a < 3; ++a) v[j][a] = (double)T->tv[9 * s + 3 * j + a];
 }
 
+/* Leaf moments (same steps as the device refit): one pass accumulates the area-weighted
+ * centroid and the moments about the first triangle's centroid c0; the moments are then moved to
+ * P = float(area-weighted centroid) with the parent recentring formulas (e = c0 - P); a second,
+ * vertex-only pass gives r = max |v - P| (rounded up to a float). */
 static void lb_leaf(const lb_tree* T, int64_t f, int64_t l, lb_stage* R) {
-    double A = 0.0, S[3] = {0, 0, 0}, Cs[3] = {0, 0, 0};
-    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-    for (int64_t s = f; s <= l; ++s) {
-        double v[3][3], e1[3], e2[3], nn[3], c[3];
-        lb_tri_d(T, s, v);
-        for (int a = 0; a < 3; ++a) {
-            e1[a] = v[1][a] - v[0][a];
-            e2[a] = v[2][a] - v[0][a];
-        }
-        nn[0] = 0.5 * (e1[1] * e2[2] - e1[2] * e2[1]);
-        nn[1] = 0.5 * (e1[2] * e2[0] - e1[0] * e2[2]);
-        nn[2] = 0.5 * (e1[0] * e2[1] - e1[1] * e2[0]);
-        const double at = sqrt(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
-        for (int a = 0; a < 3; ++a) {
-            c[a] = ((v[0][a] + v[1][a]) + v[2][a]) / 3.0;
-            S[a] = S[a] + at * c[a];
-            Cs[a] = Cs[a] + c[a];
-        }
-        A = A + at;
-        for (int j = 0; j < 3; ++j)
-            for (int a = 0; a < 3; ++a) {
-                const float x = (float)v[j][a];
-                lo[a] = fminf(lo[a], x);
-                hi[a] = fmaxf(hi[a], x);
-            }
-    }
-    const double cnt = (double)(l - f + 1);
-    double P[3];
-    for (int a = 0; a < 3; ++a) {
-        const double pe = A > 0.0 ? S[a] / A : Cs[a] / cnt;
-        P[a] = (double)(float)pe;
-    }
-    double N[3] = {0, 0, 0}, M1[9] = {0}, M2[18] = {0}, r2 = 0.0;
+    static const double kThird = 1.0 / 3.0, kTwelfth = 1.0 / 12.0;
     static const int SJ[6] = {0, 1, 2, 0, 0, 1}, SK[6] = {0, 1, 2, 1, 2, 2};
+    double A = 0.0, S[3] = {0, 0, 0}, Cs[3] = {0, 0, 0}, c0[3] = {0, 0, 0};
+    double N[3] = {0, 0, 0}, M1[9] = {0}, M2[18] = {0};
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (int64_t s = f; s <= l; ++s) {
         double v[3][3], e1[3], e2[3], nn[3], c[3], d[3], w[3][3], Q[6];
         lb_tri_d(T, s, v);
@@ -512,15 +487,21 @@ static void lb_leaf(const lb_tree* T, int64_t f, int64_t l, lb_stage* R) {
         nn[0] = 0.5 * (e1[1] * e2[2] - e1[2] * e2[1]);
         nn[1] = 0.5 * (e1[2] * e2[0] - e1[0] * e2[2]);
         nn[2] = 0.5 * (e1[0] * e2[1] - e1[1] * e2[0]);
+        const double at = sqrt(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
+        for (int a = 0; a < 3; ++a) c[a] = ((v[0][a] + v[1][a]) + v[2][a]) * kThird;
+        if (s == f)
+            for (int a = 0; a < 3; ++a) c0[a] = c[a];
         for (int a = 0; a < 3; ++a) {
-            c[a] = ((v[0][a] + v[1][a]) + v[2][a]) / 3.0;
-            d[a] = c[a] - P[a];
+            S[a] = S[a] + at * c[a];
+            Cs[a] = Cs[a] + c[a];
+            d[a] = c[a] - c0[a];
         }
+        A = A + at;
         for (int j = 0; j < 3; ++j)
             for (int a = 0; a < 3; ++a) w[j][a] = v[j][a] - c[a];
         for (int q = 0; q < 6; ++q) {
             const int j = SJ[q], k = SK[q];
-            const double cov = ((w[0][j] * w[0][k] + w[1][j] * w[1][k]) + w[2][j] * w[2][k]) / 12.0;
+            const double cov = ((w[0][j] * w[0][k] + w[1][j] * w[1][k]) + w[2][j] * w[2][k]) * kTwelfth;
             Q[q] = d[j] * d[k] + cov;
         }
         for (int i = 0; i < 3; ++i) {
@@ -528,10 +509,35 @@ static void lb_leaf(const lb_tree* T, int64_t f, int64_t l, lb_stage* R) {
             for (int j = 0; j < 3; ++j) M1[3 * i + j] = M1[3 * i + j] + nn[i] * d[j];
             for (int q = 0; q < 6; ++q) M2[6 * i + q] = M2[6 * i + q] + nn[i] * Q[q];
         }
+        for (int j = 0; j < 3; ++j)
+            for (int a = 0; a < 3; ++a) {
+                const float x = (float)v[j][a];
+                lo[a] = fminf(lo[a], x);
+                hi[a] = fmaxf(hi[a], x);
+            }
+    }
+    const double cnt = (double)(l - f + 1);
+    double P[3], e[3];
+    for (int a = 0; a < 3; ++a) {
+        const double pe = A > 0.0 ? S[a] / A : Cs[a] / cnt;
+        P[a] = (double)(float)pe;
+        e[a] = c0[a] - P[a];
+    }
+    for (int i = 0; i < 3; ++i) {
+        for (int q = 0; q < 6; ++q) {
+            const int j = SJ[q], k = SK[q];
+            R->M2[6 * i + q] = ((M2[6 * i + q] + M1[3 * i + j] * e[k]) + M1[3 * i + k] * e[j]) +
+                               N[i] * (e[j] * e[k]);
+        }
+        for (int j = 0; j < 3; ++j) R->M1[3 * i + j] = M1[3 * i + j] + N[i] * e[j];
+    }
+    double r2 = 0.0;
+    for (int64_t s = f; s <= l; ++s) {
+        double v[3][3];
+        lb_tri_d(T, s, v);
         for (int j = 0; j < 3; ++j) {
             const double dx = v[j][0] - P[0], dy = v[j][1] - P[1], dz = v[j][2] - P[2];
-            const double q2 = (dx * dx + dy * dy) + dz * dz;
-            r2 = fmax(r2, q2);
+            r2 = fmax(r2, (dx * dx + dy * dy) + dz * dz);
         }
     }
     for (int a = 0; a < 3; ++a) {
@@ -540,8 +546,6 @@ static void lb_leaf(const lb_tree* T, int64_t f, int64_t l, lb_stage* R) {
         R->lo[a] = lo[a];
         R->hi[a] = hi[a];
     }
-    memcpy(R->M1, M1, sizeof(M1));
-    memcpy(R->M2, M2, sizeof(M2));
     R->area = A;
     R->r = round_up_float(sqrt(r2));
 }
