@@ -59,13 +59,16 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--nu", type=int, default=316)
-    p.add_argument("--queries", type=int, default=10_000_000)
+    p.add_argument("--workload", default="icosphere",
+                   choices=["icosphere", "soup", "uvsphere", "forest", "voxel"])
+    p.add_argument("--nu", type=int, default=None)
+    p.add_argument("--queries", type=int, default=None)
     p.add_argument("--leaf", type=int, default=8)
     p.add_argument("--traversal", default="warp", choices=["thread", "warp"])
     p.add_argument("--block", type=int, default=128)
     p.add_argument("--fp64-steps", type=int, default=2)
     p.add_argument("--cpu-sample", type=int, default=100_000)
+    p.add_argument("--brute", type=int, default=1024)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -190,6 +193,31 @@ def measured_peaks():
 
 
 # ---------------------------------------------------------------------------------------------
+def make_workload(args):
+    """Single-mesh workloads: icosphere (default: 1,997,120 triangles, 10M queries), soup (the
+    defective 1M-triangle soup, 5M queries), uvsphere (3,968 triangles, 100k queries)."""
+    from lagrange_gb300 import workloads as W
+    if args.workload == "soup":
+        return W.defective_soup_workload(nu=args.nu or 224, n_queries=args.queries or 5_000_000)
+    if args.workload == "uvsphere":
+        return W.uv_sphere_workload(n_queries=args.queries or 100_000)
+    return W.displaced_icosphere_workload(nu=args.nu or 316, n_queries=args.queries or 10_000_000)
+
+
+def cpu_sample(wl, size: int, seed: int = 7):
+    """A bounded sample of the workload's queries: half far/box, half near-surface when the
+    workload has both kinds, else uniform."""
+    rng = np.random.default_rng(seed)
+    size = min(size, len(wl.Q))
+    if wl.near_mask is None or not wl.near_mask.any() or wl.near_mask.all():
+        return wl.Q[rng.choice(len(wl.Q), size, replace=False)]
+    far_idx = np.nonzero(~wl.near_mask)[0]
+    near_idx = np.nonzero(wl.near_mask)[0]
+    half = size // 2
+    return np.concatenate([wl.Q[rng.choice(far_idx, half, replace=False)],
+                           wl.Q[rng.choice(near_idx, size - half, replace=False)]])
+
+
 def run_reference(args, rank, world):
     """CPU implementation of the reference path (oracle restatement O2), all host threads."""
     dist = init_dist(world, "gloo")
@@ -197,18 +225,17 @@ def run_reference(args, rank, world):
         barrier(dist)
         return
     import oracle
-    from lagrange_gb300 import workloads as W
-    wl = W.displaced_icosphere_workload(nu=args.nu, n_queries=args.queries)
+    if args.workload in ("forest", "voxel"):
+        print(json.dumps({"impl": "reference", "unavailable": "the reference arm times the "
+                          "single-mesh workloads; forest/voxel are GPU-side comparisons"}))
+        barrier(dist)
+        return
+    wl = make_workload(args)
     nthr = oracle.nthreads_default()
     t0 = time.perf_counter()
     tree = oracle.RefTree(wl.V, wl.F, leaf_size=args.leaf)
     build_s = time.perf_counter() - t0
-    rng = np.random.default_rng(7)
-    nb = len(wl.Q) // 2
-    half = args.cpu_sample // 2
-    sample = np.concatenate([wl.Q[rng.choice(nb, half, replace=False)],
-                             wl.Q[nb + rng.choice(len(wl.Q) - nb, args.cpu_sample - half,
-                                                  replace=False)]])
+    sample = cpu_sample(wl, args.cpu_sample)
     for _ in range(args.warmup):
         tree.query(sample[:2000], beta=wl.beta, nthreads=nthr)
     t0 = time.perf_counter()
@@ -224,8 +251,9 @@ def run_reference(args, rank, world):
         "config": {"workload": wl.name, "triangles": int(len(wl.F)), "queries": int(len(wl.Q)),
                    "beta": wl.beta, "leaf_size": args.leaf},
         "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": nthr, "kind": "port",
-                         "sample": f"{len(sample)} queries per step (half box, half near-surface)"
-                                   f" of the {len(wl.Q)}-query workload; tree build "
+                         "sample": f"{len(sample)} queries per step (half far, half near-surface "
+                                   f"where the workload has both) of the {len(wl.Q)}-query "
+                                   f"workload; tree build "
                                    f"{build_s:.2f} s single-thread",
                          "build_s": build_s},
         "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -246,7 +274,9 @@ def run_ours(args, rank, world, local):
     import lagrange_gb300 as fwn
     from lagrange_gb300 import workloads as W
 
-    wl = W.displaced_icosphere_workload(nu=args.nu, n_queries=args.queries)
+    wl = make_workload(args)
+    if wl.near_mask is None:
+        wl.near_mask = np.zeros(len(wl.Q), bool)
     wl.Q, wl.near_mask = rank_queries(wl.Q, wl.near_mask, rank)
     n = len(wl.Q)
     trav = fwn.TRAVERSAL_WARP if args.traversal == "warp" else fwn.TRAVERSAL_THREAD
@@ -363,11 +393,22 @@ def run_ours(args, rank, world, local):
         torch.cuda.synchronize()
         dw = (w_out.double() - w64).abs() / FOUR_PI
         near = torch.from_numpy(wl.near_mask).to(dev)
+
+        def pct(x):
+            if x.numel() == 0:
+                return None
+            x = x[torch.randperm(x.numel(), device=x.device)[:4_000_000]] if x.numel() > 4_000_000 else x
+            qs = torch.tensor([0.5, 0.9, 0.99, 0.999], dtype=x.dtype, device=x.device)
+            return {"p50": float(torch.quantile(x, qs[0])), "p90": float(torch.quantile(x, qs[1])),
+                    "p99": float(torch.quantile(x, qs[2])), "p99.9": float(torch.quantile(x, qs[3])),
+                    "max": float(x.max())}
         result["plain_fp64"] = {
             "value": n / (ms64 / 1e3), "unit": "queries/s", "ms_per_step": ms64,
             "speedup_mixed_over_fp64": ms64 / ms,
             "max_dw": float(dw.max()), "rms_dw": float(dw.pow(2).mean().sqrt()),
-            "max_dw_near": float(dw[near].max()), "max_dw_far": float(dw[~near].max()),
+            "max_dw_near": float(dw[near].max()) if bool(near.any()) else None,
+            "max_dw_far": float(dw[~near].max()) if bool((~near).any()) else None,
+            "dw_percentiles": {"near": pct(dw[near]), "far": pct(dw[~near])},
             "gate_1e-4": bool(float(dw.max()) <= 1e-4),
             "inside_disagree_band": int(((i_out.bool() != (w64 > 2 * math.pi)) &
                                          ((w64 / FOUR_PI - 0.5).abs() > 1e-3)).sum()),
@@ -404,18 +445,14 @@ def run_ours(args, rank, world, local):
         t0 = time.perf_counter()
         tree = oracle.RefTree(wl.V, wl.F, leaf_size=args.leaf)
         build_s = time.perf_counter() - t0
-        rng = np.random.default_rng(7)
-        nb = n // 2
-        half = args.cpu_sample // 2
-        sample = np.concatenate([wl.Q[rng.choice(nb, half, replace=False)],
-                                 wl.Q[nb + rng.choice(n - nb, args.cpu_sample - half, replace=False)]])
+        sample = cpu_sample(wl, args.cpu_sample)
         tree.query(sample[:1000], nthreads=nthr)
         t0 = time.perf_counter()
         om_cpu, in_cpu = tree.query(sample, beta=wl.beta, nthreads=nthr)
         dt = time.perf_counter() - t0
         result["cpu_baseline"] = {
             "value": len(sample) / dt, "unit": "queries/s", "cores": nthr, "kind": "port",
-            "sample": f"{len(sample)} queries (half box, half near-surface) of the workload; "
+            "sample": f"{len(sample)} queries (half far, half near-surface) of the workload; "
                       f"float order-2 Barill tree restating the reference path; build "
                       f"{build_s:.2f} s single-thread",
         }
@@ -428,7 +465,126 @@ def run_ours(args, rank, world, local):
         result["inside_vs_reference"] = {
             "sample": len(sample), "disagree_outside_band": int(np.sum(ig[band] != in_cpu[band])),
             "max_dw_vs_reference_restatement": float(np.max(np.abs(wg - om_cpu)) / FOUR_PI)}
+        # against the FP64 brute force over all triangles, on a stratified sample
+        nb_pts = len(wl.Q) if len(wl.F) * len(wl.Q) <= 5e8 else args.brute
+        bs = cpu_sample(wl, nb_pts, seed=11)
+        exact = oracle.brute_f64(wl.V, wl.F, bs, nthreads=nthr)
+        bq = torch.from_numpy(bs).to(dev)
+        wm, _ = eng.query(bq, traversal=trav)
+        torch.cuda.synchronize()
+        dwb = np.abs(wm.cpu().numpy().astype(np.float64) - exact) / FOUR_PI
+        half = len(bs) // 2 if wl.near_mask.any() else len(bs)
+        result["vs_brute_force_fp64"] = {
+            "sample": len(bs), "max_dw": float(dwb.max()), "rms_dw": float(np.sqrt(np.mean(dwb ** 2))),
+            "max_dw_far": float(dwb[:half].max()),
+            "max_dw_near": float(dwb[half:].max()) if half < len(bs) else None,
+            "note": "includes the beta=2 far-field truncation error (same for the FP64 form)"}
 
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    barrier(dist)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def run_forest(args, rank, world, local):
+    """Batched workloads: `forest` (512 uneven spheres/tori, seed 3) and `voxel` (4 x 5M-triangle
+    meshes, each on a 256^3 voxel-centre grid). Build: one launch per stage over all meshes.
+    Mixed query: one persistent launch over all meshes, captured in a CUDA graph and replayed.
+    Plain form: FP64 everywhere, one launch per mesh."""
+    import torch
+    torch.cuda.set_device(local)
+    dist = init_dist(world, "nccl")
+    dev = torch.device("cuda", local)
+    import lagrange_gb300 as fwn
+    from lagrange_gb300 import workloads as W
+
+    t0 = time.perf_counter()
+    fo = W.batched_forest_workload() if args.workload == "forest" else W.voxel_workload(
+        nu=args.nu or 500)
+    gen_s = time.perf_counter() - t0
+    M = len(fo.voff) - 1
+    n = len(fo.Q)
+    Vd = torch.from_numpy(fo.V).to(dev)
+    Fd = torch.from_numpy(fo.F).to(dev)
+    Qd = torch.from_numpy(fo.Q).to(dev)
+    L = fwn.library()
+    builds = []
+    for _ in range(3):
+        f2 = fwn.Forest(Vd, fo.voff, Fd, fo.foff, leaf_size=args.leaf, records=fwn.RECORDS_F32)
+        builds.append(f2.info()["build_ms"])
+        f2.close()
+    forest = fwn.Forest(Vd, fo.voff, Fd, fo.foff, leaf_size=args.leaf,
+                        records=fwn.RECORDS_F32 | (0 if args.no_fp64 else fwn.RECORDS_F64))
+    qoff = torch.from_numpy(fo.qoff.astype(np.int64)).pin_memory()  # pinned: capturable copy
+    w = torch.empty(n, dtype=torch.float32, device=dev)
+    ins = torch.empty(n, dtype=torch.uint8, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    opts = fwn._opts(precision=fwn.PRECISION_MIXED)
+
+    def q_mixed(stream_ptr):
+        fwn._check(L.fwn_forest_query(forest.handle, C.c_void_p(Qd.data_ptr()),
+                                      C.c_void_p(qoff.data_ptr()), C.c_void_p(w.data_ptr()),
+                                      C.c_void_p(ins.data_ptr()), C.byref(opts), stream_ptr))
+    side = torch.cuda.Stream(dev)
+    side.wait_stream(torch.cuda.current_stream(dev))
+    with torch.cuda.stream(side):
+        for _ in range(args.warmup):
+            q_mixed(C.c_void_p(side.cuda_stream))
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        q_mixed(C.c_void_p(torch.cuda.current_stream(dev).cuda_stream))
+    torch.cuda.synchronize()
+    graph.replay()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream(dev)
+    ts = []
+    with Clocks(not args.no_clocks and rank == 0, local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            graph.replay()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+    ms = max_over_ranks(dist, sum(ts) / len(ts), dev)
+    build_ms = min(builds)
+    result = {
+        "metric": f"winding queries/s, {M} meshes in one persistent CUDA-graph launch",
+        "value": job_value(n, world, ms / 1e3), "unit": "queries/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 near field/refit)",
+        "data": "synthetic",
+        "config": {"workload": fo.name, "meshes": M, "triangles": int(fo.foff[-1]),
+                   "queries": n, "beta": fo.beta, "leaf_size": args.leaf,
+                   "l2": "flushed before every step (256 MB write)", "generation_s": gen_s},
+        "build_ms": build_ms, "tree_nodes": forest.info()["num_nodes"],
+        "meshes_per_s_build_plus_query": M / ((build_ms + ms) / 1e3),
+        "clocks": clk.summary(),
+    }
+    if not args.no_fp64:
+        w64 = torch.empty(n, dtype=torch.float32, device=dev)
+        o64 = fwn._opts(precision=fwn.PRECISION_FP64)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fwn._check(L.fwn_forest_query(forest.handle, C.c_void_p(Qd.data_ptr()),
+                                      C.c_void_p(qoff.data_ptr()), C.c_void_p(w64.data_ptr()),
+                                      None, C.byref(o64), C.c_void_p(stream.cuda_stream)))
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms64 = a.elapsed_time(b)
+        dw = (w.double() - w64.double()).abs() / FOUR_PI
+        band = (w64.double() / FOUR_PI - 0.5).abs() > 1e-3
+        result["plain_fp64_per_mesh_launches"] = {
+            "value": n / (ms64 / 1e3), "unit": "queries/s", "ms": ms64, "launches": M,
+            "speedup_mixed_over_fp64": ms64 / ms,
+            "max_dw": float(dw.max()), "rms_dw": float(dw.pow(2).mean().sqrt()),
+            "note": "FP64 output rounded to float; |dw| includes that rounding (<= 4e-8)",
+            "inside_disagree_band": int(((ins.bool() != (w64.double() > 2 * math.pi)) & band).sum()),
+        }
     if rank == 0:
         print(json.dumps(result), flush=True)
     barrier(dist)
@@ -441,6 +597,8 @@ def main():
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)
+    elif args.workload in ("forest", "voxel"):
+        run_forest(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)
 

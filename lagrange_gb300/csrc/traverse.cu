@@ -357,47 +357,37 @@ k_query_thread(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tri
 // of the warp's lanes, and a lane takes part in a step only when the cursor equals its own resume
 // index. Node loads are therefore warp-uniform (one L1 wavefront each), while every lane still
 // visits exactly its own path, in DFS order (so the result does not depend on which queries share
-// the warp). The walk is software-pipelined: the next cursor is reduced right after the far test
-// and its 32 B test sector is loaded before this step's Taylor / leaf work, and the coefficient
-// sectors of the current node are requested before its far test.
+// the warp). A lane is done when its resume index reaches the end of its own mesh's subtree, so
+// one warp may serve queries of consecutive meshes of a forest (their subtrees are consecutive
+// ranges of the DFS order). The walk is software-pipelined: the next cursor is reduced right
+// after the far test and its 32 B test sector is loaded before this step's Taylor / leaf work,
+// and the coefficient sectors of the current node are requested before its far test.
 // Near leaves: the (query, triangle) pairs of the leaf under the cursor are spread over all 32
 // lanes (triangles staged in shared memory) and each owner adds its results in triangle order.
 constexpr int WARP_LEAF_MAX = 16;
 constexpr int WARP_BLOCK = 128;
+constexpr int DONE = INT_MAX;
 
-template <bool STATS, int MINB>
-__global__ void __launch_bounds__(WARP_BLOCK, MINB)
-k_query_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
-             const MeshInfo mi, const float* __restrict__ Q, const uint32_t* __restrict__ order,
-             int64_t n, float beta, float* __restrict__ omega, uint8_t* __restrict__ inside,
-             unsigned* __restrict__ status, unsigned long long* __restrict__ stats) {
-    __shared__ float4 leafbuf[WARP_BLOCK / 32][WARP_LEAF_MAX * 3];
-    __shared__ float4 qbuf[WARP_BLOCK / 32][32];
-    __shared__ float resbuf[WARP_BLOCK / 32][32 * WARP_LEAF_MAX];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k - lane >= n) return;  // whole warp out of range (warp-uniform)
-    const bool valid = k < n;
-    QCounters qc;
-    float qx = 0.f, qy = 0.f, qz = 0.f;
-    int64_t qi = 0;
-    if (valid) {
-        qi = order ? (int64_t)order[k] : k;
-        qx = Q[3 * qi];
-        qy = Q[3 * qi + 1];
-        qz = Q[3 * qi + 2];
-    }
-    const float tau = mi.tau;
-    const float cond = mi.cond;
-    const int end = mi.end;
+struct WarpSmem {
+    float4 leaf[WARP_LEAF_MAX * 3];
+    float4 q[32];
+    float res[32 * WARP_LEAF_MAX];
+};
+
+template <bool STATS>
+__device__ __forceinline__ void warp_walk(const NodeF32* __restrict__ nodes,
+                                          const TriF32* __restrict__ tris, int root, int lane_end,
+                                          float tau, float cond, float qx, float qy, float qz,
+                                          float beta, WarpSmem& sm, float& s, float& c,
+                                          QCounters& qc, unsigned* __restrict__ status) {
+    const int lane = threadIdx.x & 31;
     const unsigned lt = lanemask_lt();
-    float s = 0.f, c = 0.f;
-    int resume = valid ? mi.root : INT_MAX;
+    int resume = root < lane_end ? root : DONE;
     int cursor = __reduce_min_sync(0xffffffffu, resume);
     float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
     int4 b = make_int4(0, 0, 0, 0);
-    if (cursor < end) load_sector0(nodes + cursor, a, b);
-    while (cursor < end) {
+    if (cursor != DONE) load_sector0(nodes + cursor, a, b);
+    while (cursor != DONE) {
         const NodeF32* nd = nodes + cursor;
         float4 m0, m1, m2, m3, m4, m5;
         ld_v8(&nd->m0, m0, m1);
@@ -415,11 +405,12 @@ k_query_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
             } else {
                 resume = cursor + 1;
             }
+            if (resume >= lane_end) resume = DONE;
         }
         const int nc = __reduce_min_sync(0xffffffffu, resume);
         float4 an = a;
         int4 bn = b;
-        if (nc < end) load_sector0(nodes + nc, an, bn);  // next step's test sector, in flight now
+        if (nc != DONE) load_sector0(nodes + nc, an, bn);  // next step's test sector, in flight
         if (far) {
             kahan_add(s, c, taylor_f32(m0, m1, m2, m3, m4, m5, dx, dy, dz, d2, __int_as_float(b.w)));
             if (STATS) ++qc.far;
@@ -429,8 +420,8 @@ k_query_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
             const int cnt = b.z;  // warp-uniform (same node for all lanes), <= WARP_LEAF_MAX
             const int nl = __popc(lm);
             const float4* src = reinterpret_cast<const float4*>(tris + b.y);
-            for (int j = lane; j < 3 * cnt; j += 32) leafbuf[w][j] = __ldg(src + j);
-            if (need_leaf) qbuf[w][__popc(lm & lt)] = make_float4(qx, qy, qz, 0.f);
+            for (int j = lane; j < 3 * cnt; j += 32) sm.leaf[j] = __ldg(src + j);
+            if (need_leaf) sm.q[__popc(lm & lt)] = make_float4(qx, qy, qz, 0.f);
             __syncwarp();
             const int np = nl * cnt;
             const float inv = 1.0f / (float)cnt;
@@ -439,18 +430,17 @@ k_query_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
                 if (p < np) {
                     const int r = (int)(((float)p + 0.5f) * inv);  // p = r * cnt + t
                     const int t = p - r * cnt;
-                    const float4 qq = qbuf[w][r];
-                    const float4 t0 = leafbuf[w][3 * t], t1 = leafbuf[w][3 * t + 1],
-                                 t2 = leafbuf[w][3 * t + 2];
-                    resbuf[w][p] = tri_omega_mixed<STATS>(t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z,
-                                                          t1.w, t2.x, t2.y, t2.z, qq.x, qq.y, qq.z,
-                                                          tau, cond, qc);
+                    const float4 qq = sm.q[r];
+                    const float4 t0 = sm.leaf[3 * t], t1 = sm.leaf[3 * t + 1], t2 = sm.leaf[3 * t + 2];
+                    sm.res[p] = tri_omega_mixed<STATS>(t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z,
+                                                       t1.w, t2.x, t2.y, t2.z, qq.x, qq.y, qq.z,
+                                                       tau, cond, qc);
                 }
             }
             __syncwarp();
             if (need_leaf) {
                 const int r = __popc(lm & lt);
-                for (int t = 0; t < cnt; ++t) kahan_add(s, c, resbuf[w][r * cnt + t]);
+                for (int t = 0; t < cnt; ++t) kahan_add(s, c, sm.res[r * cnt + t]);
                 if (STATS) qc.tri += cnt;
             }
             __syncwarp();
@@ -464,12 +454,83 @@ k_query_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
         a = an;
         b = bn;
     }
+}
+
+template <bool STATS, int MINB>
+__global__ void __launch_bounds__(WARP_BLOCK, MINB)
+k_query_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
+             const MeshInfo mi, const float* __restrict__ Q, const uint32_t* __restrict__ order,
+             int64_t n, float beta, float* __restrict__ omega, uint8_t* __restrict__ inside,
+             unsigned* __restrict__ status, unsigned long long* __restrict__ stats) {
+    __shared__ WarpSmem smem[WARP_BLOCK / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k - lane >= n) return;  // whole warp out of range (warp-uniform)
+    const bool valid = k < n;
+    QCounters qc;
+    float qx = 0.f, qy = 0.f, qz = 0.f;
+    int64_t qi = 0;
+    if (valid) {
+        qi = order ? (int64_t)order[k] : k;
+        qx = Q[3 * qi];
+        qy = Q[3 * qi + 1];
+        qz = Q[3 * qi + 2];
+    }
+    float s = 0.f, c = 0.f;
+    warp_walk<STATS>(nodes, tris, valid ? mi.root : DONE, mi.end, mi.tau, mi.cond, qx, qy, qz,
+                     beta, smem[w], s, c, qc, status);
     if (valid) {
         const float res = s - c;
         if (omega) omega[qi] = res;
         if (inside) inside[qi] = (double)res > TWO_PI_D ? 1 : 0;
     }
     if (STATS) flush_stats(qc, stats);
+}
+
+// Forest: one persistent launch over all meshes. Queries are sorted by (mesh, Morton code); each
+// warp takes the next 32 sorted queries from a global work counter until none are left.
+template <int MINB>
+__global__ void __launch_bounds__(WARP_BLOCK, MINB)
+k_forest_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
+              const MeshInfo* __restrict__ meshes, const float* __restrict__ Q,
+              const uint64_t* __restrict__ sorted_keys, const uint32_t* __restrict__ order,
+              int64_t n, float beta, float* __restrict__ omega, uint8_t* __restrict__ inside,
+              unsigned* __restrict__ work, unsigned* __restrict__ status) {
+    __shared__ WarpSmem smem[WARP_BLOCK / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t nchunks = (n + 31) / 32;
+    QCounters qc;
+    while (true) {
+        unsigned chunk = 0;
+        if (lane == 0) chunk = atomicAdd(work, 1u);
+        chunk = __shfl_sync(0xffffffffu, chunk, 0);
+        if ((int64_t)chunk >= nchunks) break;
+        const int64_t k = (int64_t)chunk * 32 + lane;
+        const bool valid = k < n;
+        float qx = 0.f, qy = 0.f, qz = 0.f;
+        int64_t qi = 0;
+        int root = DONE, end = DONE;
+        float tau = 0.f, cond = 0.f;
+        if (valid) {
+            qi = order[k];
+            qx = Q[3 * qi];
+            qy = Q[3 * qi + 1];
+            qz = Q[3 * qi + 2];
+            const MeshInfo& mi = meshes[sorted_keys[k] >> 30];
+            root = mi.root < 0 ? DONE : mi.root;
+            end = mi.end;
+            tau = mi.tau;
+            cond = mi.cond;
+        }
+        float s = 0.f, c = 0.f;
+        warp_walk<false>(nodes, tris, root, end, tau, cond, qx, qy, qz, beta, smem[w], s, c, qc,
+                         status);
+        if (valid) {
+            const float res = s - c;
+            if (omega) omega[qi] = res;
+            if (inside) inside[qi] = (double)res > TWO_PI_D ? 1 : 0;
+        }
+    }
 }
 
 // ---- plain FP64 form ----------------------------------------------------------------------------
@@ -556,6 +617,32 @@ __global__ void k_query_keys(const float* __restrict__ Q, int64_t n, const MeshI
         code |= spread3q((unsigned)qv) << (2 - a);
     }
     keys[k] = code;
+    vals[k] = (uint32_t)k;
+}
+
+__global__ void k_forest_keys(const float* __restrict__ Q, int64_t n,
+                              const int64_t* __restrict__ qoff, int nmeshes,
+                              const MeshInfo* __restrict__ meshes, uint64_t* __restrict__ keys,
+                              uint32_t* __restrict__ vals) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    int lo = 0, hi = nmeshes - 1;  // last mesh with qoff[m] <= k
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (qoff[mid] <= k) lo = mid; else hi = mid - 1;
+    }
+    const MeshInfo& mi = meshes[lo];
+    unsigned code = 0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float ext = mi.hi[a] - mi.lo[a];
+        const float l0 = mi.lo[a] - 0.25f * ext;
+        const float inv = ext > 0.f ? 1.0f / (1.5f * ext) : 0.f;
+        const float u = (Q[3 * k + a] - l0) * inv * 1024.0f;
+        const int qv = u >= 0.f ? (int)fminf(u, 1023.0f) : 0;
+        code |= spread3q((unsigned)qv) << (2 - a);
+    }
+    keys[k] = ((uint64_t)lo << 30) | code;
     vals[k] = (uint32_t)k;
 }
 
@@ -680,12 +767,53 @@ void query_mesh(const Engine& e, int mesh, const QueryArgs& a, const float* d_po
 void query_forest(const Engine& e, const QueryArgs& a, const float* d_points,
                   const int64_t* query_offsets, float* d_omega, uint8_t* d_inside,
                   cudaStream_t st) {
-    for (int64_t m = 0; m < e.nmeshes; ++m) {
-        const int64_t q0 = query_offsets[m], q1 = query_offsets[m + 1];
-        if (q1 <= q0) continue;
-        query_mesh(e, (int)m, a, d_points + 3 * q0, q1 - q0, d_omega ? d_omega + q0 : nullptr,
-                   d_inside ? d_inside + q0 : nullptr, nullptr, nullptr, st);
+    const int64_t n = query_offsets[e.nmeshes];
+    if (n <= 0) return;
+    if (a.precision == FWN_PRECISION_FP64 || e.num_nodes == 0) {
+        // the plain form: one launch per mesh
+        for (int64_t m = 0; m < e.nmeshes; ++m) {
+            const int64_t q0 = query_offsets[m], q1 = query_offsets[m + 1];
+            if (q1 <= q0) continue;
+            query_mesh(e, (int)m, a, d_points + 3 * q0, q1 - q0, d_omega ? d_omega + q0 : nullptr,
+                       d_inside ? d_inside + q0 : nullptr, nullptr, nullptr, st);
+        }
+        return;
     }
+    if (!e.nodes32) throw Error(FWN_INVALID_ARG, "engine was built without FP32 records (FWN_RECORDS_F32)");
+    if (n > (int64_t)UINT32_MAX) throw Error(FWN_INVALID_ARG, "too many forest queries");
+    int mesh_bits = 0;
+    while ((1ll << mesh_bits) < e.nmeshes) ++mesh_bits;
+    const size_t nb = (size_t)n;
+    const size_t bytes = 256 + (e.nmeshes + 1) * sizeof(int64_t) + 2 * nb * sizeof(uint64_t) +
+                         2 * nb * sizeof(uint32_t) + radix_sort_temp_bytes(n, 8) + 1024;
+    Scratch buf(bytes, st);
+    char* p = buf.as<char>();
+    unsigned* d_status = reinterpret_cast<unsigned*>(p);          // [0]: status, [1]: work counter
+    int64_t* d_qoff = reinterpret_cast<int64_t*>(p + 256);
+    uint64_t* ka = reinterpret_cast<uint64_t*>(p + 256 + ((e.nmeshes + 1) * sizeof(int64_t) + 255) / 256 * 256);
+    uint64_t* kb = ka + nb;
+    uint32_t* va = reinterpret_cast<uint32_t*>(kb + nb);
+    uint32_t* vb = va + nb;
+    void* tmp = vb + nb;
+    FWN_CUDA_CHECK(cudaMemsetAsync(d_status, 0, 2 * sizeof(unsigned), st));
+    FWN_CUDA_CHECK(cudaMemcpyAsync(d_qoff, query_offsets, (e.nmeshes + 1) * sizeof(int64_t),
+                                   cudaMemcpyHostToDevice, st));
+    k_forest_keys<<<grid_for(n, 256), 256, 0, st>>>(d_points, n, d_qoff, (int)e.nmeshes, e.meshes,
+                                                   ka, va);
+    const bool in_b = radix_sort_u64(ka, va, kb, vb, n, 30 + mesh_bits, tmp, st);
+    const uint64_t* keys = in_b ? kb : ka;
+    const uint32_t* order = in_b ? vb : va;
+    int dev = 0, sms = 0, per_sm = 0;
+    FWN_CUDA_CHECK(cudaGetDevice(&dev));
+    FWN_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    FWN_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_forest_warp<8>, WARP_BLOCK, 0));
+    const int64_t chunks = (n + 31) / 32;
+    const int64_t want = (chunks + WARP_BLOCK / 32 - 1) / (WARP_BLOCK / 32);
+    const unsigned grid = (unsigned)std::min<int64_t>(want, (int64_t)sms * std::max(per_sm, 1));
+    k_forest_warp<8><<<grid, WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, e.meshes, d_points, keys, order,
+                                                 n, a.beta, d_omega, d_inside, d_status + 1,
+                                                 d_status);
+    FWN_CUDA_CHECK(cudaGetLastError());
 }
 
 // Scratch layout of query_mesh_prealloc: [status word, 256 B][4 x n u32 sort keys/values]
