@@ -83,7 +83,8 @@ typedef struct fwn_config {
     float fp64_cond;       /* ... and its FP32 evaluation is ill-conditioned: |a||b||c| >
                               fp64_cond * |(det, D)|, or det is within rounding of 0 with D <= 0.
                               0 = every triangle within the distance. Default 4 */
-    int32_t reserved[7];
+    int32_t tuning;        /* schedule variant (0 = default; set by fwn_autotune) */
+    int32_t reserved[6];
 } fwn_config;
 
 /* Per-query options (override the handle's defaults; pass NULL for defaults). */
@@ -107,6 +108,18 @@ typedef struct fwn_query_stats {
     uint64_t warp_steps;       /* node steps summed over warps (max over the warp's lanes);
                                   nodes_tested / (32 * warp_steps) = lane utilisation */
 } fwn_query_stats;
+
+/* Result of fwn_autotune: the fastest (leaf_size, traversal, block_size, tuning) on the sample. */
+typedef struct fwn_tune_result {
+    int32_t leaf_size;
+    int32_t traversal;
+    int32_t block_size;
+    int32_t tuning;
+    double ms;                 /* median device time of the winning configuration on the sample */
+    int32_t candidates;        /* configurations timed (0 when the result came from the cache) */
+    int32_t from_cache;
+    int32_t reserved[4];
+} fwn_tune_result;
 
 typedef struct fwn_info {
     int64_t num_vertices;
@@ -193,6 +206,19 @@ FWN_API fwn_status fwn_export_tree(fwn_handle h, int32_t* skip, int32_t* tri_beg
  * component, column j=offset component) M2(18, [i][xx,yy,zz,xy,xz,yz]). Needs FWN_RECORDS_F64 or
  * a build that kept the staging records (tests). */
 FWN_API fwn_status fwn_export_moments(fwn_handle h, double* moments);
+
+/* Autotuner (no reference counterpart: the reference has no tunable parameters). For one mesh
+ * (DEVICE arrays) and a representative DEVICE sample of query points, builds the tree for leaf
+ * sizes 4, 8 and 16 and times every query schedule (warp cursor with and without the register
+ * cap; thread per query with blocks of 64/128/256) with CUDA events; returns the fastest. Apply it
+ * with cfg.leaf_size, cfg.traversal, cfg.block_size, cfg.tuning. `base` gives beta and the
+ * precision knobs (NULL = defaults). cache_path (may be NULL) names a text file keyed by GPU name
+ * and log2 of the triangle and query counts: a hit returns without timing, a miss appends.
+ * Synchronous on `stream`. */
+FWN_API fwn_status fwn_autotune(const float* d_vertices, int64_t num_vertices,
+                                const int32_t* d_triangles, int64_t num_triangles,
+                                const float* d_points, int64_t num_points, const fwn_config* base,
+                                const char* cache_path, fwn_tune_result* out, void* stream);
 
 /* ---- Forest: many meshes built and queried together (one launch per stage over all meshes).
  * vertices/triangles are concatenated; triangle indices are LOCAL to their mesh.

@@ -16,7 +16,7 @@ from pathlib import Path
 
 import numpy as np
 
-__all__ = ["FastWindingNumber", "Forest", "WindingError", "library", "config_default",
+__all__ = ["FastWindingNumber", "Forest", "WindingError", "library", "config_default", "autotune",
            "PRECISION_MIXED", "PRECISION_FP64", "TRAVERSAL_AUTO", "TRAVERSAL_THREAD",
            "TRAVERSAL_WARP", "RECORDS_F32", "RECORDS_F64", "RECORDS_MOMENTS"]
 
@@ -43,7 +43,7 @@ class fwn_config(C.Structure):
     _fields_ = [("beta", C.c_float), ("leaf_size", C.c_int32), ("records", C.c_int32),
                 ("precision", C.c_int32), ("traversal", C.c_int32), ("block_size", C.c_int32),
                 ("sort_queries", C.c_int32), ("fp64_near_scale", C.c_float),
-                ("fp64_cond", C.c_float), ("reserved", C.c_int32 * 7)]
+                ("fp64_cond", C.c_float), ("tuning", C.c_int32), ("reserved", C.c_int32 * 6)]
 
 
 class fwn_query_opts(C.Structure):
@@ -61,6 +61,15 @@ class fwn_query_stats(C.Structure):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}
 
 
+class fwn_tune_result(C.Structure):
+    _fields_ = [("leaf_size", C.c_int32), ("traversal", C.c_int32), ("block_size", C.c_int32),
+                ("tuning", C.c_int32), ("ms", C.c_double), ("candidates", C.c_int32),
+                ("from_cache", C.c_int32), ("reserved", C.c_int32 * 4)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
 class fwn_info(C.Structure):
     _fields_ = [("num_vertices", C.c_int64), ("num_triangles", C.c_int64),
                 ("num_nodes", C.c_int64), ("num_leaves", C.c_int64), ("num_meshes", C.c_int64),
@@ -75,7 +84,7 @@ _lib = None
 EXPORTS = ["fwn_config_default", "fwn_last_error", "fwn_version", "fwn_build", "fwn_build_device",
            "fwn_destroy", "fwn_get_info", "fwn_query", "fwn_query_ex", "fwn_query_host",
            "fwn_export_tree", "fwn_export_moments", "fwn_forest_build",
-           "fwn_forest_build_device", "fwn_forest_query", "fwn_query_noalloc"]
+           "fwn_forest_build_device", "fwn_forest_query", "fwn_query_noalloc", "fwn_autotune"]
 
 
 def library():
@@ -110,10 +119,12 @@ def library():
                                           C.POINTER(P)]
     L.fwn_forest_query.argtypes = [P, P, P, P, P, C.POINTER(fwn_query_opts), P]
     L.fwn_query_noalloc.argtypes = [P, P, i64, P, P, P]
+    L.fwn_autotune.argtypes = [P, i64, P, i64, P, i64, C.POINTER(fwn_config), C.c_char_p,
+                               C.POINTER(fwn_tune_result), P]
     for name in ("fwn_build", "fwn_build_device", "fwn_destroy", "fwn_get_info", "fwn_query",
                  "fwn_query_ex", "fwn_query_host", "fwn_export_tree", "fwn_export_moments",
                  "fwn_forest_build", "fwn_forest_build_device", "fwn_forest_query",
-                 "fwn_query_noalloc"):
+                 "fwn_query_noalloc", "fwn_autotune"):
         getattr(L, name).restype = st
     _lib = L
     return L
@@ -357,3 +368,27 @@ class Forest(FastWindingNumber):
                                           C.c_void_p(w.data_ptr()), C.c_void_p(ins.data_ptr()),
                                           C.byref(o), _stream_ptr(stream)))
         return w, ins
+
+
+def autotune(vertices, facets, points, *, cache_path=None, config: fwn_config | None = None,
+             **cfg_overrides) -> dict:
+    """Times every (leaf size, schedule, block, variant) candidate on a sample of query points
+    and returns the fastest; ``result["config"]`` can be passed as keyword arguments to
+    ``FastWindingNumber``. With ``cache_path`` the choice is cached per GPU and size bucket."""
+    import torch
+    V = torch.as_tensor(np.asarray(vertices, np.float32)).cuda() if not _is_cuda_tensor(vertices) \
+        else vertices.detach().to(torch.float32).contiguous()
+    F = torch.as_tensor(np.asarray(facets, np.int32)).cuda() if not _is_cuda_tensor(facets) \
+        else facets.detach().to(torch.int32).contiguous()
+    Q = torch.as_tensor(np.asarray(points, np.float32)).cuda() if not _is_cuda_tensor(points) \
+        else points.detach().to(torch.float32).contiguous()
+    cfg = config if config is not None else config_default(**cfg_overrides)
+    r = fwn_tune_result()
+    _check(library().fwn_autotune(C.c_void_p(V.data_ptr()), V.shape[0], C.c_void_p(F.data_ptr()),
+                                  F.shape[0], C.c_void_p(Q.data_ptr()), Q.reshape(-1, 3).shape[0],
+                                  C.byref(cfg), cache_path.encode() if cache_path else None,
+                                  C.byref(r), _stream_ptr(None)))
+    d = r.as_dict()
+    d["config"] = {"leaf_size": r.leaf_size, "traversal": r.traversal,
+                   "block_size": r.block_size, "tuning": r.tuning}
+    return d

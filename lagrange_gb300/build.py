@@ -34,6 +34,7 @@ SOURCES = [
     ("forest.cu", []),
     ("fwn_capi.cu", []),
     ("noalloc.cu", []),
+    ("autotune.cu", []),
 ]
 
 

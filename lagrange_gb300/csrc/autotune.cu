@@ -1,0 +1,174 @@
+// Autotuner: picks the leaf size (build), the traversal schedule, block size and register-cap
+// variant (query) for one mesh and a representative query sample, by timing every candidate with
+// CUDA events on the device. beta does not enter the choice (the schedule and block shape are
+// tuned at the caller's beta, which only changes how deep the walk goes).
+//
+// Optional cache: a text file with one line per (GPU name, log2 triangles, log2 queries) key:
+//   <gpu name>|<log2 nf>|<log2 n> <leaf> <traversal> <block> <tuning> <ms>
+// A hit skips the timing; a miss appends the new line.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "fwn_internal.cuh"
+
+namespace fwn {
+namespace {
+
+struct Candidate {
+    int traversal, block, tuning;
+};
+
+const Candidate kCandidates[] = {
+    {FWN_TRAVERSAL_WARP, 128, 0},    // warp cursor, 64-register cap
+    {FWN_TRAVERSAL_WARP, 128, 2},    // warp cursor, no register cap
+    {FWN_TRAVERSAL_THREAD, 64, 0},   // thread per query
+    {FWN_TRAVERSAL_THREAD, 128, 0},
+    {FWN_TRAVERSAL_THREAD, 256, 0},
+};
+const int kLeafSizes[] = {4, 8, 16};
+
+std::mutex g_cache_mutex;
+
+int log2_bucket(int64_t x) {
+    int b = 0;
+    while (x > 1) {
+        x >>= 1;
+        ++b;
+    }
+    return b;
+}
+
+std::string cache_key(int64_t nf, int64_t n) {
+    int dev = 0;
+    cudaDeviceProp prop;
+    FWN_CUDA_CHECK(cudaGetDevice(&dev));
+    FWN_CUDA_CHECK(cudaGetDeviceProperties(&prop, dev));
+    std::string name(prop.name);
+    for (char& ch : name)
+        if (ch == ' ' || ch == '|') ch = '_';
+    return name + "|" + std::to_string(log2_bucket(nf)) + "|" + std::to_string(log2_bucket(n));
+}
+
+bool cache_lookup(const char* path, const std::string& key, fwn_tune_result* out) {
+    std::lock_guard<std::mutex> lock(g_cache_mutex);
+    std::ifstream f(path);
+    if (!f) return false;
+    std::string line;
+    while (std::getline(f, line)) {
+        std::istringstream is(line);
+        std::string k;
+        fwn_tune_result r;
+        std::memset(&r, 0, sizeof(r));
+        if (!(is >> k >> r.leaf_size >> r.traversal >> r.block_size >> r.tuning >> r.ms)) continue;
+        if (k == key) {
+            r.from_cache = 1;
+            *out = r;
+            return true;
+        }
+    }
+    return false;
+}
+
+void cache_store(const char* path, const std::string& key, const fwn_tune_result& r) {
+    std::lock_guard<std::mutex> lock(g_cache_mutex);
+    std::ofstream f(path, std::ios::app);
+    if (!f) return;  // a read-only cache location only loses the caching
+    f << key << " " << r.leaf_size << " " << r.traversal << " " << r.block_size << " " << r.tuning
+      << " " << r.ms << "\n";
+}
+
+}  // namespace
+}  // namespace fwn
+
+using namespace fwn;
+
+extern "C" FWN_API fwn_status fwn_autotune(const float* d_V, int64_t nv, const int32_t* d_F,
+                                           int64_t nf, const float* d_Q, int64_t n,
+                                           const fwn_config* base, const char* cache_path,
+                                           fwn_tune_result* out, void* stream) {
+    try {
+        if (!out) throw Error(FWN_INVALID_ARG, "out is null");
+        std::memset(out, 0, sizeof(*out));
+        if (nv < 0 || nf < 0 || n <= 0) throw Error(FWN_INVALID_ARG, "sizes must be >= 0 (n > 0)");
+        if ((nv && !d_V) || (nf && !d_F) || !d_Q) throw Error(FWN_INVALID_ARG, "null pointer");
+        if (n > (int64_t)INT32_MAX) throw Error(FWN_INVALID_ARG, "at most 2^31-1 sample points");
+        fwn_config cfg;
+        fwn_config_default(&cfg);
+        if (base) cfg = *base;
+        cfg.records = FWN_RECORDS_F32;
+        const std::string key = cache_key(nf, n);
+        if (cache_path && cache_lookup(cache_path, key, out)) return FWN_OK;
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        Scratch wbuf((size_t)n * sizeof(float), st), ibuf((size_t)n, st);
+        cudaEvent_t e0, e1;
+        FWN_CUDA_CHECK(cudaEventCreate(&e0));
+        FWN_CUDA_CHECK(cudaEventCreate(&e1));
+        std::unique_ptr<cudaEvent_t[], void (*)(cudaEvent_t*)> guard(
+            new cudaEvent_t[2]{e0, e1}, [](cudaEvent_t* p) {
+                cudaEventDestroy(p[0]);
+                cudaEventDestroy(p[1]);
+                delete[] p;
+            });
+        fwn_tune_result best;
+        std::memset(&best, 0, sizeof(best));
+        best.ms = 1e300;
+        int evaluated = 0;
+        for (int leaf : kLeafSizes) {
+            Engine e;
+            e.cfg = cfg;
+            e.cfg.leaf_size = leaf;
+            FWN_CUDA_CHECK(cudaGetDevice(&e.device));
+            const int64_t voff[2] = {0, nv}, foff[2] = {0, nf};
+            build_forest(e, d_V, voff, d_F, foff, 1, st);
+            for (const Candidate& cand : kCandidates) {
+                QueryArgs a = resolve_query_args(e, nullptr);
+                a.precision = FWN_PRECISION_MIXED;
+                a.traversal = cand.traversal;
+                a.block_size = cand.traversal == FWN_TRAVERSAL_WARP ? 128 : cand.block;
+                a.tuning = cand.tuning;
+                // one warm-up, then the median of three timed passes
+                query_mesh(e, 0, a, d_Q, n, wbuf.as<float>(), ibuf.as<uint8_t>(), nullptr,
+                           nullptr, st);
+                float t[3];
+                for (int r = 0; r < 3; ++r) {
+                    FWN_CUDA_CHECK(cudaEventRecord(e0, st));
+                    query_mesh(e, 0, a, d_Q, n, wbuf.as<float>(), ibuf.as<uint8_t>(), nullptr,
+                               nullptr, st);
+                    FWN_CUDA_CHECK(cudaEventRecord(e1, st));
+                    FWN_CUDA_CHECK(cudaEventSynchronize(e1));
+                    FWN_CUDA_CHECK(cudaEventElapsedTime(&t[r], e0, e1));
+                }
+                std::sort(t, t + 3);
+                ++evaluated;
+                if (t[1] < best.ms) {
+                    best.ms = t[1];
+                    best.leaf_size = leaf;
+                    best.traversal = a.traversal;
+                    best.block_size = a.block_size;
+                    best.tuning = a.tuning;
+                }
+            }
+        }
+        best.candidates = evaluated;
+        *out = best;
+        if (cache_path) cache_store(cache_path, key, best);
+        return FWN_OK;
+    } catch (const Error& err) {
+        set_last_error(err.what());
+        return err.status;
+    } catch (const std::exception& err) {
+        set_last_error(err.what());
+        return FWN_INTERNAL;
+    } catch (...) {
+        set_last_error("unknown error");
+        return FWN_INTERNAL;
+    }
+}

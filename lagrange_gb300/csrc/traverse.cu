@@ -665,6 +665,7 @@ QueryArgs resolve_query_args(const Engine& e, const fwn_query_opts* o) {
     a.block_size = e.cfg.block_size;
     a.sort_queries = e.cfg.sort_queries;
     a.beta = e.cfg.beta;
+    a.tuning = e.cfg.tuning;
     if (o) {
         if (o->precision >= 0) a.precision = o->precision;
         if (o->traversal >= 0) a.traversal = o->traversal;

@@ -1,0 +1,38 @@
+"""Autotuner (fwn_autotune): picks leaf size, schedule, block and variant by timing candidates
+on the device; the tuned engine must give the same answers (within the parity tolerance) and the
+cache must return the stored choice without timing."""
+import math
+
+import numpy as np
+import pytest
+
+import lagrange_gb300 as fwn
+from lagrange_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+FOUR_PI = 4 * math.pi
+
+
+def test_autotune_choice_and_cache(tmp_path):
+    import torch
+    torch.cuda.set_device(0)
+    wl = W.displaced_icosphere_workload(nu=60, n_queries=60_000)
+    cache = tmp_path / "tune.txt"
+    r = fwn.autotune(wl.V, wl.F, wl.Q, cache_path=str(cache))
+    assert r["from_cache"] == 0 and r["candidates"] == 15 and r["ms"] > 0
+    assert r["leaf_size"] in (4, 8, 16)
+    assert r["traversal"] in (fwn.TRAVERSAL_THREAD, fwn.TRAVERSAL_WARP)
+    assert r["block_size"] % 32 == 0
+    # the cached answer comes back without timing
+    r2 = fwn.autotune(wl.V, wl.F, wl.Q, cache_path=str(cache))
+    assert r2["from_cache"] == 1 and r2["candidates"] == 0
+    assert r2["config"] == r["config"]
+    assert len(cache.read_text().splitlines()) == 1
+    # the tuned engine agrees with the plain FP64 form built with the same leaf size
+    eng = fwn.FastWindingNumber(wl.V, wl.F, records=fwn.RECORDS_F32 | fwn.RECORDS_F64,
+                                **r["config"])
+    Qd = torch.from_numpy(wl.Q).cuda()
+    w, ins = eng.query(Qd)
+    w64, _ = eng.query(Qd, precision=fwn.PRECISION_FP64)
+    torch.cuda.synchronize()
+    assert float((w.double() - w64.double()).abs().max()) / FOUR_PI <= 2e-6
