@@ -220,6 +220,26 @@ FWN_API fwn_status fwn_autotune(const float* d_vertices, int64_t num_vertices,
                                 const float* d_points, int64_t num_points, const fwn_config* base,
                                 const char* cache_path, fwn_tune_result* out, void* stream);
 
+/* Voxel-grid sign pass (batched form of the winding-number signing in volume::mesh_to_volume,
+ * modules/volume/src/mesh_to_volume.cpp:156-183, which calls is_inside once per voxel). Classifies
+ * the centres of an nx x ny x nz grid of mesh `mesh` (0 for a single-mesh handle): voxel
+ * (i, j, k) has centre fmaf(i + 0.5, spacing[0], origin[0]) (and likewise for y, z); outputs are
+ * DEVICE arrays indexed i + nx * (j + ny * k). The centres are generated on the device (no point
+ * array, no sort). Either output may be NULL. Asynchronous on `stream`. */
+FWN_API fwn_status fwn_query_grid(fwn_handle h, int64_t mesh, const float* origin,
+                                  const float* spacing, const int64_t* dims, float* d_omega,
+                                  uint8_t* d_inside, void* stream);
+
+/* Orientation test of modules/winding/examples/fix_orientation.cpp:75-115 for every triangle f of
+ * a second mesh (DEVICE arrays, local indices): with unit normal n_f (zero for a degenerate
+ * triangle) and barycentre b_f, criterion_f = (Omega(b_f + eps n_f) - Omega(b_f - eps n_f)) /
+ * (4 pi) against this handle's (reference) mesh, and flip_f = criterion_f > threshold. The
+ * example's defaults are eps = 1e-2, threshold = 0.8. Either output may be NULL. Synchronous. */
+FWN_API fwn_status fwn_orientation_criterion(fwn_handle h, const float* d_vertices,
+                                             int64_t num_vertices, const int32_t* d_triangles,
+                                             int64_t num_triangles, float eps, float threshold,
+                                             float* d_criterion, uint8_t* d_flip, void* stream);
+
 /* ---- Forest: many meshes built and queried together (one launch per stage over all meshes).
  * vertices/triangles are concatenated; triangle indices are LOCAL to their mesh.
  * vertex_offsets [num_meshes+1], triangle_offsets [num_meshes+1] (host int64 prefix offsets).

@@ -84,7 +84,8 @@ _lib = None
 EXPORTS = ["fwn_config_default", "fwn_last_error", "fwn_version", "fwn_build", "fwn_build_device",
            "fwn_destroy", "fwn_get_info", "fwn_query", "fwn_query_ex", "fwn_query_host",
            "fwn_export_tree", "fwn_export_moments", "fwn_forest_build",
-           "fwn_forest_build_device", "fwn_forest_query", "fwn_query_noalloc", "fwn_autotune"]
+           "fwn_forest_build_device", "fwn_forest_query", "fwn_query_noalloc", "fwn_autotune",
+           "fwn_query_grid", "fwn_orientation_criterion"]
 
 
 def library():
@@ -119,12 +120,15 @@ def library():
                                           C.POINTER(P)]
     L.fwn_forest_query.argtypes = [P, P, P, P, P, C.POINTER(fwn_query_opts), P]
     L.fwn_query_noalloc.argtypes = [P, P, i64, P, P, P]
+    L.fwn_query_grid.argtypes = [P, i64, P, P, P, P, P, P]
+    L.fwn_orientation_criterion.argtypes = [P, P, i64, P, i64, C.c_float, C.c_float, P, P, P]
     L.fwn_autotune.argtypes = [P, i64, P, i64, P, i64, C.POINTER(fwn_config), C.c_char_p,
                                C.POINTER(fwn_tune_result), P]
     for name in ("fwn_build", "fwn_build_device", "fwn_destroy", "fwn_get_info", "fwn_query",
                  "fwn_query_ex", "fwn_query_host", "fwn_export_tree", "fwn_export_moments",
                  "fwn_forest_build", "fwn_forest_build_device", "fwn_forest_query",
-                 "fwn_query_noalloc", "fwn_autotune"):
+                 "fwn_query_noalloc", "fwn_autotune", "fwn_query_grid",
+                 "fwn_orientation_criterion"):
         getattr(L, name).restype = st
     _lib = L
     return L
@@ -303,6 +307,61 @@ class FastWindingNumber:
         single = np.ndim(points) == 1 and not _is_cuda_tensor(points)
         _, ins = self.query(points, omega=False)
         return bool(ins[0]) if single else (ins.astype(bool) if isinstance(ins, np.ndarray) else ins)
+
+    # ---- callers of the path ----------------------------------------------------------------
+    def query_grid(self, origin, spacing, dims, *, mesh: int = 0, omega=True, inside=True,
+                   stream=None):
+        """Voxel-grid sign pass: classifies the centres of a dims = (nx, ny, nz) grid, centre of
+        voxel (i, j, k) = origin + (i + 0.5, j + 0.5, k + 0.5) * spacing (one fused rounding per
+        axis). Returns CUDA tensors of shape (nz, ny, nx) (x fastest)."""
+        import torch
+        nx, ny, nz = (int(d) for d in dims)
+        o = (C.c_float * 3)(*[float(x) for x in origin])
+        s = (C.c_float * 3)(*[float(x) for x in spacing])
+        d = (C.c_int64 * 3)(nx, ny, nz)
+        n = nx * ny * nz
+        w = torch.empty(n, dtype=torch.float32, device="cuda") if omega else None
+        ins = torch.empty(n, dtype=torch.uint8, device="cuda") if inside else None
+        ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else None  # noqa: E731
+        _check(library().fwn_query_grid(self._h, mesh, o, s, d, ptr(w), ptr(ins),
+                                        _stream_ptr(stream)))
+        shape = (nz, ny, nx)
+        return (w.view(shape) if w is not None else None,
+                ins.view(shape) if ins is not None else None)
+
+    def orientation_criterion(self, vertices, facets, *, eps: float = 1e-2,
+                              threshold: float = 0.8, stream=None):
+        """Per-facet orientation test of another mesh against this (reference) mesh:
+        criterion = (Omega(b + eps n) - Omega(b - eps n)) / (4 pi), flip = criterion > threshold
+        (modules/winding/examples/fix_orientation.cpp:75-115). Returns CUDA tensors."""
+        import torch
+        V = vertices if _is_cuda_tensor(vertices) else torch.from_numpy(
+            np.ascontiguousarray(vertices, np.float32)).cuda()
+        F = facets if _is_cuda_tensor(facets) else torch.from_numpy(
+            np.ascontiguousarray(facets, np.int32)).cuda()
+        V = V.to(torch.float32).contiguous()
+        F = F.to(torch.int32).contiguous().reshape(-1, 3)
+        nf = F.shape[0]
+        crit = torch.empty(nf, dtype=torch.float32, device=V.device)
+        flip = torch.empty(nf, dtype=torch.uint8, device=V.device)
+        _check(library().fwn_orientation_criterion(
+            self._h, C.c_void_p(V.data_ptr()), V.shape[0], C.c_void_p(F.data_ptr()), nf,
+            float(eps), float(threshold), C.c_void_p(crit.data_ptr()), C.c_void_p(flip.data_ptr()),
+            _stream_ptr(stream)))
+        return crit, flip
+
+    def sample_inside(self, num_samples: int, *, seed: int = 0):
+        """Rejection sampling of interior points (modules/winding/examples/
+        sample_points_in_mesh.cpp:59-76): num_samples uniform points in the mesh bbox, kept where
+        is_inside holds. Returns a CUDA tensor (k, 3)."""
+        import torch
+        inf = self.info()
+        lo = torch.tensor(inf["bbox_min"], dtype=torch.float32, device="cuda")
+        hi = torch.tensor(inf["bbox_max"], dtype=torch.float32, device="cuda")
+        g = torch.Generator(device="cuda").manual_seed(seed)
+        P = lo + (hi - lo) * torch.rand((int(num_samples), 3), generator=g, device="cuda")
+        _, ins = self.query(P, omega=False)
+        return P[ins.bool()]
 
     # ---- inspection ------------------------------------------------------------------------
     def export_tree(self) -> dict:

@@ -35,6 +35,7 @@ SOURCES = [
     ("fwn_capi.cu", []),
     ("noalloc.cu", []),
     ("autotune.cu", []),
+    ("callers.cu", []),
 ]
 
 

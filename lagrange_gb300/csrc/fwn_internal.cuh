@@ -203,6 +203,10 @@ struct QueryArgs {
 void query_mesh(const Engine& e, int mesh, const QueryArgs& a, const float* d_points, int64_t n,
                 float* d_omega, uint8_t* d_inside, double* d_omega64, fwn_query_stats* stats,
                 cudaStream_t stream, bool check = false);
+// Regular voxel-centre grid of mesh `mesh` (no point array); outputs indexed i + nx (j + ny k).
+void query_grid(const Engine& e, int mesh, const QueryArgs& a, const float origin[3],
+                const float spacing[3], const int64_t dims[3], float* d_omega, uint8_t* d_inside,
+                cudaStream_t stream);
 void query_forest(const Engine& e, const QueryArgs& a, const float* d_points,
                   const int64_t* query_offsets, float* d_omega, uint8_t* d_inside,
                   cudaStream_t stream);

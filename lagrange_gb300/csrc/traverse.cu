@@ -487,6 +487,38 @@ k_query_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
     if (STATS) flush_stats(qc, stats);
 }
 
+// Regular grid: voxel (i, j, k) has centre fmaf(i + 0.5, spacing, origin) per axis and output
+// index i + nx (j + ny k). Each warp takes one 4 x 4 x 2 brick of voxels (bricks in raster order),
+// so a warp's 32 queries are spatially compact without a sort; no point array is read.
+template <int MINB>
+__global__ void __launch_bounds__(WARP_BLOCK, MINB)
+k_query_grid(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
+             const MeshInfo mi, float ox, float oy, float oz, float sx, float sy, float sz,
+             int64_t nx, int64_t ny, int64_t nz, int64_t bx, int64_t by, int64_t nbricks,
+             float beta, float* __restrict__ omega, uint8_t* __restrict__ inside,
+             unsigned* __restrict__ status) {
+    __shared__ WarpSmem smem[WARP_BLOCK / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t brick = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (brick >= nbricks) return;  // warp-uniform
+    const int64_t bi = brick % bx, bj = (brick / bx) % by, bk = brick / (bx * by);
+    const int64_t i = bi * 4 + (lane & 3), j = bj * 4 + ((lane >> 2) & 3), k = bk * 2 + (lane >> 4);
+    const bool valid = i < nx && j < ny && k < nz;
+    const float qx = fmaf((float)i + 0.5f, sx, ox);
+    const float qy = fmaf((float)j + 0.5f, sy, oy);
+    const float qz = fmaf((float)k + 0.5f, sz, oz);
+    QCounters qc;
+    float s = 0.f, c = 0.f;
+    warp_walk<false>(nodes, tris, valid ? mi.root : DONE, mi.end, mi.tau, mi.cond, qx, qy, qz,
+                     beta, smem[w], s, c, qc, status);
+    if (valid) {
+        const int64_t o = i + nx * (j + ny * k);
+        const float res = s - c;
+        if (omega) omega[o] = res;
+        if (inside) inside[o] = (double)res > TWO_PI_D ? 1 : 0;
+    }
+}
+
 // Forest: one persistent launch over all meshes. Queries are sorted by (mesh, Morton code); each
 // warp takes the next 32 sorted queries from a global work counter until none are left.
 template <int MINB>
@@ -763,6 +795,30 @@ void query_mesh(const Engine& e, int mesh, const QueryArgs& a, const float* d_po
         }
         if (sh & ST_BAD_LINK) throw Error(FWN_INTERNAL, "traversal met a non-advancing skip link");
     }
+}
+
+void query_grid(const Engine& e, int mesh, const QueryArgs& a, const float origin[3],
+                const float spacing[3], const int64_t dims[3], float* d_omega, uint8_t* d_inside,
+                cudaStream_t st) {
+    const int64_t nx = dims[0], ny = dims[1], nz = dims[2];
+    if (nx <= 0 || ny <= 0 || nz <= 0) return;
+    const MeshInfo& mi = e.meshes_h[mesh];
+    const int64_t n = nx * ny * nz;
+    if (mi.root < 0) {
+        k_fill_zero<<<grid_for(n, 256), 256, 0, st>>>(d_omega, d_inside, nullptr, n);
+        FWN_CUDA_CHECK(cudaGetLastError());
+        return;
+    }
+    if (!e.nodes32) throw Error(FWN_INVALID_ARG, "engine was built without FP32 records (FWN_RECORDS_F32)");
+    const int64_t bx = (nx + 3) / 4, by = (ny + 3) / 4, bz = (nz + 1) / 2;
+    const int64_t nbricks = bx * by * bz;
+    Scratch status(sizeof(unsigned), st);
+    FWN_CUDA_CHECK(cudaMemsetAsync(status.p, 0, sizeof(unsigned), st));
+    const int64_t threads = nbricks * 32;
+    k_query_grid<8><<<grid_for(threads, WARP_BLOCK), WARP_BLOCK, 0, st>>>(
+        e.nodes32, e.tris, mi, origin[0], origin[1], origin[2], spacing[0], spacing[1], spacing[2],
+        nx, ny, nz, bx, by, nbricks, a.beta, d_omega, d_inside, status.as<unsigned>());
+    FWN_CUDA_CHECK(cudaGetLastError());
 }
 
 void query_forest(const Engine& e, const QueryArgs& a, const float* d_points,
