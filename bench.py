@@ -19,7 +19,7 @@ since the reference library cannot be built here) on the same workload and print
 line with ``"impl": "reference"``.
 
 Multi-GPU (torchrun): every rank builds its own replica of the tree and answers its own 10M
-queries (seed offset by rank) — no collective on the data path; value = all ranks' queries /
+queries (rank r > 0: a seeded shuffle of the set) — no collective on the data path; value = all ranks' queries /
 the slowest rank's time (weak scaling).
 """
 from __future__ import annotations
@@ -364,7 +364,6 @@ def run_ours(args, rank, world, local):
                        f"{sm_max:.0f} MHz (no FP32 figure in MEASURED_PEAKS.json)",
         "per_query": {"far_evals": far / n, "tri_evals": tri / n, "nodes_tested": nodes / n,
                       "tri_fp64": stats["tri_evals_fp64"] / n,
-                      "far_tests_fp64": stats["far_tests_fp64"] / n,
                       "flops": flops / n, "l2_bytes": l2_bytes / n},
         "l2_gbs_algorithmic": l2_bytes / (ms / 1e3) / 1e9,
     }
@@ -564,6 +563,45 @@ def run_forest(args, rank, world, local):
         "meshes_per_s_build_plus_query": M / ((build_ms + ms) / 1e3),
         "clocks": clk.summary(),
     }
+    if args.workload == "voxel":
+        # the same classification through the grid sign pass: centres generated on the device,
+        # no point array and no sort (one launch per mesh)
+        res = round((fo.qoff[1] - fo.qoff[0]) ** (1 / 3))
+        grids = []
+        for m in range(M):
+            Vm = fo.V[fo.voff[m]:fo.voff[m + 1]].astype(np.float64)
+            lo, hi = Vm.min(0), Vm.max(0)
+            c, h = (lo + hi) / 2, (hi - lo) / 2 * 1.05
+            grids.append(((c - h).astype(np.float32), (2 * h / res).astype(np.float32)))
+        wg = torch.empty(n, dtype=torch.float32, device=dev)
+        ig = torch.empty(n, dtype=torch.uint8, device=dev)
+        dims = (C.c_int64 * 3)(res, res, res)
+
+        def q_grid():
+            for m, (o, s) in enumerate(grids):
+                q0 = int(fo.qoff[m])
+                fwn._check(L.fwn_query_grid(forest.handle, m, (C.c_float * 3)(*o), (C.c_float * 3)(*s),
+                                            dims, C.c_void_p(wg.data_ptr() + 4 * q0),
+                                            C.c_void_p(ig.data_ptr() + q0),
+                                            C.c_void_p(stream.cuda_stream)))
+        q_grid()
+        torch.cuda.synchronize()
+        tg = []
+        for _ in range(args.steps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            q_grid()
+            b.record(stream)
+            torch.cuda.synchronize()
+            tg.append(a.elapsed_time(b))
+        msg = sum(tg) / len(tg)
+        result["grid_path"] = {
+            "value": n / (msg / 1e3), "unit": "queries/s", "ms_per_step": msg, "launches": M,
+            "api": "fwn_query_grid (voxel centres generated on the device, no point array)",
+            "inside_fraction": float(ig.float().mean()),
+            "inside_fraction_explicit_points": float(ins.float().mean()),
+            "h2d_bytes_per_step": 0}
     if not args.no_fp64:
         w64 = torch.empty(n, dtype=torch.float32, device=dev)
         o64 = fwn._opts(precision=fwn.PRECISION_FP64)

@@ -104,7 +104,6 @@ typedef struct fwn_query_stats {
     uint64_t far_evals;        /* order-2 Taylor evaluations */
     uint64_t tri_evals;        /* exact triangle solid angles (all precisions) */
     uint64_t tri_evals_fp64;   /* of which evaluated in FP64 (mixed form only) */
-    uint64_t far_tests_fp64;   /* far tests re-decided in FP64 inside the guard band */
     uint64_t warp_steps;       /* node steps summed over warps (max over the warp's lanes);
                                   nodes_tested / (32 * warp_steps) = lane utilisation */
 } fwn_query_stats;

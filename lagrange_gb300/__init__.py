@@ -55,7 +55,7 @@ class fwn_query_opts(C.Structure):
 class fwn_query_stats(C.Structure):
     _fields_ = [("nodes_tested", C.c_uint64), ("far_evals", C.c_uint64),
                 ("tri_evals", C.c_uint64), ("tri_evals_fp64", C.c_uint64),
-                ("far_tests_fp64", C.c_uint64), ("warp_steps", C.c_uint64)]
+                ("warp_steps", C.c_uint64)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}

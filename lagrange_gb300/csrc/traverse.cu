@@ -7,10 +7,15 @@
 //   near internal               -> step to i+1 (the first child)
 // The cursor strictly increases, so every walk ends in at most num_nodes steps.
 //
+// The far/near decision is one FP32 predicate shared by every form (and by the oracle):
+//   far  <=>  fma(dx, dx, fma(dy, dy, dz*dz)) > (beta*r)^2,  d = P - q, each step rounded to
+//   float as written. The reference tree makes this decision in float as well (its engine is
+//   UT_SolidAngle<float, float>, modules/winding/src/FastWindingNumber.cpp:80), and sharing it
+//   makes the mixed and FP64 forms visit exactly the same nodes, so they differ only in
+//   arithmetic.
+//
 // Forms:
 //   mixed / thread : one thread per query, FP32 far field and near field with a Kahan sum;
-//                    far tests inside a 1e-5 guard band are re-decided with the exact FP64
-//                    expression the FP64 form uses (so both forms take identical branches);
 //                    triangles within tau = fp64_near_scale * bbox diagonal get det and the
 //                    Van Oosterom denominator in FP64.
 //   mixed / warp   : 32 queries share one cursor (warp-uniform node loads, lanes inactive until
@@ -26,7 +31,6 @@ namespace fwn {
 namespace {
 
 constexpr double TWO_PI_D = 6.283185307179586476925286766559;  // Omega/(4 pi) > 0.5 <=> Omega > 2 pi
-constexpr float GUARD = 1e-5f;
 
 __device__ __forceinline__ unsigned lanemask_lt() {
     unsigned m;
@@ -35,7 +39,7 @@ __device__ __forceinline__ unsigned lanemask_lt() {
 }
 
 struct QCounters {
-    unsigned nodes = 0, far = 0, tri = 0, tri64 = 0, test64 = 0, steps = 0;
+    unsigned nodes = 0, far = 0, tri = 0, tri64 = 0, steps = 0;
 };
 
 __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
@@ -45,13 +49,17 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
     s = t;
 }
 
-// Exact-order FP64 far test shared by the mixed and FP64 forms (P, r are float values).
-__device__ __forceinline__ bool far_test_f64(double qx, double qy, double qz, double px,
-                                             double py, double pz, double r, double beta) {
-    const double dx = __dsub_rn(px, qx), dy = __dsub_rn(py, qy), dz = __dsub_rn(pz, qz);
-    const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-    const double br = __dmul_rn(beta, r);
-    return d2 > __dmul_rn(br, br);
+// The shared far predicate (see the top of this file); also returns d = P - q and |d|^2 in
+// float. Explicit _rn intrinsics keep the compiler from contracting it differently anywhere.
+__device__ __forceinline__ bool far_pred(float px, float py, float pz, float r, float qx, float qy,
+                                         float qz, float beta, float& dx, float& dy, float& dz,
+                                         float& d2) {
+    dx = __fsub_rn(px, qx);
+    dy = __fsub_rn(py, qy);
+    dz = __fsub_rn(pz, qz);
+    d2 = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
+    const float br = __fmul_rn(beta, r);
+    return d2 > __fmul_rn(br, br);
 }
 
 // Order-2 far-field term of a node (coefficients pre-scaled, see NodeF32), d = P - q.
@@ -180,16 +188,16 @@ __device__ __forceinline__ float tri_omega_mixed(float v0x, float v0y, float v0z
 
 __device__ __forceinline__ void flush_stats(const QCounters& c, unsigned long long* stats) {
     // warp-aggregated: all lanes of the warp call this (no early exits in STATS kernels)
-    unsigned v[5] = {c.nodes, c.far, c.tri, c.tri64, c.test64};
+    unsigned v[4] = {c.nodes, c.far, c.tri, c.tri64};
 #pragma unroll
-    for (int i = 0; i < 5; ++i) {
+    for (int i = 0; i < 4; ++i) {
         unsigned s = __reduce_add_sync(0xffffffffu, v[i]);
         if ((threadIdx.x & 31) == 0 && s) atomicAdd(&stats[i], (unsigned long long)s);
     }
     // warp steps: the warp runs as many steps as its longest lane (per-lane step counts) or
     // as its shared cursor (all lanes hold the same count)
     const unsigned ws = __reduce_max_sync(0xffffffffu, c.steps);
-    if ((threadIdx.x & 31) == 0 && ws) atomicAdd(&stats[5], (unsigned long long)ws);
+    if ((threadIdx.x & 31) == 0 && ws) atomicAdd(&stats[4], (unsigned long long)ws);
 }
 
 // ---- 256-bit record loads ----------------------------------------------------------------------
@@ -219,24 +227,12 @@ __device__ __forceinline__ float taylor_node(const NodeF32* nd, float dx, float 
     return taylor_f32(m0, m1, m2, m3, m4, m5, dx, dy, dz, d2, trM1);
 }
 
-// far test: FP32 decision, re-decided with the exact FP64 expression inside the guard band
 template <bool STATS>
 __device__ __forceinline__ bool far_test(const float4 a, float qx, float qy, float qz, float beta,
                                          float& dx, float& dy, float& dz, float& d2,
                                          QCounters& qc) {
-    dx = a.x - qx;
-    dy = a.y - qy;
-    dz = a.z - qz;
-    d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-    const float br = beta * a.w;
-    const float br2 = br * br;
-    bool far = d2 > br2;
-    if (fabsf(d2 - br2) <= GUARD * br2) {
-        far = far_test_f64(qx, qy, qz, a.x, a.y, a.z, a.w, beta);
-        if (STATS) ++qc.test64;
-    }
     if (STATS) ++qc.nodes;
-    return far;
+    return far_pred(a.x, a.y, a.z, a.w, qx, qy, qz, beta, dx, dy, dz, d2);
 }
 
 // ---- mixed, one thread per query --------------------------------------------------------------
@@ -393,27 +389,28 @@ __device__ __forceinline__ void warp_walk(const NodeF32* __restrict__ nodes,
         ld_v8(&nd->m0, m0, m1);
         ld_v8(&nd->m2, m2, m3);
         ld_v8(&nd->m4, m4, m5);
-        bool far = false, need_leaf = false;
-        float dx = 0.f, dy = 0.f, dz = 0.f, d2 = 1.f;
-        if (resume == cursor) {
-            far = far_test<STATS>(a, qx, qy, qz, beta, dx, dy, dz, d2, qc);
-            if (far) {
-                resume = b.x;
-            } else if (b.z > 0) {
-                need_leaf = true;
-                resume = b.x;
-            } else {
-                resume = cursor + 1;
-            }
-            if (resume >= lane_end) resume = DONE;
-        }
+        // far test on every lane (only lanes whose resume index is the cursor use the result),
+        // with no divergent branch around it and the resume update as selects
+        const bool active = resume == cursor;
+        float dx, dy, dz, d2;
+        const bool far = far_pred(a.x, a.y, a.z, a.w, qx, qy, qz, beta, dx, dy, dz, d2);
+        if (STATS && active) ++qc.nodes;
+        const bool leafnode = b.z > 0;
+        int nr = (far || leafnode) ? b.x : cursor + 1;
+        nr = nr >= lane_end ? DONE : nr;
+        resume = active ? nr : resume;
+        const bool do_far = active && far;
+        const bool need_leaf = active && !far && leafnode;
         const int nc = __reduce_min_sync(0xffffffffu, resume);
         float4 an = a;
         int4 bn = b;
         if (nc != DONE) load_sector0(nodes + nc, an, bn);  // next step's test sector, in flight
-        if (far) {
-            kahan_add(s, c, taylor_f32(m0, m1, m2, m3, m4, m5, dx, dy, dz, d2, __int_as_float(b.w)));
-            if (STATS) ++qc.far;
+        if (__any_sync(0xffffffffu, do_far)) {  // warp-uniform: every lane evaluates, far lanes add
+            const float t = taylor_f32(m0, m1, m2, m3, m4, m5, dx, dy, dz, d2, __int_as_float(b.w));
+            if (do_far) {
+                kahan_add(s, c, t);
+                if (STATS) ++qc.far;
+            }
         }
         const unsigned lm = __ballot_sync(0xffffffffu, need_leaf);
         if (lm) {
@@ -580,14 +577,15 @@ k_query_f64(const NodeF64* __restrict__ nodes, const TriF32* __restrict__ tris, 
     if (valid) {
         const int64_t qi = order ? (int64_t)order[k] : k;
         const double qx = Q[3 * qi], qy = Q[3 * qi + 1], qz = Q[3 * qi + 2];
-        const double betad = beta;
         double s = 0.0;
         int i = mi.root;
         const int end = mi.end;
         while (i < end) {
             const NodeF64* nd = nodes + i;
             const double px = nd->P[0], py = nd->P[1], pz = nd->P[2];
-            const bool far = far_test_f64(qx, qy, qz, px, py, pz, nd->r, betad);
+            float fdx, fdy, fdz, fd2;  // P, r and q are float values: the shared predicate
+            const bool far = far_pred((float)px, (float)py, (float)pz, (float)nd->r, (float)qx,
+                                      (float)qy, (float)qz, beta, fdx, fdy, fdz, fd2);
             if (STATS) { ++qc.nodes; ++qc.steps; }
             int next;
             const int skip = nd->skip, tc = nd->tri_count;
@@ -790,8 +788,7 @@ void query_mesh(const Engine& e, int mesh, const QueryArgs& a, const float* d_po
             stats->far_evals = h[1];
             stats->tri_evals = h[2];
             stats->tri_evals_fp64 = h[3];
-            stats->far_tests_fp64 = h[4];
-            stats->warp_steps = h[5];
+            stats->warp_steps = h[4];
         }
         if (sh & ST_BAD_LINK) throw Error(FWN_INTERNAL, "traversal met a non-advancing skip link");
     }

@@ -25,11 +25,16 @@
  *                          the plain FP64 traversal. Compiled with -ffp-contract=off so keys,
  *                          topology, centres and radii match the device build bit for bit.
  */
+#include <float.h>
 #include <math.h>
 #include <pthread.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
+
+#if FLT_EVAL_METHOD != 0
+#error "float arithmetic must round to float (the shared far predicate)"
+#endif
 
 #define MORTON_BITS 30
 
@@ -885,6 +890,18 @@ static double lb_taylor(const lb_stage* s, const double* d) {
     return t;
 }
 
+/* The far/near predicate every form of the device path shares, in float, each step rounded as
+ * written: fma(dx, dx, fma(dy, dy, dz * dz)) > (beta * r)^2 with d = P - q (P and r are float
+ * values). The reference tree decides in float too (UT_SolidAngle<float, float>,
+ * modules/winding/src/FastWindingNumber.cpp:80). Needs FLT_EVAL_METHOD == 0 and no
+ * contraction (-ffp-contract=off). */
+static int lb_far_pred(const lb_stage* st, const float* q, float beta) {
+    const float dx = (float)st->P[0] - q[0], dy = (float)st->P[1] - q[1], dz = (float)st->P[2] - q[2];
+    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    const float br = beta * (float)st->r;
+    return d2 > br * br;
+}
+
 typedef struct {
     const lb_tree* T;
     const float* Q;
@@ -910,9 +927,7 @@ static void lb_q_range(void* p, int64_t b, int64_t e) {
         while (i < end) {
             const lb_stage* st = &T->st[i];
             const double dx = st->P[0] - q[0], dy = st->P[1] - q[1], dz = st->P[2] - q[2];
-            const double d2 = (dx * dx + dy * dy) + dz * dz;
-            const double br = c->beta * st->r;
-            const int far = !c->exact && d2 > br * br;
+            const int far = !c->exact && lb_far_pred(st, c->Q + 3 * qi, (float)c->beta);
             if (far) {
                 const double d[3] = {dx, dy, dz};
                 s += lb_taylor(st, d);
@@ -932,8 +947,8 @@ static void lb_q_range(void* p, int64_t b, int64_t e) {
     }
 }
 
-/* FP64 traversal of the restated LBVH (same far test as the device: |P-q|^2 > (beta r)^2,
- * each product and sum rounded separately). exact=1 evaluates every triangle. */
+/* FP64 traversal of the restated LBVH (the device's shared FP32 far predicate, lb_far_pred;
+ * FP64 far field and near field). exact=1 evaluates every triangle. */
 void oracle_lbvh_query_f64(void* h, const float* Q, const int32_t* qmesh, int64_t nq, double beta,
                            int exact, double* omega, int nthreads) {
     lb_q_ctx c = {(const lb_tree*)h, Q, qmesh, beta, omega, exact};
