@@ -51,6 +51,9 @@ BYTES_NODE_TEST = 32   # sector 0 of a NodeF32 record
 BYTES_NODE_FAR = 96    # sectors 1-3 (far-field coefficients)
 BYTES_TRI = 48
 BYTES_QUERY_IO = 12 + 4 + 1 + 4  # point in, Omega + inside out, sort index
+# DRAM bytes (read + write) of one traversal launch, from the one-pass ncu capture of the same
+# command line (profiles/k_query_warp_traffic_icosphere2m_q10m.md); other workloads: not captured
+NCU_TRAFFIC = {"displaced_icosphere_nu316_q10000000": 1.38e9 + 304.88e6}
 
 
 def parse():
@@ -68,7 +71,8 @@ def parse():
     p.add_argument("--block", type=int, default=128)
     p.add_argument("--fp64-steps", type=int, default=2)
     p.add_argument("--cpu-sample", type=int, default=100_000)
-    p.add_argument("--brute", type=int, default=1024)
+    p.add_argument("--brute", type=int, default=1024)      # CPU O1 sample
+    p.add_argument("--brute-gpu", type=int, default=8192)  # GPU FP64 all-triangle sample
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
@@ -344,10 +348,38 @@ def run_ours(args, rank, world, local):
                    "parallelism": f"replicas x{world} (query shards, no collective)"},
         "build_ms": min(build_ms), "tree": {"nodes": info["num_nodes"], "leaves": info["num_leaves"],
                                             "device_bytes": info["device_bytes"]},
-        "step_ms_min": min(step_ms), "wall_s_timed": t_wall,
+        "step_ms_min": min(step_ms), "step_ms_median": statistics.median(step_ms),
+        "wall_s_timed": t_wall,
         "gpu_launches": (1 + (4 * 3 + 1)) * args.steps,  # per step: 4 sort passes x3 + keys + traversal
         "clocks": clocks,
     }
+
+    # ---- the traversal launch alone (roofline denominator) --------------------------------------
+    # the points gathered once in the query's own Morton order and queried with sort_queries=0:
+    # each call is then the status-word memset + one traversal launch, same warps, same results
+    order = eng.query_order(Qd)
+    Qs = Qd[order].contiguous()
+    opts_k = fwn._opts(precision=fwn.PRECISION_MIXED, traversal=trav, block_size=args.block,
+                       sort_queries=0)
+
+    def query_kernel():
+        fwn._check(L.fwn_query_ex(eng.handle, C.byref(opts_k), C.c_void_p(Qs.data_ptr()), n,
+                                  C.c_void_p(w_out.data_ptr()), C.c_void_p(i_out.data_ptr()),
+                                  None, None, sptr))
+
+    for _ in range(max(3, args.warmup)):
+        query_kernel()
+    kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        flush.zero_()
+        kev[k][0].record(stream)
+        query_kernel()
+        kev[k][1].record(stream)
+    torch.cuda.synchronize()
+    kernel_ms = sum(a.elapsed_time(b) for a, b in kev) / args.steps
+    del Qs, order
 
     # ---- roofline from the counters --------------------------------------------------------
     far, tri, nodes = stats["far_evals"], stats["tri_evals"], stats["nodes_tested"]
@@ -356,16 +388,24 @@ def run_ours(args, rank, world, local):
     props = torch.cuda.get_device_properties(dev)
     sm_max = clocks.get("sm_max_mhz") or measured_peaks().get("sm_max_mhz") or 2070.0
     peak_fp32 = props.multi_processor_count * 128 * 2 * sm_max * 1e6 / 1e12
-    achieved = flops / (ms / 1e3) / 1e12
+    achieved = flops / (kernel_ms / 1e3) / 1e12
+    traffic = NCU_TRAFFIC.get(wl.name) if world == 1 else None
+    hbm_peak = measured_peaks().get("hbm_gbs")
     result["roofline"] = {
         "bound": "fp32", "achieved": achieved, "peak": peak_fp32, "unit": "TFLOP/s",
-        "frac": achieved / peak_fp32, "traffic": None,
+        "frac": achieved / peak_fp32, "traffic": traffic,
+        "kernel": "k_query_warp (traversal)", "kernel_ms": kernel_ms,
+        "kernel_share_of_step": kernel_ms / ms,
         "peak_source": f"nominal FP32: {props.multi_processor_count} SMs x 128 lanes x 2 x "
                        f"{sm_max:.0f} MHz (no FP32 figure in MEASURED_PEAKS.json)",
+        "hbm": ({"achieved_gbs": traffic / (kernel_ms / 1e3) / 1e9, "peak_gbs": hbm_peak,
+                 "frac": traffic / (kernel_ms / 1e3) / 1e9 / hbm_peak,
+                 "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)"}
+                if traffic and hbm_peak else None),
         "per_query": {"far_evals": far / n, "tri_evals": tri / n, "nodes_tested": nodes / n,
                       "tri_fp64": stats["tri_evals_fp64"] / n,
                       "flops": flops / n, "l2_bytes": l2_bytes / n},
-        "l2_gbs_algorithmic": l2_bytes / (ms / 1e3) / 1e9,
+        "l2_gbs_algorithmic": l2_bytes / (kernel_ms / 1e3) / 1e9,
     }
 
     # ---- plain FP64 form + accuracy gate ----------------------------------------------------
@@ -449,11 +489,16 @@ def run_ours(args, rank, world, local):
         t0 = time.perf_counter()
         om_cpu, in_cpu = tree.query(sample, beta=wl.beta, nthreads=nthr)
         dt = time.perf_counter() - t0
+        s1 = sample[: max(1, len(sample) // 10)]
+        t0 = time.perf_counter()
+        tree.query(s1, beta=wl.beta, nthreads=1)
+        dt1 = time.perf_counter() - t0
         result["cpu_baseline"] = {
             "value": len(sample) / dt, "unit": "queries/s", "cores": nthr, "kind": "port",
             "sample": f"{len(sample)} queries (half far, half near-surface) of the workload; "
                       f"float order-2 Barill tree restating the reference path; build "
                       f"{build_s:.2f} s single-thread",
+            "single_thread": {"value": len(s1) / dt1, "unit": "queries/s", "sample": len(s1)},
         }
         # is_inside agreement with the restated reference outside the +-1e-3 band
         Qs = torch.from_numpy(sample).to(dev)
@@ -478,6 +523,37 @@ def run_ours(args, rank, world, local):
             "max_dw_far": float(dwb[:half].max()),
             "max_dw_near": float(dwb[half:].max()) if half < len(bs) else None,
             "note": "includes the beta=2 far-field truncation error (same for the FP64 form)"}
+        # FP64 brute force on the GPU: the FP64 form with beta = 1e30 evaluates every triangle
+        # of every leaf exactly in FP64. Checked against O1 on the CPU sample, then run on a
+        # larger stratified sample.
+        if not args.no_fp64 and args.brute_gpu > 0:
+            _, _, xb = eng.query(bq, precision=fwn.PRECISION_FP64, beta=1e30, omega_f64=True)
+            torch.cuda.synchronize()
+            check = float(np.max(np.abs(xb.cpu().numpy() - exact)) / FOUR_PI)
+            gs = cpu_sample(wl, min(args.brute_gpu, len(wl.Q)), seed=12)
+            gq = torch.from_numpy(gs).to(dev)
+            t0 = time.perf_counter()
+            _, _, xg = eng.query(gq, precision=fwn.PRECISION_FP64, beta=1e30, omega_f64=True)
+            torch.cuda.synchronize()
+            bt = time.perf_counter() - t0
+            wmg, _ = eng.query(gq, traversal=trav)
+            _, _, w64g = eng.query(gq, precision=fwn.PRECISION_FP64, omega_f64=True)
+            torch.cuda.synchronize()
+            xg = xg.cpu().numpy()
+            dg = np.abs(wmg.cpu().numpy().astype(np.float64) - xg) / FOUR_PI
+            d64 = np.abs(w64g.cpu().numpy() - xg) / FOUR_PI
+            hg = len(gs) // 2 if wl.near_mask.any() else len(gs)
+            result["vs_brute_force_fp64_gpu"] = {
+                "sample": len(gs), "max_dw": float(dg.max()),
+                "rms_dw": float(np.sqrt(np.mean(dg ** 2))),
+                "max_dw_far": float(dg[:hg].max()),
+                "max_dw_near": float(dg[hg:].max()) if hg < len(gs) else None,
+                "fp64_form_max_dw": float(d64.max()),
+                "fp64_form_rms_dw": float(np.sqrt(np.mean(d64 ** 2))),
+                "brute_force_s": bt,
+                "gpu_brute_vs_cpu_O1_max_dw": check,
+                "note": "GPU FP64 all-triangle sums (FP64 form, beta=1e30); the mixed and FP64 "
+                        "forms carry the same beta=2 truncation error"}
 
     if rank == 0:
         print(json.dumps(result), flush=True)
@@ -550,6 +626,8 @@ def run_forest(args, rank, world, local):
             ts.append(a.elapsed_time(b))
     ms = max_over_ranks(dist, sum(ts) / len(ts), dev)
     build_ms = min(builds)
+    mesh_bits = max(0, (M - 1).bit_length())
+    launches_per_query = 1 + 3 * math.ceil((30 + mesh_bits) / 8) + 1  # keys, sort passes, walk
     result = {
         "metric": f"winding queries/s, {M} meshes in one persistent CUDA-graph launch",
         "value": job_value(n, world, ms / 1e3), "unit": "queries/s", "n_gpus": world,
@@ -561,8 +639,70 @@ def run_forest(args, rank, world, local):
                    "l2": "flushed before every step (256 MB write)", "generation_s": gen_s},
         "build_ms": build_ms, "tree_nodes": forest.info()["num_nodes"],
         "meshes_per_s_build_plus_query": M / ((build_ms + ms) / 1e3),
+        "gpu_launches": launches_per_query * args.steps,
         "clocks": clk.summary(),
     }
+    # ---- end to end: pinned host points in, Omega + inside out, through fwn_forest_query ------
+    if not args.no_e2e:
+        Qh = torch.from_numpy(fo.Q).pin_memory()
+        wh = torch.empty(n, dtype=torch.float32).pin_memory()
+        ih = torch.empty(n, dtype=torch.uint8).pin_memory()
+        Qe = torch.empty_like(Qd)
+        sp = C.c_void_p(stream.cuda_stream)
+
+        def e2e_call():
+            Qe.copy_(Qh, non_blocking=True)
+            fwn._check(L.fwn_forest_query(forest.handle, C.c_void_p(Qe.data_ptr()),
+                                          C.c_void_p(qoff.data_ptr()), C.c_void_p(w.data_ptr()),
+                                          C.c_void_p(ins.data_ptr()), C.byref(opts), sp))
+            wh.copy_(w, non_blocking=True)
+            ih.copy_(ins, non_blocking=True)
+            stream.synchronize()
+        e2e_call()
+        te = []
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            e2e_call()
+            te.append(time.perf_counter() - t0)
+        e2e_s = max_over_ranks(dist, sum(te) / len(te), dev)
+        result["e2e"] = {"value": job_value(n, world, e2e_s), "unit": "queries/s",
+                         "h2d_bytes_per_step": n * 12, "d2h_bytes_per_step": n * 5,
+                         "ms_per_step": e2e_s * 1e3,
+                         "api": "fwn_forest_query (pinned host points copied in, results out)"}
+        del Qe
+    # ---- CPU restatement of the reference path on a few meshes (rank 0, N=1) ---------------
+    if rank == 0 and world == 1 and not args.no_cpu:
+        import oracle
+        nthr = oracle.nthreads_default()
+        rng = np.random.default_rng(21)
+        picks = [0] if args.workload == "voxel" else sorted(rng.choice(M, 4, replace=False).tolist())
+        per = 100_000 if args.workload == "voxel" else 25_000
+        wh_all, ih_all = w.cpu().numpy(), ins.cpu().numpy()
+        nq_cpu, t_cpu, dis, maxdw, build_s = 0, 0.0, 0, 0.0, 0.0
+        for m in picks:
+            Vm = fo.V[fo.voff[m]:fo.voff[m + 1]]
+            Fm = fo.F[fo.foff[m]:fo.foff[m + 1]]
+            q0, q1 = int(fo.qoff[m]), int(fo.qoff[m + 1])
+            idx = np.sort(rng.choice(q1 - q0, min(per, q1 - q0), replace=False)) + q0
+            t0 = time.perf_counter()
+            tree = oracle.RefTree(Vm, Fm, leaf_size=args.leaf)
+            build_s += time.perf_counter() - t0
+            t0 = time.perf_counter()
+            om, inn = tree.query(fo.Q[idx], beta=fo.beta, nthreads=nthr)
+            t_cpu += time.perf_counter() - t0
+            nq_cpu += len(idx)
+            band = np.abs(om / FOUR_PI - 0.5) > 1e-3
+            dis += int(np.sum(ih_all[idx][band] != inn[band]))
+            maxdw = max(maxdw, float(np.max(np.abs(wh_all[idx] - om)) / FOUR_PI))
+        result["cpu_baseline"] = {
+            "value": nq_cpu / t_cpu, "unit": "queries/s", "cores": nthr, "kind": "port",
+            "sample": f"{nq_cpu} queries of meshes {picks} (float order-2 Barill tree restating "
+                      f"the reference path, one tree per mesh; builds {build_s:.2f} s "
+                      f"single-thread, not in the rate)"}
+        result["inside_vs_reference"] = {"sample": nq_cpu, "disagree_outside_band": dis,
+                                         "max_dw_vs_reference_restatement": maxdw}
     if args.workload == "voxel":
         # the same classification through the grid sign pass: centres generated on the device,
         # no point array and no sort (one launch per mesh)

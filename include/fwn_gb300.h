@@ -175,6 +175,14 @@ FWN_API fwn_status fwn_query_ex(fwn_handle h, const fwn_query_opts* opts,
                                 uint8_t* d_inside, double* d_omega_f64,
                                 fwn_query_stats* stats, void* stream);
 
+/* No counterpart in the reference (it answers one point per call). Writes the permutation the
+ * query applies to group nearby points into warps: d_order[k] (uint32, device) is the index of
+ * the k-th point in Morton order of the mesh's frame. A caller that queries the same points
+ * repeatedly can gather them once in this order and pass sort_queries = 0 in fwn_query_opts;
+ * the results are the same. Asynchronous on `stream`. */
+FWN_API fwn_status fwn_query_order(fwn_handle h, const float* d_points, int64_t n,
+                                   uint32_t* d_order, void* stream);
+
 /* Queries on HOST buffers (pinned or pageable): copies in, runs, copies out. Synchronous. */
 FWN_API fwn_status fwn_query_host(fwn_handle h, const float* points, int64_t n,
                                   float* omega, uint8_t* inside);

@@ -85,7 +85,7 @@ EXPORTS = ["fwn_config_default", "fwn_last_error", "fwn_version", "fwn_build", "
            "fwn_destroy", "fwn_get_info", "fwn_query", "fwn_query_ex", "fwn_query_host",
            "fwn_export_tree", "fwn_export_moments", "fwn_forest_build",
            "fwn_forest_build_device", "fwn_forest_query", "fwn_query_noalloc", "fwn_autotune",
-           "fwn_query_grid", "fwn_orientation_criterion"]
+           "fwn_query_grid", "fwn_orientation_criterion", "fwn_query_order"]
 
 
 def library():
@@ -113,6 +113,7 @@ def library():
     L.fwn_query_ex.argtypes = [P, C.POINTER(fwn_query_opts), P, i64, P, P, P,
                                C.POINTER(fwn_query_stats), P]
     L.fwn_query_host.argtypes = [P, P, i64, P, P]
+    L.fwn_query_order.argtypes = [P, P, i64, P, P]
     L.fwn_export_tree.argtypes = [P, P, P, P, P, P, P]
     L.fwn_export_moments.argtypes = [P, P]
     L.fwn_forest_build.argtypes = [P, P, P, P, i64, C.POINTER(fwn_config), C.POINTER(P)]
@@ -294,6 +295,17 @@ class FastWindingNumber:
                          stream=stream)
         torch.cuda.synchronize()
         return tuple(r.cpu().numpy() if hasattr(r, "cpu") else r for r in res)
+
+    def query_order(self, points, stream=None):
+        """The permutation the query applies to group nearby points into warps (int64 CUDA
+        tensor): points[order] queried with sort_queries=False gives the same results."""
+        import torch
+        Q = points.detach().to(torch.float32).contiguous().reshape(-1, 3)
+        n = Q.shape[0]
+        o = torch.empty(n, dtype=torch.int32, device=Q.device)  # uint32 bits, n < 2^31
+        _check(library().fwn_query_order(self._h, C.c_void_p(Q.data_ptr()), n,
+                                         C.c_void_p(o.data_ptr()), _stream_ptr(stream)))
+        return o.long()
 
     def solid_angle(self, points):
         """Solid angle(s) in steradians (FastWindingNumber.cpp:69-76). A single point (3,)

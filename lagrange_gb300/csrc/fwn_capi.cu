@@ -216,6 +216,17 @@ FWN_API fwn_status fwn_query_ex(fwn_handle h, const fwn_query_opts* opts, const 
     });
 }
 
+FWN_API fwn_status fwn_query_order(fwn_handle h, const float* d_points, int64_t n,
+                                   uint32_t* d_order, void* stream) {
+    return guarded([&] {
+        Engine* e = engine_of(h);
+        check_points(n, d_points);
+        if (e->nmeshes != 1) throw Error(FWN_INVALID_ARG, "forest handle: build one engine per mesh");
+        if (n > 0 && !d_order) throw Error(FWN_INVALID_ARG, "order pointer is null");
+        query_order(*e, 0, d_points, n, d_order, static_cast<cudaStream_t>(stream));
+    });
+}
+
 FWN_API fwn_status fwn_query_host(fwn_handle h, const float* points, int64_t n, float* omega,
                                   uint8_t* inside) {
     return guarded([&] {

@@ -156,8 +156,7 @@ bool radix_sort_u32(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b, uint32
 bool radix_sort_u64(uint64_t* keys_a, uint32_t* vals_a, uint64_t* keys_b, uint32_t* vals_b,
                     int64_t n, int key_bits, void* temp, cudaStream_t stream);
 
-// Exclusive scan of n int32 values in place (scan.cu); returns nothing, total is written to
-// data[n] if the buffer has n+1 entries and `write_total` is true.
+// Exclusive scan of n int32 values in place (radix_sort.cu).
 size_t exclusive_scan_temp_bytes(int64_t n);
 void exclusive_scan_i32(int* data, int64_t n, void* temp, cudaStream_t stream);
 
@@ -212,6 +211,11 @@ void query_forest(const Engine& e, const QueryArgs& a, const float* d_points,
                   cudaStream_t stream);
 
 QueryArgs resolve_query_args(const Engine& e, const fwn_query_opts* opts);
+
+// The permutation query_mesh applies when sort_queries is set (Morton order of the points in
+// mesh `mesh`'s frame): d_order[k] = index of the k-th point. Async.
+void query_order(const Engine& e, int mesh, const float* d_points, int64_t n, uint32_t* d_order,
+                 cudaStream_t stream);
 
 // Query with caller-provided device scratch (no allocation): `scratch` holds the status word and
 // the Morton-sort buffers, at least query_prealloc_bytes(n) bytes, 256-byte aligned. Async.

@@ -717,6 +717,22 @@ QueryArgs resolve_query_args(const Engine& e, const fwn_query_opts* o) {
     return a;
 }
 
+void query_order(const Engine& e, int mesh, const float* d_points, int64_t n, uint32_t* d_order,
+                 cudaStream_t st) {
+    if (n <= 0) return;
+    const MeshInfo& mi = e.meshes_h[mesh];
+    Scratch buf(3 * (size_t)n * sizeof(uint32_t) + radix_sort_temp_bytes(n, 4) + 256, st);
+    uint32_t* ka = buf.as<uint32_t>();
+    uint32_t* kb = ka + n;
+    uint32_t* vb = kb + n;
+    void* tmp = vb + n;
+    k_query_keys<<<grid_for(n, 256), 256, 0, st>>>(d_points, n, mi, ka, d_order);
+    FWN_CUDA_CHECK(cudaGetLastError());
+    if (n > 1 && radix_sort_u32(ka, d_order, kb, vb, n, 30, tmp, st))
+        FWN_CUDA_CHECK(cudaMemcpyAsync(d_order, vb, (size_t)n * sizeof(uint32_t),
+                                       cudaMemcpyDeviceToDevice, st));
+}
+
 void query_mesh(const Engine& e, int mesh, const QueryArgs& a, const float* d_points, int64_t n,
                 float* d_omega, uint8_t* d_inside, double* d_omega64, fwn_query_stats* stats,
                 cudaStream_t st, bool check) {

@@ -10,6 +10,7 @@ Tolerances (w = Omega / 4 pi):
     mixed vs O1 |dw| <= 1e-5.
   * is_inside agrees with the FP64 oracle on every point with |w - 0.5| > 1e-3.
 """
+import ctypes as C
 import math
 import threading
 from pathlib import Path
@@ -175,6 +176,33 @@ def test_invalid_meshes(torch_cuda):
     e32 = fwn.FastWindingNumber(V, F)
     with pytest.raises(fwn.WindingError, match="FP64 records"):
         e32.query(np.zeros((1, 3), np.float32), precision=fwn.PRECISION_FP64)
+
+
+def test_query_order_presorted(torch_cuda):
+    """fwn_query_order returns the query's own permutation: gathering the points in that order
+    and querying with sort_queries=0 reproduces the sorted query bit for bit (both forms)."""
+    torch = torch_cuda
+    wl = W.displaced_icosphere_workload(nu=24, n_queries=50_000)
+    eng = _engine(wl.V, wl.F)
+    Q = torch.from_numpy(wl.Q).cuda()
+    order = eng.query_order(Q)
+    torch.cuda.synchronize()
+    assert torch.equal(torch.sort(order).values, torch.arange(len(Q), device=order.device))
+    Qs = Q[order]
+    for prec in (fwn.PRECISION_MIXED, fwn.PRECISION_FP64):
+        w, ins = eng.query(Q, precision=prec)
+        ws, inss = eng.query(Qs, precision=prec, sort_queries=False)
+        torch.cuda.synchronize()
+        assert torch.equal(ws, w[order]) and torch.equal(inss, ins[order])
+    # empty batch, forest handle refused
+    assert eng.query_order(Q[:0]).numel() == 0
+    fo = W.batched_forest_workload(n_meshes=2, seed=1, f_lo=100, f_hi=200, q_lo=5, q_hi=10)
+    forest = fwn.Forest(fo.V, fo.voff, fo.F, fo.foff)
+    buf = torch.empty(4, dtype=torch.int32, device=Q.device)
+    with pytest.raises(fwn.WindingError, match="forest") as e:
+        fwn._check(fwn.library().fwn_query_order(forest._h, C.c_void_p(Q.data_ptr()), 4,
+                                                 C.c_void_p(buf.data_ptr()), None))
+    assert e.value.status == 1
 
 
 def test_concurrent_queries_one_handle(torch_cuda):
