@@ -1,8 +1,10 @@
 // C ABI of the engine (declared in include/fwn_gb300.h). No exception crosses this boundary:
 // every entry point catches, stores the message in a thread-local slot and returns a status.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -14,6 +16,47 @@ namespace fwn {
 static thread_local std::string g_last_error;
 
 void set_last_error(const std::string& m) { g_last_error = m; }
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_pool_mutex;
+cudaMemPool_t g_pools[kMaxDevices] = {};  // created on first use, kept for the process lifetime
+
+cudaMemPool_t scratch_pool(int dev) {
+    if (dev < 0 || dev >= kMaxDevices) throw Error(FWN_INTERNAL, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_pool_mutex);
+    if (!g_pools[dev]) {
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool = nullptr;
+        FWN_CUDA_CHECK(cudaMemPoolCreate(&pool, &props));
+        uint64_t keep = kScratchRetainBytes;
+        const cudaError_t err = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        if (err != cudaSuccess) {
+            cudaMemPoolDestroy(pool);
+            FWN_CUDA_CHECK(err);
+        }
+        g_pools[dev] = pool;
+    }
+    return g_pools[dev];
+}
+}  // namespace
+
+void* scratch_alloc(size_t bytes, cudaStream_t st) {
+    void* p = nullptr;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    FWN_CUDA_CHECK(cudaStreamIsCapturing(st, &cs));
+    if (cs != cudaStreamCaptureStatusNone) {
+        FWN_CUDA_CHECK(cudaMallocAsync(&p, bytes, st));
+        return p;
+    }
+    int dev = 0;
+    FWN_CUDA_CHECK(cudaGetDevice(&dev));
+    FWN_CUDA_CHECK(cudaMallocFromPoolAsync(&p, bytes, scratch_pool(dev), st));
+    return p;
+}
 
 Engine::~Engine() {
     if (nodes32) cudaFree(nodes32);

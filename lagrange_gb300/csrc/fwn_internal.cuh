@@ -128,14 +128,22 @@ enum : unsigned {
 };
 
 // ---------------------------------------------------------------------------------------------
-// Stream-ordered scratch buffer (cudaMallocAsync / cudaFreeAsync)
+// Stream-ordered scratch buffer
 // ---------------------------------------------------------------------------------------------
+// Scratch comes from a memory pool per device owned by the library, which keeps up to
+// kScratchRetainBytes of freed memory across synchronisations. (The device's default pool
+// returns freed memory to the driver at every synchronisation, so a host-synchronous call would
+// map all of its scratch again on every call.) During stream capture the allocation goes to the
+// default pool instead, so that it becomes a graph memory node. Freed with cudaFreeAsync.
+constexpr uint64_t kScratchRetainBytes = uint64_t(8) << 30;
+void* scratch_alloc(size_t bytes, cudaStream_t stream);
+
 struct Scratch {
     void* p = nullptr;
     cudaStream_t s = 0;
     Scratch() = default;
     Scratch(size_t bytes, cudaStream_t st) : s(st) {
-        if (bytes) FWN_CUDA_CHECK(cudaMallocAsync(&p, bytes, st));
+        if (bytes) p = scratch_alloc(bytes, st);
     }
     Scratch(const Scratch&) = delete;
     Scratch& operator=(const Scratch&) = delete;

@@ -148,6 +148,13 @@ __device__ __noinline__ float tri_omega_near64(float v0x, float v0y, float v0z, 
     return 2.0f * atan2f((float)(det * sc), (float)(D * sc));
 }
 
+// sqrt(x) for x >= 0 as x * rsqrt(x): two instructions instead of the correctly rounded square
+// root, a few ulp of error (well inside the mixed form's budget; the ill-conditioned triangles
+// where it could matter are re-evaluated in FP64). Exactly 0 for x = 0.
+__device__ __forceinline__ float sqrt_fast(float x) {
+    return x * rsqrtf(fmaxf(x, 1e-37f));
+}
+
 template <bool STATS>
 __device__ __forceinline__ float tri_omega_mixed(float v0x, float v0y, float v0z, float v1x,
                                                  float v1y, float v1z, float v2x, float v2y,
@@ -158,9 +165,9 @@ __device__ __forceinline__ float tri_omega_mixed(float v0x, float v0y, float v0z
     const float bx = v1x - qx, by = v1y - qy, bz = v1z - qz;
     const float cx = v2x - qx, cy = v2y - qy, cz = v2z - qz;
     const float det = ax * (by * cz - bz * cy) + ay * (bz * cx - bx * cz) + az * (bx * cy - by * cx);
-    const float la = sqrtf(ax * ax + ay * ay + az * az);
-    const float lb = sqrtf(bx * bx + by * by + bz * bz);
-    const float lc = sqrtf(cx * cx + cy * cy + cz * cz);
+    const float la = sqrt_fast(ax * ax + ay * ay + az * az);
+    const float lb = sqrt_fast(bx * bx + by * by + bz * bz);
+    const float lc = sqrt_fast(cx * cx + cy * cy + cz * cz);
     const float D = la * lb * lc + (ax * bx + ay * by + az * bz) * lc +
                     (bx * cx + by * cy + bz * cz) * la + (cx * ax + cy * ay + cz * az) * lb;
     // FP64 near field: the triangle is within tau of q (lower bound of the distance:
@@ -171,7 +178,7 @@ __device__ __forceinline__ float tri_omega_mixed(float v0x, float v0y, float v0z
     const float h = fabsf(det) * inv_nlen;
     if (h < tau) {
         const float sx = ax + bx + cx, sy = ay + by + cy, sz = az + bz + cz;
-        const float dc = sqrtf(sx * sx + sy * sy + sz * sz) * (1.0f / 3.0f);
+        const float dc = sqrt_fast(sx * sx + sy * sy + sz * sz) * (1.0f / 3.0f);
         if (dc - rt < tau) {
             const float prod = la * lb * lc;
             const bool ill = prod > cond * sqrtf(fmaf(det, det, D * D)) ||

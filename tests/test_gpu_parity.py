@@ -205,6 +205,32 @@ def test_query_order_presorted(torch_cuda):
     assert e.value.status == 1
 
 
+def test_host_query_large_batch(torch_cuda):
+    """fwn_query_host on a 4.5M-point batch (pinned and pageable host buffers, one output or
+    both) equals the device query bit for bit."""
+    torch = torch_cuda
+    V, F = W.icosphere(12)
+    eng = _engine(V.astype(np.float32), F)
+    Q = np.random.default_rng(8).uniform(-1.3, 1.3, (4_500_000, 3)).astype(np.float32)
+    wd, idv = eng.query(torch.from_numpy(Q).cuda())
+    torch.cuda.synchronize()
+    wd, idv = wd.cpu().numpy(), idv.cpu().numpy()
+    wh, ih = eng.query(Q)  # pageable numpy buffers
+    np.testing.assert_array_equal(wh, wd)
+    np.testing.assert_array_equal(ih, idv)
+    Qp = torch.from_numpy(Q).pin_memory()
+    wp = torch.empty(len(Q), dtype=torch.float32).pin_memory()
+    ip = torch.empty(len(Q), dtype=torch.uint8).pin_memory()
+    fwn._check(fwn.library().fwn_query_host(eng.handle, C.c_void_p(Qp.data_ptr()), len(Q),
+                                            C.c_void_p(wp.data_ptr()), C.c_void_p(ip.data_ptr())))
+    np.testing.assert_array_equal(wp.numpy(), wd)
+    np.testing.assert_array_equal(ip.numpy(), idv)
+    # one output only
+    fwn._check(fwn.library().fwn_query_host(eng.handle, C.c_void_p(Qp.data_ptr()), len(Q), None,
+                                            C.c_void_p(ip.data_ptr())))
+    np.testing.assert_array_equal(ip.numpy(), idv)
+
+
 def test_concurrent_queries_one_handle(torch_cuda):
     wl = W.displaced_icosphere_workload(nu=20, n_queries=5000)
     eng = _engine(wl.V, wl.F)
