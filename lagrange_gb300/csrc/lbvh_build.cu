@@ -327,6 +327,11 @@ __device__ __forceinline__ void load_tri_d(const float* __restrict__ V, const in
 constexpr double kThird = 1.0 / 3.0;
 constexpr double kTwelfth = 1.0 / 12.0;
 
+// Fused multiply-add, correctly rounded. This file is compiled with -fmad=false so that no
+// product is contracted implicitly; every fused operation of the refit is written out, at the
+// same places as in the oracle's restatement (C fma()), which keeps the two bit-identical.
+__device__ __forceinline__ double fmad(double a, double b, double c) { return __fma_rn(a, b, c); }
+
 __device__ void leaf_moments(const float* __restrict__ V, const int32_t* __restrict__ F,
                              const int64_t* __restrict__ voff, const uint64_t* __restrict__ keys,
                              const uint32_t* __restrict__ tri_of_slot, int f, int l,
@@ -348,15 +353,15 @@ __device__ void leaf_moments(const float* __restrict__ V, const int32_t* __restr
             e1[a] = v[1][a] - v[0][a];
             e2[a] = v[2][a] - v[0][a];
         }
-        nn[0] = 0.5 * (e1[1] * e2[2] - e1[2] * e2[1]);
-        nn[1] = 0.5 * (e1[2] * e2[0] - e1[0] * e2[2]);
-        nn[2] = 0.5 * (e1[0] * e2[1] - e1[1] * e2[0]);
-        const double a_t = sqrt(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
+        nn[0] = 0.5 * fmad(e1[1], e2[2], -(e1[2] * e2[1]));
+        nn[1] = 0.5 * fmad(e1[2], e2[0], -(e1[0] * e2[2]));
+        nn[2] = 0.5 * fmad(e1[0], e2[1], -(e1[1] * e2[0]));
+        const double a_t = sqrt(fmad(nn[0], nn[0], fmad(nn[1], nn[1], nn[2] * nn[2])));
         for (int a = 0; a < 3; ++a) c[a] = ((v[0][a] + v[1][a]) + v[2][a]) * kThird;
         if (s == f)
             for (int a = 0; a < 3; ++a) c0[a] = c[a];
         for (int a = 0; a < 3; ++a) {
-            S[a] = S[a] + a_t * c[a];
+            S[a] = fmad(a_t, c[a], S[a]);
             Cs[a] = Cs[a] + c[a];
             d[a] = c[a] - c0[a];
         }
@@ -366,14 +371,14 @@ __device__ void leaf_moments(const float* __restrict__ V, const int32_t* __restr
 #pragma unroll
         for (int q = 0; q < 6; ++q) {
             const int j = SJ[q], k = SK[q];
-            const double cov = ((w[0][j] * w[0][k] + w[1][j] * w[1][k]) + w[2][j] * w[2][k]) * kTwelfth;
-            Q[q] = d[j] * d[k] + cov;
+            const double cov = fmad(w[0][j], w[0][k], fmad(w[1][j], w[1][k], w[2][j] * w[2][k])) * kTwelfth;
+            Q[q] = fmad(d[j], d[k], cov);
         }
         for (int i = 0; i < 3; ++i) {
             N[i] = N[i] + nn[i];
-            for (int j = 0; j < 3; ++j) M1[3 * i + j] = M1[3 * i + j] + nn[i] * d[j];
+            for (int j = 0; j < 3; ++j) M1[3 * i + j] = fmad(nn[i], d[j], M1[3 * i + j]);
 #pragma unroll
-            for (int q = 0; q < 6; ++q) M2[6 * i + q] = M2[6 * i + q] + nn[i] * Q[q];
+            for (int q = 0; q < 6; ++q) M2[6 * i + q] = fmad(nn[i], Q[q], M2[6 * i + q]);
         }
         for (int j = 0; j < 3; ++j)
             for (int a = 0; a < 3; ++a) {
@@ -393,10 +398,10 @@ __device__ void leaf_moments(const float* __restrict__ V, const int32_t* __restr
 #pragma unroll
         for (int q = 0; q < 6; ++q) {
             const int j = SJ[q], k = SK[q];
-            R.M2[6 * i + q] = ((M2[6 * i + q] + M1[3 * i + j] * e[k]) + M1[3 * i + k] * e[j]) +
-                              N[i] * (e[j] * e[k]);
+            R.M2[6 * i + q] =
+                fmad(N[i], e[j] * e[k], fmad(M1[3 * i + k], e[j], fmad(M1[3 * i + j], e[k], M2[6 * i + q])));
         }
-        for (int j = 0; j < 3; ++j) R.M1[3 * i + j] = M1[3 * i + j] + N[i] * e[j];
+        for (int j = 0; j < 3; ++j) R.M1[3 * i + j] = fmad(N[i], e[j], M1[3 * i + j]);
     }
     double r2 = 0.0;
     for (int s = f; s <= l; ++s) {
@@ -406,7 +411,7 @@ __device__ void leaf_moments(const float* __restrict__ V, const int32_t* __restr
         load_tri_d(V, F, voff[m], t, v);
         for (int j = 0; j < 3; ++j) {
             const double dx = v[j][0] - P[0], dy = v[j][1] - P[1], dz = v[j][2] - P[2];
-            r2 = fmax(r2, (dx * dx + dy * dy) + dz * dz);
+            r2 = fmax(r2, fmad(dx, dx, fmad(dy, dy, dz * dz)));
         }
     }
     for (int a = 0; a < 3; ++a) {
@@ -440,7 +445,7 @@ __device__ void combine_moments(const StageRec* __restrict__ a_, const StageRec*
     const double A = Aa + Ab;
     double P[3], ea[3], eb[3];
     for (int i = 0; i < 3; ++i) {
-        const double pe = A > 0.0 ? (Aa * Pa[i] + Ab * Pb[i]) / A : (Pa[i] + Pb[i]) * 0.5;
+        const double pe = A > 0.0 ? fmad(Aa, Pa[i], Ab * Pb[i]) / A : (Pa[i] + Pb[i]) * 0.5;
         P[i] = (double)(float)pe;
         ea[i] = Pa[i] - P[i];
         eb[i] = Pb[i] - P[i];
@@ -449,7 +454,7 @@ __device__ void combine_moments(const StageRec* __restrict__ a_, const StageRec*
         R.P[i] = P[i];
         R.N[i] = Na[i] + Nb[i];
         for (int j = 0; j < 3; ++j)
-            R.M1[3 * i + j] = (M1a[3 * i + j] + Na[i] * ea[j]) + (M1b[3 * i + j] + Nb[i] * eb[j]);
+            R.M1[3 * i + j] = fmad(Na[i], ea[j], M1a[3 * i + j]) + fmad(Nb[i], eb[j], M1b[3 * i + j]);
     }
     const int SJ[6] = {0, 1, 2, 0, 0, 1};
     const int SK[6] = {0, 1, 2, 1, 2, 2};
@@ -457,10 +462,10 @@ __device__ void combine_moments(const StageRec* __restrict__ a_, const StageRec*
 #pragma unroll
         for (int q = 0; q < 6; ++q) {
             const int j = SJ[q], k = SK[q];
-            const double ta = ((ldcg_d(&a_->M2[6 * i + q]) + M1a[3 * i + j] * ea[k]) +
-                               M1a[3 * i + k] * ea[j]) + Na[i] * (ea[j] * ea[k]);
-            const double tb = ((ldcg_d(&b_->M2[6 * i + q]) + M1b[3 * i + j] * eb[k]) +
-                               M1b[3 * i + k] * eb[j]) + Nb[i] * (eb[j] * eb[k]);
+            const double ta = fmad(Na[i], ea[j] * ea[k],
+                                   fmad(M1a[3 * i + k], ea[j], fmad(M1a[3 * i + j], ea[k], ldcg_d(&a_->M2[6 * i + q]))));
+            const double tb = fmad(Nb[i], eb[j] * eb[k],
+                                   fmad(M1b[3 * i + k], eb[j], fmad(M1b[3 * i + j], eb[k], ldcg_d(&b_->M2[6 * i + q]))));
             R.M2[6 * i + q] = ta + tb;
         }
     double lo[3], hi[3];
@@ -475,12 +480,12 @@ __device__ void combine_moments(const StageRec* __restrict__ a_, const StageRec*
     R.area = A;
     // radius: min of (a) the sphere around both child spheres, (b) farthest bbox corner
     const double ra = ldcg_d(&a_->r), rb = ldcg_d(&b_->r);
-    const double da = sqrt((ea[0] * ea[0] + ea[1] * ea[1]) + ea[2] * ea[2]) + ra;
-    const double db = sqrt((eb[0] * eb[0] + eb[1] * eb[1]) + eb[2] * eb[2]) + rb;
+    const double da = sqrt(fmad(ea[0], ea[0], fmad(ea[1], ea[1], ea[2] * ea[2]))) + ra;
+    const double db = sqrt(fmad(eb[0], eb[0], fmad(eb[1], eb[1], eb[2] * eb[2]))) + rb;
     double c2 = 0.0;
     for (int a = 0; a < 3; ++a) {
         const double x = fmax(fabs(P[a] - lo[a]), fabs(P[a] - hi[a]));
-        c2 = c2 + x * x;
+        c2 = fmad(x, x, c2);
     }
     R.r = round_up_float(fmin(fmax(da, db), sqrt(c2)));
 }

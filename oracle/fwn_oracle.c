@@ -476,6 +476,8 @@ static void lb_tri_d(const lb_tree* T, int64_t s, double v[3][3]) {
  * centroid and the moments about the first triangle's centroid c0; the moments are then moved to
  * P = float(area-weighted centroid) with the parent recentring formulas (e = c0 - P); a second,
  * vertex-only pass gives r = max |v - P| (rounded up to a float). */
+/* The refit's fused multiply-adds are written out (C fma(), correctly rounded) at the same places
+ * as in the device refit, which is compiled without implicit contraction. */
 static void lb_leaf(const lb_tree* T, int64_t f, int64_t l, lb_stage* R) {
     static const double kThird = 1.0 / 3.0, kTwelfth = 1.0 / 12.0;
     static const int SJ[6] = {0, 1, 2, 0, 0, 1}, SK[6] = {0, 1, 2, 1, 2, 2};
@@ -489,15 +491,15 @@ static void lb_leaf(const lb_tree* T, int64_t f, int64_t l, lb_stage* R) {
             e1[a] = v[1][a] - v[0][a];
             e2[a] = v[2][a] - v[0][a];
         }
-        nn[0] = 0.5 * (e1[1] * e2[2] - e1[2] * e2[1]);
-        nn[1] = 0.5 * (e1[2] * e2[0] - e1[0] * e2[2]);
-        nn[2] = 0.5 * (e1[0] * e2[1] - e1[1] * e2[0]);
-        const double at = sqrt(nn[0] * nn[0] + nn[1] * nn[1] + nn[2] * nn[2]);
+        nn[0] = 0.5 * fma(e1[1], e2[2], -(e1[2] * e2[1]));
+        nn[1] = 0.5 * fma(e1[2], e2[0], -(e1[0] * e2[2]));
+        nn[2] = 0.5 * fma(e1[0], e2[1], -(e1[1] * e2[0]));
+        const double at = sqrt(fma(nn[0], nn[0], fma(nn[1], nn[1], nn[2] * nn[2])));
         for (int a = 0; a < 3; ++a) c[a] = ((v[0][a] + v[1][a]) + v[2][a]) * kThird;
         if (s == f)
             for (int a = 0; a < 3; ++a) c0[a] = c[a];
         for (int a = 0; a < 3; ++a) {
-            S[a] = S[a] + at * c[a];
+            S[a] = fma(at, c[a], S[a]);
             Cs[a] = Cs[a] + c[a];
             d[a] = c[a] - c0[a];
         }
@@ -506,13 +508,13 @@ static void lb_leaf(const lb_tree* T, int64_t f, int64_t l, lb_stage* R) {
             for (int a = 0; a < 3; ++a) w[j][a] = v[j][a] - c[a];
         for (int q = 0; q < 6; ++q) {
             const int j = SJ[q], k = SK[q];
-            const double cov = ((w[0][j] * w[0][k] + w[1][j] * w[1][k]) + w[2][j] * w[2][k]) * kTwelfth;
-            Q[q] = d[j] * d[k] + cov;
+            const double cov = fma(w[0][j], w[0][k], fma(w[1][j], w[1][k], w[2][j] * w[2][k])) * kTwelfth;
+            Q[q] = fma(d[j], d[k], cov);
         }
         for (int i = 0; i < 3; ++i) {
             N[i] = N[i] + nn[i];
-            for (int j = 0; j < 3; ++j) M1[3 * i + j] = M1[3 * i + j] + nn[i] * d[j];
-            for (int q = 0; q < 6; ++q) M2[6 * i + q] = M2[6 * i + q] + nn[i] * Q[q];
+            for (int j = 0; j < 3; ++j) M1[3 * i + j] = fma(nn[i], d[j], M1[3 * i + j]);
+            for (int q = 0; q < 6; ++q) M2[6 * i + q] = fma(nn[i], Q[q], M2[6 * i + q]);
         }
         for (int j = 0; j < 3; ++j)
             for (int a = 0; a < 3; ++a) {
@@ -531,10 +533,10 @@ static void lb_leaf(const lb_tree* T, int64_t f, int64_t l, lb_stage* R) {
     for (int i = 0; i < 3; ++i) {
         for (int q = 0; q < 6; ++q) {
             const int j = SJ[q], k = SK[q];
-            R->M2[6 * i + q] = ((M2[6 * i + q] + M1[3 * i + j] * e[k]) + M1[3 * i + k] * e[j]) +
-                               N[i] * (e[j] * e[k]);
+            R->M2[6 * i + q] =
+                fma(N[i], e[j] * e[k], fma(M1[3 * i + k], e[j], fma(M1[3 * i + j], e[k], M2[6 * i + q])));
         }
-        for (int j = 0; j < 3; ++j) R->M1[3 * i + j] = M1[3 * i + j] + N[i] * e[j];
+        for (int j = 0; j < 3; ++j) R->M1[3 * i + j] = fma(N[i], e[j], M1[3 * i + j]);
     }
     double r2 = 0.0;
     for (int64_t s = f; s <= l; ++s) {
@@ -542,7 +544,7 @@ static void lb_leaf(const lb_tree* T, int64_t f, int64_t l, lb_stage* R) {
         lb_tri_d(T, s, v);
         for (int j = 0; j < 3; ++j) {
             const double dx = v[j][0] - P[0], dy = v[j][1] - P[1], dz = v[j][2] - P[2];
-            r2 = fmax(r2, (dx * dx + dy * dy) + dz * dz);
+            r2 = fmax(r2, fma(dx, dx, fma(dy, dy, dz * dz)));
         }
     }
     for (int a = 0; a < 3; ++a) {
@@ -559,7 +561,7 @@ static void lb_combine(const lb_stage* a, const lb_stage* b, lb_stage* R) {
     const double A = a->area + b->area;
     double P[3], ea[3], eb[3];
     for (int i = 0; i < 3; ++i) {
-        const double pe = A > 0.0 ? (a->area * a->P[i] + b->area * b->P[i]) / A : (a->P[i] + b->P[i]) * 0.5;
+        const double pe = A > 0.0 ? fma(a->area, a->P[i], b->area * b->P[i]) / A : (a->P[i] + b->P[i]) * 0.5;
         P[i] = (double)(float)pe;
         ea[i] = a->P[i] - P[i];
         eb[i] = b->P[i] - P[i];
@@ -569,16 +571,16 @@ static void lb_combine(const lb_stage* a, const lb_stage* b, lb_stage* R) {
         o.P[i] = P[i];
         o.N[i] = a->N[i] + b->N[i];
         for (int j = 0; j < 3; ++j)
-            o.M1[3 * i + j] = (a->M1[3 * i + j] + a->N[i] * ea[j]) + (b->M1[3 * i + j] + b->N[i] * eb[j]);
+            o.M1[3 * i + j] = fma(a->N[i], ea[j], a->M1[3 * i + j]) + fma(b->N[i], eb[j], b->M1[3 * i + j]);
     }
     static const int SJ[6] = {0, 1, 2, 0, 0, 1}, SK[6] = {0, 1, 2, 1, 2, 2};
     for (int i = 0; i < 3; ++i)
         for (int q = 0; q < 6; ++q) {
             const int j = SJ[q], k = SK[q];
-            const double ta = ((a->M2[6 * i + q] + a->M1[3 * i + j] * ea[k]) + a->M1[3 * i + k] * ea[j]) +
-                              a->N[i] * (ea[j] * ea[k]);
-            const double tb = ((b->M2[6 * i + q] + b->M1[3 * i + j] * eb[k]) + b->M1[3 * i + k] * eb[j]) +
-                              b->N[i] * (eb[j] * eb[k]);
+            const double ta = fma(a->N[i], ea[j] * ea[k],
+                                  fma(a->M1[3 * i + k], ea[j], fma(a->M1[3 * i + j], ea[k], a->M2[6 * i + q])));
+            const double tb = fma(b->N[i], eb[j] * eb[k],
+                                  fma(b->M1[3 * i + k], eb[j], fma(b->M1[3 * i + j], eb[k], b->M2[6 * i + q])));
             o.M2[6 * i + q] = ta + tb;
         }
     double lo[3], hi[3];
@@ -589,12 +591,12 @@ static void lb_combine(const lb_stage* a, const lb_stage* b, lb_stage* R) {
         hi[a2] = o.hi[a2];
     }
     o.area = A;
-    const double da = sqrt((ea[0] * ea[0] + ea[1] * ea[1]) + ea[2] * ea[2]) + a->r;
-    const double db = sqrt((eb[0] * eb[0] + eb[1] * eb[1]) + eb[2] * eb[2]) + b->r;
+    const double da = sqrt(fma(ea[0], ea[0], fma(ea[1], ea[1], ea[2] * ea[2]))) + a->r;
+    const double db = sqrt(fma(eb[0], eb[0], fma(eb[1], eb[1], eb[2] * eb[2]))) + b->r;
     double c2 = 0.0;
     for (int a2 = 0; a2 < 3; ++a2) {
         const double x = fmax(fabs(P[a2] - lo[a2]), fabs(P[a2] - hi[a2]));
-        c2 = c2 + x * x;
+        c2 = fma(x, x, c2);
     }
     o.r = round_up_float(fmin(fmax(da, db), sqrt(c2)));
     *R = o;
