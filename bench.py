@@ -51,6 +51,7 @@ BYTES_NODE_TEST = 32   # sector 0 of a NodeF32 record
 BYTES_NODE_FAR = 96    # sectors 1-3 (far-field coefficients)
 BYTES_TRI = 48
 BYTES_QUERY_IO = 12 + 4 + 1 + 4  # point in, Omega + inside out, sort index
+CPU_LEAF = 8  # leaf size of the CPU restatement of the reference tree, in every CPU timing
 # DRAM bytes (read + write) of one traversal launch, from the one-pass ncu capture of the same
 # command line (profiles/k_query_warp_traffic_icosphere2m_q10m.md); other workloads: not captured
 NCU_TRAFFIC = {"displaced_icosphere_nu316_q10000000": 1.38e9 + 304.88e6}
@@ -66,7 +67,7 @@ def parse():
                    choices=["icosphere", "soup", "uvsphere", "forest", "voxel"])
     p.add_argument("--nu", type=int, default=None)
     p.add_argument("--queries", type=int, default=None)
-    p.add_argument("--leaf", type=int, default=8)
+    p.add_argument("--leaf", type=int, default=0)  # 0: the autotuner picks (untimed)
     p.add_argument("--traversal", default="warp", choices=["thread", "warp"])
     p.add_argument("--block", type=int, default=128)
     p.add_argument("--fp64-steps", type=int, default=2)
@@ -208,6 +209,24 @@ def make_workload(args):
     return W.displaced_icosphere_workload(nu=args.nu or 316, n_queries=args.queries or 10_000_000)
 
 
+def autotune_choice(fwn, Vd, Fd, Qd, sample: int = 2_000_000, seed: int = 5):
+    """fwn_autotune on a seeded sample of the workload's own queries: returns (leaf, traversal,
+    block, tuning, summary). Untimed; the bench then measures the chosen configuration."""
+    import torch
+    n = Qd.shape[0]
+    if n > sample:
+        g = torch.Generator(device="cpu").manual_seed(seed)
+        idx = torch.randperm(n, generator=g)[:sample].to(Qd.device)
+        Qs = Qd[idx].contiguous()
+    else:
+        Qs = Qd
+    r = fwn.autotune(Vd, Fd, Qs)
+    summary = {"leaf_size": r["leaf_size"], "traversal": r["traversal"],
+               "block_size": r["block_size"], "tuning": r["tuning"],
+               "sample_ms": r["ms"], "candidates": r["candidates"], "sample": int(Qs.shape[0])}
+    return r["leaf_size"], r["traversal"], r["block_size"], r["tuning"], summary
+
+
 def cpu_sample(wl, size: int, seed: int = 7):
     """A bounded sample of the workload's queries: half far/box, half near-surface when the
     workload has both kinds, else uniform."""
@@ -237,7 +256,7 @@ def run_reference(args, rank, world):
     wl = make_workload(args)
     nthr = oracle.nthreads_default()
     t0 = time.perf_counter()
-    tree = oracle.RefTree(wl.V, wl.F, leaf_size=args.leaf)
+    tree = oracle.RefTree(wl.V, wl.F, leaf_size=CPU_LEAF)
     build_s = time.perf_counter() - t0
     sample = cpu_sample(wl, args.cpu_sample)
     for _ in range(args.warmup):
@@ -253,7 +272,7 @@ def run_reference(args, rank, world):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
         "config": {"workload": wl.name, "triangles": int(len(wl.F)), "queries": int(len(wl.Q)),
-                   "beta": wl.beta, "leaf_size": args.leaf},
+                   "beta": wl.beta, "leaf_size": CPU_LEAF},
         "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": nthr, "kind": "port",
                          "sample": f"{len(sample)} queries per step (half far, half near-surface "
                                    f"where the workload has both) of the {len(wl.Q)}-query "
@@ -288,7 +307,13 @@ def run_ours(args, rank, world, local):
     Fd = torch.from_numpy(wl.F).to(dev)
     Qd = torch.from_numpy(wl.Q).to(dev)
     stream = torch.cuda.current_stream(dev)
-    eng = fwn.FastWindingNumber(Vd, Fd, leaf_size=args.leaf,
+    leaf, block, tuning, tuned = args.leaf, args.block, 0, None
+    if leaf == 0:  # the autotuner's choice for this mesh and query distribution (untimed)
+        leaf, trav, block, tuning, tuned = autotune_choice(fwn, Vd, Fd, Qd)
+    args.leaf, args.block = leaf, block
+    # the handle's defaults are the chosen schedule too, so the host-buffer path (e2e) runs it
+    eng = fwn.FastWindingNumber(Vd, Fd, leaf_size=args.leaf, traversal=trav, block_size=block,
+                                tuning=tuning,
                                 records=fwn.RECORDS_F32 | (0 if args.no_fp64 else fwn.RECORDS_F64))
     torch.cuda.synchronize()
     # build timing (device, CUDA events inside the library): best of 3 extra builds
@@ -302,7 +327,8 @@ def run_ours(args, rank, world, local):
     i_out = torch.empty(n, dtype=torch.uint8, device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > L2 (129 MB)
     L = fwn.library()
-    opts = fwn._opts(precision=fwn.PRECISION_MIXED, traversal=trav, block_size=args.block)
+    opts = fwn._opts(precision=fwn.PRECISION_MIXED, traversal=trav, block_size=args.block,
+                     tuning=tuning)
     sptr = C.c_void_p(stream.cuda_stream)
 
     def query_mixed():
@@ -343,8 +369,10 @@ def run_ours(args, rank, world, local):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 near field/refit)",
         "data": "synthetic",
         "config": {"workload": wl.name, "triangles": int(len(wl.F)), "queries_per_gpu": n,
-                   "beta": wl.beta, "leaf_size": args.leaf, "traversal": args.traversal,
-                   "block": args.block, "l2": "flushed before every step (256 MB write)",
+                   "beta": wl.beta, "leaf_size": args.leaf,
+                   "traversal": "warp" if trav == fwn.TRAVERSAL_WARP else "thread",
+                   "block": args.block, "tuning": tuning, "autotuned": tuned,
+                   "l2": "flushed before every step (256 MB write)",
                    "parallelism": f"replicas x{world} (query shards, no collective)"},
         "build_ms": min(build_ms), "tree": {"nodes": info["num_nodes"], "leaves": info["num_leaves"],
                                             "device_bytes": info["device_bytes"]},
@@ -360,7 +388,7 @@ def run_ours(args, rank, world, local):
     order = eng.query_order(Qd)
     Qs = Qd[order].contiguous()
     opts_k = fwn._opts(precision=fwn.PRECISION_MIXED, traversal=trav, block_size=args.block,
-                       sort_queries=0)
+                       sort_queries=0, tuning=tuning)
 
     def query_kernel():
         fwn._check(L.fwn_query_ex(eng.handle, C.byref(opts_k), C.c_void_p(Qs.data_ptr()), n,
@@ -482,7 +510,7 @@ def run_ours(args, rank, world, local):
         import oracle
         nthr = oracle.nthreads_default()
         t0 = time.perf_counter()
-        tree = oracle.RefTree(wl.V, wl.F, leaf_size=args.leaf)
+        tree = oracle.RefTree(wl.V, wl.F, leaf_size=CPU_LEAF)
         build_s = time.perf_counter() - t0
         sample = cpu_sample(wl, args.cpu_sample)
         tree.query(sample[:1000], nthreads=nthr)
@@ -584,6 +612,12 @@ def run_forest(args, rank, world, local):
     Fd = torch.from_numpy(fo.F).to(dev)
     Qd = torch.from_numpy(fo.Q).to(dev)
     L = fwn.library()
+    tuned = None
+    if args.leaf == 0:  # leaf size picked by the forest autotuner on this forest (untimed)
+        r = fwn.autotune_forest(Vd, fo.voff, Fd, fo.foff, Qd, fo.qoff)
+        args.leaf = r["leaf_size"]
+        tuned = {"leaf_size": r["leaf_size"], "forest_query_ms": r["ms"],
+                 "candidates": r["candidates"]}
     builds = []
     for _ in range(3):
         f2 = fwn.Forest(Vd, fo.voff, Fd, fo.foff, leaf_size=args.leaf, records=fwn.RECORDS_F32)
@@ -635,7 +669,7 @@ def run_forest(args, rank, world, local):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 near field/refit)",
         "data": "synthetic",
         "config": {"workload": fo.name, "meshes": M, "triangles": int(fo.foff[-1]),
-                   "queries": n, "beta": fo.beta, "leaf_size": args.leaf,
+                   "queries": n, "beta": fo.beta, "leaf_size": args.leaf, "autotuned": tuned,
                    "l2": "flushed before every step (256 MB write)", "generation_s": gen_s},
         "build_ms": build_ms, "tree_nodes": forest.info()["num_nodes"],
         "meshes_per_s_build_plus_query": M / ((build_ms + ms) / 1e3),
@@ -669,7 +703,7 @@ def run_forest(args, rank, world, local):
         e2e_s = max_over_ranks(dist, sum(te) / len(te), dev)
         result["e2e"] = {"value": job_value(n, world, e2e_s), "unit": "queries/s",
                          "h2d_bytes_per_step": n * 12, "d2h_bytes_per_step": n * 5,
-                         "ms_per_step": e2e_s * 1e3,
+                         "ms_per_step": e2e_s * 1e3, "ms_each": [t * 1e3 for t in te],
                          "api": "fwn_forest_query (pinned host points copied in, results out)"}
         del Qe
     # ---- CPU restatement of the reference path on a few meshes (rank 0, N=1) ---------------
@@ -687,7 +721,7 @@ def run_forest(args, rank, world, local):
             q0, q1 = int(fo.qoff[m]), int(fo.qoff[m + 1])
             idx = np.sort(rng.choice(q1 - q0, min(per, q1 - q0), replace=False)) + q0
             t0 = time.perf_counter()
-            tree = oracle.RefTree(Vm, Fm, leaf_size=args.leaf)
+            tree = oracle.RefTree(Vm, Fm, leaf_size=CPU_LEAF)
             build_s += time.perf_counter() - t0
             t0 = time.perf_counter()
             om, inn = tree.query(fo.Q[idx], beta=fo.beta, nthreads=nthr)

@@ -216,7 +216,7 @@ FWN_API fwn_status fwn_export_moments(fwn_handle h, double* moments);
 
 /* Autotuner (no reference counterpart: the reference has no tunable parameters). For one mesh
  * (DEVICE arrays) and a representative DEVICE sample of query points, builds the tree for leaf
- * sizes 4, 8 and 16 and times every query schedule (warp cursor with and without the register
+ * sizes 4, 8, 12 and 16 and times every query schedule (warp cursor with and without the register
  * cap; thread per query with blocks of 64/128/256) with CUDA events; returns the fastest. Apply it
  * with cfg.leaf_size, cfg.traversal, cfg.block_size, cfg.tuning. `base` gives beta and the
  * precision knobs (NULL = defaults). cache_path (may be NULL) names a text file keyed by GPU name
@@ -226,6 +226,19 @@ FWN_API fwn_status fwn_autotune(const float* d_vertices, int64_t num_vertices,
                                 const int32_t* d_triangles, int64_t num_triangles,
                                 const float* d_points, int64_t num_points, const fwn_config* base,
                                 const char* cache_path, fwn_tune_result* out, void* stream);
+
+/* Forest autotuner (no reference counterpart). The mixed forest query is one persistent kernel,
+ * so its one knob is the leaf size: builds the forest (DEVICE vertex/triangle arrays, HOST offset
+ * arrays as in fwn_forest_build_device) for leaf sizes 4, 8, 12 and 16 and times the forest query
+ * on the DEVICE points with HOST query_offsets [num_meshes + 1]. Returns the fastest leaf size
+ * (traversal WARP, block 128). Cache as in fwn_autotune, keyed also by log2 of the mesh count.
+ * Synchronous on `stream`. */
+FWN_API fwn_status fwn_forest_autotune(const float* d_vertices, const int64_t* vertex_offsets,
+                                       const int32_t* d_triangles,
+                                       const int64_t* triangle_offsets, int64_t num_meshes,
+                                       const float* d_points, const int64_t* query_offsets,
+                                       const fwn_config* base, const char* cache_path,
+                                       fwn_tune_result* out, void* stream);
 
 /* Voxel-grid sign pass (batched form of the winding-number signing in volume::mesh_to_volume,
  * modules/volume/src/mesh_to_volume.cpp:156-183, which calls is_inside once per voxel). Classifies

@@ -85,7 +85,8 @@ EXPORTS = ["fwn_config_default", "fwn_last_error", "fwn_version", "fwn_build", "
            "fwn_destroy", "fwn_get_info", "fwn_query", "fwn_query_ex", "fwn_query_host",
            "fwn_export_tree", "fwn_export_moments", "fwn_forest_build",
            "fwn_forest_build_device", "fwn_forest_query", "fwn_query_noalloc", "fwn_autotune",
-           "fwn_query_grid", "fwn_orientation_criterion", "fwn_query_order"]
+           "fwn_query_grid", "fwn_orientation_criterion", "fwn_query_order",
+           "fwn_forest_autotune"]
 
 
 def library():
@@ -125,11 +126,13 @@ def library():
     L.fwn_orientation_criterion.argtypes = [P, P, i64, P, i64, C.c_float, C.c_float, P, P, P]
     L.fwn_autotune.argtypes = [P, i64, P, i64, P, i64, C.POINTER(fwn_config), C.c_char_p,
                                C.POINTER(fwn_tune_result), P]
+    L.fwn_forest_autotune.argtypes = [P, P, P, P, i64, P, P, C.POINTER(fwn_config), C.c_char_p,
+                                      C.POINTER(fwn_tune_result), P]
     for name in ("fwn_build", "fwn_build_device", "fwn_destroy", "fwn_get_info", "fwn_query",
                  "fwn_query_ex", "fwn_query_host", "fwn_export_tree", "fwn_export_moments",
                  "fwn_forest_build", "fwn_forest_build_device", "fwn_forest_query",
                  "fwn_query_noalloc", "fwn_autotune", "fwn_query_grid",
-                 "fwn_orientation_criterion"):
+                 "fwn_orientation_criterion", "fwn_query_order", "fwn_forest_autotune"):
         getattr(L, name).restype = st
     _lib = L
     return L
@@ -463,3 +466,28 @@ def autotune(vertices, facets, points, *, cache_path=None, config: fwn_config | 
     d["config"] = {"leaf_size": r.leaf_size, "traversal": r.traversal,
                    "block_size": r.block_size, "tuning": r.tuning}
     return d
+
+
+def autotune_forest(vertices, voff, facets, foff, points, qoff, *, cache_path=None,
+                    config: fwn_config | None = None, **cfg_overrides) -> dict:
+    """Picks the leaf size of a forest by building it for every candidate and timing the
+    persistent forest query on ``points`` (CUDA tensor or array, [sum Q, 3]) with host offsets
+    ``qoff``; ``result["config"]`` can be passed to ``Forest``."""
+    import torch
+
+    def dev(x, dt):
+        return x.detach().to(dt).contiguous() if _is_cuda_tensor(x) else \
+            torch.as_tensor(np.asarray(x)).to(dt).cuda().contiguous()
+    V, F, Q = dev(vertices, torch.float32), dev(facets, torch.int32), dev(points, torch.float32)
+    vo, fo, qo = (np.ascontiguousarray(o, dtype=np.int64) for o in (voff, foff, qoff))
+    cfg = config if config is not None else config_default(**cfg_overrides)
+    r = fwn_tune_result()
+    _check(library().fwn_forest_autotune(
+        C.c_void_p(V.data_ptr()), vo.ctypes.data_as(C.c_void_p), C.c_void_p(F.data_ptr()),
+        fo.ctypes.data_as(C.c_void_p), len(vo) - 1, C.c_void_p(Q.data_ptr()),
+        qo.ctypes.data_as(C.c_void_p), C.byref(cfg), cache_path.encode() if cache_path else None,
+        C.byref(r), _stream_ptr(None)))
+    d = r.as_dict()
+    d["config"] = {"leaf_size": r.leaf_size}
+    return d
+

@@ -33,7 +33,7 @@ const Candidate kCandidates[] = {
     {FWN_TRAVERSAL_THREAD, 128, 0},
     {FWN_TRAVERSAL_THREAD, 256, 0},
 };
-const int kLeafSizes[] = {4, 8, 16};
+const int kLeafSizes[] = {4, 8, 12, 16};
 
 std::mutex g_cache_mutex;
 
@@ -155,6 +155,94 @@ extern "C" FWN_API fwn_status fwn_autotune(const float* d_V, int64_t nv, const i
                     best.block_size = a.block_size;
                     best.tuning = a.tuning;
                 }
+            }
+        }
+        best.candidates = evaluated;
+        *out = best;
+        if (cache_path) cache_store(cache_path, key, best);
+        return FWN_OK;
+    } catch (const Error& err) {
+        set_last_error(err.what());
+        return err.status;
+    } catch (const std::exception& err) {
+        set_last_error(err.what());
+        return FWN_INTERNAL;
+    } catch (...) {
+        set_last_error("unknown error");
+        return FWN_INTERNAL;
+    }
+}
+
+// Forest form: the mixed forest query is one persistent kernel, so the leaf size is its one
+// knob. Each candidate builds the whole forest and times the forest query on the caller's
+// queries (median of three after a warm-up).
+extern "C" FWN_API fwn_status fwn_forest_autotune(const float* d_V, const int64_t* vertex_offsets,
+                                                  const int32_t* d_F,
+                                                  const int64_t* triangle_offsets,
+                                                  int64_t num_meshes, const float* d_Q,
+                                                  const int64_t* query_offsets,
+                                                  const fwn_config* base, const char* cache_path,
+                                                  fwn_tune_result* out, void* stream) {
+    try {
+        if (!out) throw Error(FWN_INVALID_ARG, "out is null");
+        std::memset(out, 0, sizeof(*out));
+        if (num_meshes < 1) throw Error(FWN_INVALID_ARG, "num_meshes must be >= 1");
+        if (!vertex_offsets || !triangle_offsets || !query_offsets)
+            throw Error(FWN_INVALID_ARG, "offset arrays are null");
+        const int64_t nv = vertex_offsets[num_meshes], nf = triangle_offsets[num_meshes];
+        const int64_t n = query_offsets[num_meshes];
+        if (nv < 0 || nf < 0 || n <= 0) throw Error(FWN_INVALID_ARG, "sizes must be >= 0 (queries > 0)");
+        if ((nv && !d_V) || (nf && !d_F) || !d_Q) throw Error(FWN_INVALID_ARG, "null pointer");
+        for (int64_t m = 0; m < num_meshes; ++m)
+            if (vertex_offsets[m + 1] < vertex_offsets[m] || triangle_offsets[m + 1] < triangle_offsets[m] ||
+                query_offsets[m + 1] < query_offsets[m])
+                throw Error(FWN_INVALID_ARG, "offsets must be non-decreasing");
+        fwn_config cfg;
+        fwn_config_default(&cfg);
+        if (base) cfg = *base;
+        cfg.records = FWN_RECORDS_F32;
+        const std::string key = "forest|" + cache_key(nf, n) + "|" + std::to_string(log2_bucket(num_meshes));
+        if (cache_path && cache_lookup(cache_path, key, out)) return FWN_OK;
+        cudaStream_t st = static_cast<cudaStream_t>(stream);
+        Scratch wbuf((size_t)n * sizeof(float), st), ibuf((size_t)n, st);
+        cudaEvent_t e0, e1;
+        FWN_CUDA_CHECK(cudaEventCreate(&e0));
+        FWN_CUDA_CHECK(cudaEventCreate(&e1));
+        std::unique_ptr<cudaEvent_t[], void (*)(cudaEvent_t*)> guard(
+            new cudaEvent_t[2]{e0, e1}, [](cudaEvent_t* p) {
+                cudaEventDestroy(p[0]);
+                cudaEventDestroy(p[1]);
+                delete[] p;
+            });
+        fwn_tune_result best;
+        std::memset(&best, 0, sizeof(best));
+        best.ms = 1e300;
+        int evaluated = 0;
+        for (int leaf : kLeafSizes) {
+            Engine e;
+            e.cfg = cfg;
+            e.cfg.leaf_size = leaf;
+            FWN_CUDA_CHECK(cudaGetDevice(&e.device));
+            build_forest(e, d_V, vertex_offsets, d_F, triangle_offsets, num_meshes, st);
+            QueryArgs a = resolve_query_args(e, nullptr);
+            a.precision = FWN_PRECISION_MIXED;
+            query_forest(e, a, d_Q, query_offsets, wbuf.as<float>(), ibuf.as<uint8_t>(), st);
+            float t[3];
+            for (int r = 0; r < 3; ++r) {
+                FWN_CUDA_CHECK(cudaEventRecord(e0, st));
+                query_forest(e, a, d_Q, query_offsets, wbuf.as<float>(), ibuf.as<uint8_t>(), st);
+                FWN_CUDA_CHECK(cudaEventRecord(e1, st));
+                FWN_CUDA_CHECK(cudaEventSynchronize(e1));
+                FWN_CUDA_CHECK(cudaEventElapsedTime(&t[r], e0, e1));
+            }
+            std::sort(t, t + 3);
+            ++evaluated;
+            if (t[1] < best.ms) {
+                best.ms = t[1];
+                best.leaf_size = leaf;
+                best.traversal = FWN_TRAVERSAL_WARP;
+                best.block_size = 128;
+                best.tuning = 0;
             }
         }
         best.candidates = evaluated;

@@ -181,7 +181,7 @@ __device__ __forceinline__ float tri_omega_mixed(float v0x, float v0y, float v0z
         const float dc = sqrt_fast(sx * sx + sy * sy + sz * sz) * (1.0f / 3.0f);
         if (dc - rt < tau) {
             const float prod = la * lb * lc;
-            const bool ill = prod > cond * sqrtf(fmaf(det, det, D * D)) ||
+            const bool ill = prod > cond * sqrt_fast(fmaf(det, det, D * D)) ||
                              (D <= 0.f && fabsf(det) <= 1e-6f * prod);
             if (ill) {
                 if (STATS) ++qc.tri64;

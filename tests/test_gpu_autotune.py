@@ -19,8 +19,8 @@ def test_autotune_choice_and_cache(tmp_path):
     wl = W.displaced_icosphere_workload(nu=60, n_queries=60_000)
     cache = tmp_path / "tune.txt"
     r = fwn.autotune(wl.V, wl.F, wl.Q, cache_path=str(cache))
-    assert r["from_cache"] == 0 and r["candidates"] == 15 and r["ms"] > 0
-    assert r["leaf_size"] in (4, 8, 16)
+    assert r["from_cache"] == 0 and r["candidates"] == 20 and r["ms"] > 0
+    assert r["leaf_size"] in (4, 8, 12, 16)
     assert r["traversal"] in (fwn.TRAVERSAL_THREAD, fwn.TRAVERSAL_WARP)
     assert r["block_size"] % 32 == 0
     # the cached answer comes back without timing
@@ -36,3 +36,29 @@ def test_autotune_choice_and_cache(tmp_path):
     w64, _ = eng.query(Qd, precision=fwn.PRECISION_FP64)
     torch.cuda.synchronize()
     assert float((w.double() - w64.double()).abs().max()) / FOUR_PI <= 2e-6
+
+
+def test_forest_autotune_choice_and_cache(tmp_path):
+    import torch
+    torch.cuda.set_device(0)
+    fo = W.batched_forest_workload(n_meshes=12, seed=6, f_lo=500, f_hi=20000, q_lo=500, q_hi=20000)
+    cache = tmp_path / "tune_forest.txt"
+    r = fwn.autotune_forest(fo.V, fo.voff, fo.F, fo.foff, fo.Q, fo.qoff, cache_path=str(cache))
+    assert r["from_cache"] == 0 and r["candidates"] == 4 and r["ms"] > 0
+    assert r["leaf_size"] in (4, 8, 12, 16) and r["traversal"] == fwn.TRAVERSAL_WARP
+    r2 = fwn.autotune_forest(fo.V, fo.voff, fo.F, fo.foff, fo.Q, fo.qoff, cache_path=str(cache))
+    assert r2["from_cache"] == 1 and r2["leaf_size"] == r["leaf_size"]
+    # the chosen forest agrees with its FP64 form
+    forest = fwn.Forest(fo.V, fo.voff, fo.F, fo.foff, records=fwn.RECORDS_F32 | fwn.RECORDS_F64,
+                        **r["config"])
+    Qd = torch.from_numpy(fo.Q).cuda()
+    w, _ = forest.query_forest(Qd, fo.qoff)
+    w64, _ = forest.query_forest(Qd, fo.qoff, precision=fwn.PRECISION_FP64)
+    torch.cuda.synchronize()
+    assert float((w.double() - w64.double()).abs().max()) / FOUR_PI <= 2e-6
+    # invalid offsets are refused
+    bad = fo.qoff.copy()
+    bad[1], bad[2] = bad[2], bad[1]
+    if bad[1] != bad[2]:
+        with pytest.raises(fwn.WindingError, match="non-decreasing"):
+            fwn.autotune_forest(fo.V, fo.voff, fo.F, fo.foff, fo.Q, bad)

@@ -281,3 +281,50 @@ def test_forest_matches_cpu_restatement(torch_cuda, oracle_mod):
     wr = r / FOUR_PI
     band = np.abs(wr - 0.5) > 1e-3
     np.testing.assert_array_equal(ins[band].astype(bool), wr[band] > 0.5)
+
+
+def test_graph_capture_replay(torch_cuda):
+    """Queries captured in a CUDA graph (scratch becomes graph memory nodes) replay to the same
+    bits as direct calls: one mesh through fwn_query, and a forest through fwn_forest_query with
+    its query offsets in pinned host memory."""
+    torch = torch_cuda
+    L = fwn.library()
+    wl = W.displaced_icosphere_workload(nu=30, n_queries=40_000)
+    eng = _engine(wl.V, wl.F)
+    Q = torch.from_numpy(wl.Q).cuda()
+    ref_w, ref_i = eng.query(Q)
+    fo = W.batched_forest_workload(n_meshes=6, seed=2, f_lo=500, f_hi=5000, q_lo=100, q_hi=4000)
+    forest = fwn.Forest(fo.V, fo.voff, fo.F, fo.foff)
+    Qf = torch.from_numpy(fo.Q).cuda()
+    ref_fw, ref_fi = forest.query_forest(Qf, fo.qoff)
+    torch.cuda.synchronize()
+    w = torch.empty_like(ref_w)
+    i = torch.empty_like(ref_i)
+    fw = torch.empty_like(ref_fw)
+    fi = torch.empty_like(ref_fi)
+    qoff = torch.from_numpy(fo.qoff.astype(np.int64)).pin_memory()
+    opts = fwn._opts(precision=fwn.PRECISION_MIXED)
+
+    def calls(stream):
+        sp = C.c_void_p(stream.cuda_stream)
+        fwn._check(L.fwn_query(eng.handle, C.c_void_p(Q.data_ptr()), len(Q), C.c_void_p(w.data_ptr()),
+                               C.c_void_p(i.data_ptr()), sp))
+        fwn._check(L.fwn_forest_query(forest.handle, C.c_void_p(Qf.data_ptr()),
+                                      C.c_void_p(qoff.data_ptr()), C.c_void_p(fw.data_ptr()),
+                                      C.c_void_p(fi.data_ptr()), C.byref(opts), sp))
+
+    side = torch.cuda.Stream()
+    side.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(side):
+        calls(side)  # warm-up outside the capture
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        calls(torch.cuda.current_stream())
+    for _ in range(2):
+        w.zero_()
+        fw.zero_()
+        g.replay()
+        torch.cuda.synchronize()
+        assert torch.equal(w, ref_w) and torch.equal(i, ref_i)
+        assert torch.equal(fw, ref_fw) and torch.equal(fi, ref_fi)
