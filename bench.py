@@ -52,9 +52,11 @@ BYTES_NODE_FAR = 96    # sectors 1-3 (far-field coefficients)
 BYTES_TRI = 48
 BYTES_QUERY_IO = 12 + 4 + 1 + 4  # point in, Omega + inside out, sort index
 CPU_LEAF = 8  # leaf size of the CPU restatement of the reference tree, in every CPU timing
-# DRAM bytes (read + write) of one traversal launch, from the one-pass ncu capture of the same
-# command line (profiles/k_query_warp_traffic_icosphere2m_q10m.md); other workloads: not captured
-NCU_TRAFFIC = {"displaced_icosphere_nu316_q10000000": 1.38e9 + 304.88e6}
+# DRAM bytes (read + write) of one traversal launch, keyed by (workload, leaf size), from the
+# one-pass ncu captures of the same command lines (profiles/k_query_warp_traffic_icosphere2m_q10m.md);
+# other workloads and leaf sizes: not captured (traffic null)
+NCU_TRAFFIC = {("displaced_icosphere_nu316_q10000000", 12): 1.34e9 + 299.45e6,
+               ("displaced_icosphere_nu316_q10000000", 16): 1.31e9 + 294.86e6}
 
 
 def parse():
@@ -417,7 +419,7 @@ def run_ours(args, rank, world, local):
     sm_max = clocks.get("sm_max_mhz") or measured_peaks().get("sm_max_mhz") or 2070.0
     peak_fp32 = props.multi_processor_count * 128 * 2 * sm_max * 1e6 / 1e12
     achieved = flops / (kernel_ms / 1e3) / 1e12
-    traffic = NCU_TRAFFIC.get(wl.name) if world == 1 else None
+    traffic = NCU_TRAFFIC.get((wl.name, args.leaf)) if world == 1 else None
     hbm_peak = measured_peaks().get("hbm_gbs")
     result["roofline"] = {
         "bound": "fp32", "achieved": achieved, "peak": peak_fp32, "unit": "TFLOP/s",
