@@ -83,7 +83,8 @@ typedef struct fwn_config {
     float fp64_cond;       /* ... and its FP32 evaluation is ill-conditioned: |a||b||c| >
                               fp64_cond * |(det, D)|, or det is within rounding of 0 with D <= 0.
                               0 = every triangle within the distance. Default 4 */
-    int32_t tuning;        /* schedule variant (0 = default; set by fwn_autotune) */
+    int32_t tuning;        /* schedule variant (0 = default; set by fwn_autotune). Warp schedule:
+                              register cap 64 (0), 72 (1) or none (2) */
     int32_t reserved[6];
 } fwn_config;
 
@@ -216,8 +217,8 @@ FWN_API fwn_status fwn_export_moments(fwn_handle h, double* moments);
 
 /* Autotuner (no reference counterpart: the reference has no tunable parameters). For one mesh
  * (DEVICE arrays) and a representative DEVICE sample of query points, builds the tree for leaf
- * sizes 4, 8, 12 and 16 and times every query schedule (warp cursor with and without the register
- * cap; thread per query with blocks of 64/128/256) with CUDA events; returns the fastest. Apply it
+ * sizes 4, 8, 12 and 16 and times every query schedule (warp cursor with a 64- or 72-register cap
+ * or none; thread per query with blocks of 64/128/256) with CUDA events; returns the fastest. Apply it
  * with cfg.leaf_size, cfg.traversal, cfg.block_size, cfg.tuning. `base` gives beta and the
  * precision knobs (NULL = defaults). cache_path (may be NULL) names a text file keyed by GPU name
  * and log2 of the triangle and query counts: a hit returns without timing, a miss appends.

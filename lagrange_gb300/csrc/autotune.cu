@@ -28,6 +28,7 @@ struct Candidate {
 
 const Candidate kCandidates[] = {
     {FWN_TRAVERSAL_WARP, 128, 0},    // warp cursor, 64-register cap
+    {FWN_TRAVERSAL_WARP, 128, 1},    // warp cursor, 72-register cap
     {FWN_TRAVERSAL_WARP, 128, 2},    // warp cursor, no register cap
     {FWN_TRAVERSAL_THREAD, 64, 0},   // thread per query
     {FWN_TRAVERSAL_THREAD, 128, 0},

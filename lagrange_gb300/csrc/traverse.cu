@@ -785,12 +785,14 @@ void query_mesh(const Engine& e, int mesh, const QueryArgs& a, const float* d_po
             k_query_f64<false><<<grid_for(n, 128), 128, 0, st>>>(e.nodes64, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_omega64, d_status, d_stats);
     } else if (a.traversal == FWN_TRAVERSAL_WARP) {
         const dim3 g = grid_for(n, WARP_BLOCK);
-        // default: register cap of 64 (8 blocks = 32 warps per SM); tuning 2: no cap (more
-        // registers, fewer resident warps)
+        // register caps: tuning 0 (default) 64 registers (8 blocks = 32 warps per SM), tuning 1
+        // 72 registers (7 blocks), tuning 2 none (more registers, fewer resident warps)
         if (want_stats)
             k_query_warp<true, 1><<<g, WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, d_stats);
         else if (a.tuning == 2)
             k_query_warp<false, 1><<<g, WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, d_stats);
+        else if (a.tuning == 1)
+            k_query_warp<false, 7><<<g, WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, d_stats);
         else
             k_query_warp<false, 8><<<g, WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, d_stats);
     } else {
@@ -937,6 +939,8 @@ void query_mesh_prealloc(const Engine& e, int mesh, const QueryArgs& a, const fl
         const dim3 g = grid_for(n, WARP_BLOCK);
         if (a.tuning == 2)
             k_query_warp<false, 1><<<g, WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, nullptr);
+        else if (a.tuning == 1)
+            k_query_warp<false, 7><<<g, WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, nullptr);
         else
             k_query_warp<false, 8><<<g, WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, nullptr);
     } else {
