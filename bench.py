@@ -614,24 +614,24 @@ def run_forest(args, rank, world, local):
     Fd = torch.from_numpy(fo.F).to(dev)
     Qd = torch.from_numpy(fo.Q).to(dev)
     L = fwn.library()
-    tuned = None
+    tuned, tuning = None, 0
     if args.leaf == 0:  # leaf size picked by the forest autotuner on this forest (untimed)
         r = fwn.autotune_forest(Vd, fo.voff, Fd, fo.foff, Qd, fo.qoff)
-        args.leaf = r["leaf_size"]
-        tuned = {"leaf_size": r["leaf_size"], "forest_query_ms": r["ms"],
-                 "candidates": r["candidates"]}
+        args.leaf, tuning = r["leaf_size"], r["tuning"]
+        tuned = {"leaf_size": r["leaf_size"], "tuning": r["tuning"],
+                 "forest_query_ms": r["ms"], "candidates": r["candidates"]}
     builds = []
     for _ in range(3):
         f2 = fwn.Forest(Vd, fo.voff, Fd, fo.foff, leaf_size=args.leaf, records=fwn.RECORDS_F32)
         builds.append(f2.info()["build_ms"])
         f2.close()
-    forest = fwn.Forest(Vd, fo.voff, Fd, fo.foff, leaf_size=args.leaf,
+    forest = fwn.Forest(Vd, fo.voff, Fd, fo.foff, leaf_size=args.leaf, tuning=tuning,
                         records=fwn.RECORDS_F32 | (0 if args.no_fp64 else fwn.RECORDS_F64))
     qoff = torch.from_numpy(fo.qoff.astype(np.int64)).pin_memory()  # pinned: capturable copy
     w = torch.empty(n, dtype=torch.float32, device=dev)
     ins = torch.empty(n, dtype=torch.uint8, device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    opts = fwn._opts(precision=fwn.PRECISION_MIXED)
+    opts = fwn._opts(precision=fwn.PRECISION_MIXED, tuning=tuning)
 
     def q_mixed(stream_ptr):
         fwn._check(L.fwn_forest_query(forest.handle, C.c_void_p(Qd.data_ptr()),

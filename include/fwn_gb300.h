@@ -229,11 +229,11 @@ FWN_API fwn_status fwn_autotune(const float* d_vertices, int64_t num_vertices,
                                 const char* cache_path, fwn_tune_result* out, void* stream);
 
 /* Forest autotuner (no reference counterpart). The mixed forest query is one persistent kernel,
- * so its one knob is the leaf size: builds the forest (DEVICE vertex/triangle arrays, HOST offset
- * arrays as in fwn_forest_build_device) for leaf sizes 4, 8, 12 and 16 and times the forest query
- * on the DEVICE points with HOST query_offsets [num_meshes + 1]. Returns the fastest leaf size
- * (traversal WARP, block 128). Cache as in fwn_autotune, keyed also by log2 of the mesh count.
- * Synchronous on `stream`. */
+ * so its knobs are the leaf size and the register cap: builds the forest (DEVICE vertex/triangle
+ * arrays, HOST offset arrays as in fwn_forest_build_device) for leaf sizes 4, 8, 12 and 16 and
+ * times the forest query with tuning 0 and 1 on the DEVICE points with HOST query_offsets
+ * [num_meshes + 1]. Returns the fastest (leaf size, tuning; traversal WARP, block 128). Cache as
+ * in fwn_autotune, keyed also by log2 of the mesh count. Synchronous on `stream`. */
 FWN_API fwn_status fwn_forest_autotune(const float* d_vertices, const int64_t* vertex_offsets,
                                        const int32_t* d_triangles,
                                        const int64_t* triangle_offsets, int64_t num_meshes,

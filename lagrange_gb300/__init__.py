@@ -470,8 +470,8 @@ def autotune(vertices, facets, points, *, cache_path=None, config: fwn_config | 
 
 def autotune_forest(vertices, voff, facets, foff, points, qoff, *, cache_path=None,
                     config: fwn_config | None = None, **cfg_overrides) -> dict:
-    """Picks the leaf size of a forest by building it for every candidate and timing the
-    persistent forest query on ``points`` (CUDA tensor or array, [sum Q, 3]) with host offsets
+    """Picks the leaf size and register-cap variant of a forest by building it for every
+    candidate leaf size and timing the persistent forest query on ``points`` (CUDA tensor or array, [sum Q, 3]) with host offsets
     ``qoff``; ``result["config"]`` can be passed to ``Forest``."""
     import torch
 
@@ -488,6 +488,6 @@ def autotune_forest(vertices, voff, facets, foff, points, qoff, *, cache_path=No
         qo.ctypes.data_as(C.c_void_p), C.byref(cfg), cache_path.encode() if cache_path else None,
         C.byref(r), _stream_ptr(None)))
     d = r.as_dict()
-    d["config"] = {"leaf_size": r.leaf_size}
+    d["config"] = {"leaf_size": r.leaf_size, "tuning": r.tuning}
     return d
 

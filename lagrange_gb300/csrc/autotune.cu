@@ -174,9 +174,9 @@ extern "C" FWN_API fwn_status fwn_autotune(const float* d_V, int64_t nv, const i
     }
 }
 
-// Forest form: the mixed forest query is one persistent kernel, so the leaf size is its one
-// knob. Each candidate builds the whole forest and times the forest query on the caller's
-// queries (median of three after a warm-up).
+// Forest form: the mixed forest query is one persistent kernel, so its knobs are the leaf size
+// and the register cap. Each leaf size builds the whole forest; each (leaf, cap) pair times the
+// forest query on the caller's queries (median of three after a warm-up).
 extern "C" FWN_API fwn_status fwn_forest_autotune(const float* d_V, const int64_t* vertex_offsets,
                                                   const int32_t* d_F,
                                                   const int64_t* triangle_offsets,
@@ -225,25 +225,28 @@ extern "C" FWN_API fwn_status fwn_forest_autotune(const float* d_V, const int64_
             e.cfg.leaf_size = leaf;
             FWN_CUDA_CHECK(cudaGetDevice(&e.device));
             build_forest(e, d_V, vertex_offsets, d_F, triangle_offsets, num_meshes, st);
-            QueryArgs a = resolve_query_args(e, nullptr);
-            a.precision = FWN_PRECISION_MIXED;
-            query_forest(e, a, d_Q, query_offsets, wbuf.as<float>(), ibuf.as<uint8_t>(), st);
-            float t[3];
-            for (int r = 0; r < 3; ++r) {
-                FWN_CUDA_CHECK(cudaEventRecord(e0, st));
+            for (int tuning = 0; tuning <= 1; ++tuning) {  // 64- and 72-register caps
+                QueryArgs a = resolve_query_args(e, nullptr);
+                a.precision = FWN_PRECISION_MIXED;
+                a.tuning = tuning;
                 query_forest(e, a, d_Q, query_offsets, wbuf.as<float>(), ibuf.as<uint8_t>(), st);
-                FWN_CUDA_CHECK(cudaEventRecord(e1, st));
-                FWN_CUDA_CHECK(cudaEventSynchronize(e1));
-                FWN_CUDA_CHECK(cudaEventElapsedTime(&t[r], e0, e1));
-            }
-            std::sort(t, t + 3);
-            ++evaluated;
-            if (t[1] < best.ms) {
-                best.ms = t[1];
-                best.leaf_size = leaf;
-                best.traversal = FWN_TRAVERSAL_WARP;
-                best.block_size = 128;
-                best.tuning = 0;
+                float t[3];
+                for (int r = 0; r < 3; ++r) {
+                    FWN_CUDA_CHECK(cudaEventRecord(e0, st));
+                    query_forest(e, a, d_Q, query_offsets, wbuf.as<float>(), ibuf.as<uint8_t>(), st);
+                    FWN_CUDA_CHECK(cudaEventRecord(e1, st));
+                    FWN_CUDA_CHECK(cudaEventSynchronize(e1));
+                    FWN_CUDA_CHECK(cudaEventElapsedTime(&t[r], e0, e1));
+                }
+                std::sort(t, t + 3);
+                ++evaluated;
+                if (t[1] < best.ms) {
+                    best.ms = t[1];
+                    best.leaf_size = leaf;
+                    best.traversal = FWN_TRAVERSAL_WARP;
+                    best.block_size = 128;
+                    best.tuning = tuning;
+                }
             }
         }
         best.candidates = evaluated;

@@ -837,7 +837,9 @@ void query_grid(const Engine& e, int mesh, const QueryArgs& a, const float origi
     Scratch status(sizeof(unsigned), st);
     FWN_CUDA_CHECK(cudaMemsetAsync(status.p, 0, sizeof(unsigned), st));
     const int64_t threads = nbricks * 32;
-    k_query_grid<8><<<grid_for(threads, WARP_BLOCK), WARP_BLOCK, 0, st>>>(
+    // register caps as in the point query: tuning 0 -> 64, 1 -> 72, 2 -> none
+    auto kern = a.tuning == 2 ? k_query_grid<1> : a.tuning == 1 ? k_query_grid<7> : k_query_grid<8>;
+    kern<<<grid_for(threads, WARP_BLOCK), WARP_BLOCK, 0, st>>>(
         e.nodes32, e.tris, mi, origin[0], origin[1], origin[2], spacing[0], spacing[1], spacing[2],
         nx, ny, nz, bx, by, nbricks, a.beta, d_omega, d_inside, status.as<unsigned>());
     FWN_CUDA_CHECK(cudaGetLastError());
@@ -885,13 +887,14 @@ void query_forest(const Engine& e, const QueryArgs& a, const float* d_points,
     int dev = 0, sms = 0, per_sm = 0;
     FWN_CUDA_CHECK(cudaGetDevice(&dev));
     FWN_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    FWN_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_forest_warp<8>, WARP_BLOCK, 0));
+    // register caps as in the point query: tuning 0 -> 64, 1 -> 72, 2 -> none
+    auto kern = a.tuning == 2 ? k_forest_warp<1> : a.tuning == 1 ? k_forest_warp<7> : k_forest_warp<8>;
+    FWN_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, WARP_BLOCK, 0));
     const int64_t chunks = (n + 31) / 32;
     const int64_t want = (chunks + WARP_BLOCK / 32 - 1) / (WARP_BLOCK / 32);
     const unsigned grid = (unsigned)std::min<int64_t>(want, (int64_t)sms * std::max(per_sm, 1));
-    k_forest_warp<8><<<grid, WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, e.meshes, d_points, keys, order,
-                                                 n, a.beta, d_omega, d_inside, d_status + 1,
-                                                 d_status);
+    kern<<<grid, WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, e.meshes, d_points, keys, order, n, a.beta,
+                                      d_omega, d_inside, d_status + 1, d_status);
     FWN_CUDA_CHECK(cudaGetLastError());
 }
 
