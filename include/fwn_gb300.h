@@ -78,7 +78,7 @@ typedef struct fwn_config {
     int32_t precision;     /* default query form, FWN_PRECISION_*. Default MIXED */
     int32_t traversal;     /* default schedule, FWN_TRAVERSAL_*. Default AUTO */
     int32_t block_size;    /* query kernel block size (multiple of 32, <= 1024); 0 = tuned */
-    int32_t sort_queries;  /* 1: Morton-sort queries before traversal (default), 0: input order */
+    int32_t sort_queries;  /* 1: sort queries along a Hilbert curve first (default), 0: input order */
     float fp64_near_scale; /* FP64 near field if triangle is within scale*bbox_diagonal. 1e-3 */
     float fp64_cond;       /* ... and its FP32 evaluation is ill-conditioned: |a||b||c| >
                               fp64_cond * |(det, D)|, or det is within rounding of 0 with D <= 0.
@@ -178,7 +178,7 @@ FWN_API fwn_status fwn_query_ex(fwn_handle h, const fwn_query_opts* opts,
 
 /* No counterpart in the reference (it answers one point per call). Writes the permutation the
  * query applies to group nearby points into warps: d_order[k] (uint32, device) is the index of
- * the k-th point in Morton order of the mesh's frame. A caller that queries the same points
+ * the k-th point in Hilbert-curve order of the mesh's frame. A caller that queries the same points
  * repeatedly can gather them once in this order and pass sort_queries = 0 in fwn_query_opts;
  * the results are the same. Asynchronous on `stream`. */
 FWN_API fwn_status fwn_query_order(fwn_handle h, const float* d_points, int64_t n,

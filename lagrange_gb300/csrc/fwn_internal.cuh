@@ -220,13 +220,13 @@ void query_forest(const Engine& e, const QueryArgs& a, const float* d_points,
 
 QueryArgs resolve_query_args(const Engine& e, const fwn_query_opts* opts);
 
-// The permutation query_mesh applies when sort_queries is set (Morton order of the points in
+// The permutation query_mesh applies when sort_queries is set (Hilbert-curve order of the points in
 // mesh `mesh`'s frame): d_order[k] = index of the k-th point. Async.
 void query_order(const Engine& e, int mesh, const float* d_points, int64_t n, uint32_t* d_order,
                  cudaStream_t stream);
 
 // Query with caller-provided device scratch (no allocation): `scratch` holds the status word and
-// the Morton-sort buffers, at least query_prealloc_bytes(n) bytes, 256-byte aligned. Async.
+// the query-sort buffers, at least query_prealloc_bytes(n) bytes, 256-byte aligned. Async.
 size_t query_prealloc_bytes(int64_t n);
 void query_mesh_prealloc(const Engine& e, int mesh, const QueryArgs& a, const float* d_points,
                          int64_t n, float* d_omega, uint8_t* d_inside, void* scratch,

@@ -523,7 +523,7 @@ k_query_grid(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
     }
 }
 
-// Forest: one persistent launch over all meshes. Queries are sorted by (mesh, Morton code); each
+// Forest: one persistent launch over all meshes. Queries are sorted by (mesh, Hilbert index); each
 // warp takes the next 32 sorted queries from a global work counter until none are left.
 template <int MINB>
 __global__ void __launch_bounds__(WARP_BLOCK, MINB)
@@ -628,7 +628,7 @@ k_query_f64(const NodeF64* __restrict__ nodes, const TriF32* __restrict__ tris, 
     if (STATS) flush_stats(qc, stats);
 }
 
-// ---- query Morton keys -----------------------------------------------------------------------
+// ---- query sort keys -------------------------------------------------------------------------
 __device__ __forceinline__ unsigned spread3q(unsigned x) {
     x &= 0x3ffu;
     x = (x | (x << 16)) & 0x030000ffu;
@@ -638,22 +638,57 @@ __device__ __forceinline__ unsigned spread3q(unsigned x) {
     return x;
 }
 
+// 30-bit index of a cell of a 1024^3 grid along the 3-D Hilbert curve: Skilling's transpose
+// algorithm ("Programming the Hilbert curve", AIP Conf. Proc. 707, 2004) undoes the excess work
+// per bit plane, Gray-encodes the transposed coordinates, and interleaves their bits. Sorting
+// the query points by it gives warps more compact groups than Morton order (no long jumps).
+__device__ __forceinline__ unsigned hilbert3(unsigned x, unsigned y, unsigned z) {
+    unsigned X[3] = {x, y, z};
+    constexpr unsigned kTop = 1u << 9;
+    for (unsigned q = kTop; q > 1; q >>= 1) {
+        const unsigned p = q - 1;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            if (X[i] & q) {
+                X[0] ^= p;  // invert the low bits of the first axis
+            } else {
+                const unsigned t = (X[0] ^ X[i]) & p;  // exchange the low bits with axis i
+                X[0] ^= t;
+                X[i] ^= t;
+            }
+        }
+    }
+    X[1] ^= X[0];
+    X[2] ^= X[1];
+    unsigned t = 0;
+    for (unsigned q = kTop; q > 1; q >>= 1)
+        if (X[2] & q) t ^= q - 1;
+    X[0] ^= t;
+    X[1] ^= t;
+    X[2] ^= t;
+    return (spread3q(X[0]) << 2) | (spread3q(X[1]) << 1) | spread3q(X[2]);
+}
+
+// Sort key of a query point in its mesh's frame (the mesh bbox grown by 25% per side, 1024
+// cells per axis; NaN coordinates fall in cell 0).
+__device__ __forceinline__ unsigned query_key(const MeshInfo& mi, const float* q) {
+    unsigned c[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float ext = mi.hi[a] - mi.lo[a];
+        const float lo = mi.lo[a] - 0.25f * ext;
+        const float inv = ext > 0.f ? 1.0f / (1.5f * ext) : 0.f;
+        const float u = (q[a] - lo) * inv * 1024.0f;
+        c[a] = (unsigned)(u >= 0.f ? (int)fminf(u, 1023.0f) : 0);
+    }
+    return hilbert3(c[0], c[1], c[2]);
+}
+
 __global__ void k_query_keys(const float* __restrict__ Q, int64_t n, const MeshInfo mi,
                              uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    unsigned code = 0;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        // frame: mesh bbox grown by 25% per side
-        const float ext = mi.hi[a] - mi.lo[a];
-        const float lo = mi.lo[a] - 0.25f * ext;
-        const float inv = ext > 0.f ? 1.0f / (1.5f * ext) : 0.f;
-        const float u = (Q[3 * k + a] - lo) * inv * 1024.0f;
-        const int qv = u >= 0.f ? (int)fminf(u, 1023.0f) : 0;  // NaN -> 0
-        code |= spread3q((unsigned)qv) << (2 - a);
-    }
-    keys[k] = code;
+    keys[k] = query_key(mi, Q + 3 * k);
     vals[k] = (uint32_t)k;
 }
 
@@ -668,18 +703,7 @@ __global__ void k_forest_keys(const float* __restrict__ Q, int64_t n,
         const int mid = (lo + hi + 1) >> 1;
         if (qoff[mid] <= k) lo = mid; else hi = mid - 1;
     }
-    const MeshInfo& mi = meshes[lo];
-    unsigned code = 0;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        const float ext = mi.hi[a] - mi.lo[a];
-        const float l0 = mi.lo[a] - 0.25f * ext;
-        const float inv = ext > 0.f ? 1.0f / (1.5f * ext) : 0.f;
-        const float u = (Q[3 * k + a] - l0) * inv * 1024.0f;
-        const int qv = u >= 0.f ? (int)fminf(u, 1023.0f) : 0;
-        code |= spread3q((unsigned)qv) << (2 - a);
-    }
-    keys[k] = ((uint64_t)lo << 30) | code;
+    keys[k] = ((uint64_t)lo << 30) | query_key(meshes[lo], Q + 3 * k);
     vals[k] = (uint32_t)k;
 }
 

@@ -328,3 +328,21 @@ def test_graph_capture_replay(torch_cuda):
         torch.cuda.synchronize()
         assert torch.equal(w, ref_w) and torch.equal(i, ref_i)
         assert torch.equal(fw, ref_fw) and torch.equal(fi, ref_fi)
+
+
+def test_query_order_is_a_hilbert_curve(torch_cuda):
+    """The query sort key is a Hilbert index: points at the centres of an aligned 16^3 block of
+    sort cells come out as a path whose consecutive cells are face neighbours (a Morton order
+    would jump)."""
+    torch = torch_cuda
+    V = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 1, 1]], np.float32)
+    F = np.array([[0, 2, 1], [0, 1, 3], [0, 3, 2], [1, 2, 4]], np.int32)  # bbox [0, 1]^3
+    eng = fwn.FastWindingNumber(V, F)
+    # the sort frame is the bbox grown by 25% per side, 1024 cells per axis
+    cell = 1.5 / 1024
+    idx = np.stack(np.meshgrid(*[np.arange(16)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    pts = (-0.25 + (idx + 0.5) * cell).astype(np.float32)
+    order = eng.query_order(torch.from_numpy(pts).cuda()).cpu().numpy()
+    path = idx[order]
+    steps = np.abs(np.diff(path, axis=0)).sum(1)
+    assert np.all(steps == 1)
