@@ -114,6 +114,16 @@ def max_over_ranks(dist, x: float, device=None) -> float:
     return float(t.item())
 
 
+def rank0_choice(dist, values, device=None):
+    """Every rank runs rank 0's tuning choice (ints), so all ranks time the same configuration."""
+    if dist is None:
+        return list(values)
+    import torch
+    t = torch.tensor([int(v) for v in values], dtype=torch.int64, device=device)
+    dist.broadcast(t, src=0)
+    return [int(v) for v in t.tolist()]
+
+
 def rank_queries(Q, near_mask, rank: int):
     """The query set a rank answers (weak scaling: every rank has a full-size set). Rank 0 uses
     the workload as generated; rank r > 0 a seeded shuffle of it (different points per warp,
@@ -312,6 +322,7 @@ def run_ours(args, rank, world, local):
     leaf, block, tuning, tuned = args.leaf, args.block, 0, None
     if leaf == 0:  # the autotuner's choice for this mesh and query distribution (untimed)
         leaf, trav, block, tuning, tuned = autotune_choice(fwn, Vd, Fd, Qd)
+        leaf, trav, block, tuning = rank0_choice(dist, (leaf, trav, block, tuning), dev)
     args.leaf, args.block = leaf, block
     # the handle's defaults are the chosen schedule too, so the host-buffer path (e2e) runs it
     eng = fwn.FastWindingNumber(Vd, Fd, leaf_size=args.leaf, traversal=trav, block_size=block,
@@ -617,7 +628,7 @@ def run_forest(args, rank, world, local):
     tuned, tuning = None, 0
     if args.leaf == 0:  # leaf size picked by the forest autotuner on this forest (untimed)
         r = fwn.autotune_forest(Vd, fo.voff, Fd, fo.foff, Qd, fo.qoff)
-        args.leaf, tuning = r["leaf_size"], r["tuning"]
+        args.leaf, tuning = rank0_choice(dist, (r["leaf_size"], r["tuning"]), dev)
         tuned = {"leaf_size": r["leaf_size"], "tuning": r["tuning"],
                  "forest_query_ms": r["ms"], "candidates": r["candidates"]}
     builds = []

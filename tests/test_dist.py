@@ -32,8 +32,9 @@ def _worker(rank, world, port, outdir):
     near = np.arange(64) % 2 == 0
     q, m = bench.rank_queries(Q, near, rank)
     t = bench.max_over_ranks(dist, 0.5 + rank)  # this rank's "step time"
+    choice = bench.rank0_choice(dist, (8 + 4 * rank, 2, 128, rank))  # each rank "tuned" its own
     bench.barrier(dist)
-    res = {"max_t": t, "sum": float(q.sum()), "first": q[0].tolist(),
+    res = {"max_t": t, "choice": choice, "sum": float(q.sum()), "first": q[0].tolist(),
            "near_ok": bool(np.all(m == (q[:, 0] % 6 == 0))),
            "value": bench.job_value(len(q), world, t)}
     (Path(outdir) / f"r{rank}.json").write_text(json.dumps(res))
@@ -48,6 +49,8 @@ def test_two_gloo_ranks(tmp_path):
     r = [json.loads((tmp_path / f"r{i}.json").read_text()) for i in range(world)]
     # max over ranks reaches every rank
     assert r[0]["max_t"] == r[1]["max_t"] == 1.5
+    # every rank runs rank 0's tuning choice
+    assert r[0]["choice"] == r[1]["choice"] == [8, 2, 128, 0]
     # each rank holds a full query set of the same points (weak scaling), in its own order
     assert r[0]["sum"] == r[1]["sum"]
     assert r[0]["first"] != r[1]["first"]
