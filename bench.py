@@ -80,6 +80,7 @@ def parse():
     p.add_argument("--no-fp64", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-clocks", action="store_true")
+    p.add_argument("--no-graph", action="store_true")  # time plain launches instead of a graph
     return p.parse_args()
 
 
@@ -344,14 +345,29 @@ def run_ours(args, rank, world, local):
                      tuning=tuning)
     sptr = C.c_void_p(stream.cuda_stream)
 
-    def query_mixed():
+    def query_mixed(s=None):
         fwn._check(L.fwn_query_ex(eng.handle, C.byref(opts), C.c_void_p(Qd.data_ptr()), n,
                                   C.c_void_p(w_out.data_ptr()), C.c_void_p(i_out.data_ptr()),
-                                  None, None, sptr))
+                                  None, None, sptr if s is None else C.c_void_p(s.cuda_stream)))
 
     for _ in range(args.warmup):
         query_mixed()
     torch.cuda.synchronize()
+    step = query_mixed
+    if not args.no_graph:
+        # the timed step replays a CUDA graph of one query call (the same keys, sort and
+        # traversal launches, without the host's launch overhead)
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(stream)
+        with torch.cuda.stream(side):
+            query_mixed(side)
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            query_mixed(torch.cuda.current_stream(dev))
+        graph.replay()
+        torch.cuda.synchronize()
+        step = graph.replay
     # work counters (untimed)
     _, _, stats = eng.query(Qd, traversal=trav, block_size=args.block, stats=True)
     torch.cuda.synchronize()
@@ -365,7 +381,7 @@ def run_ours(args, rank, world, local):
         for k in range(args.steps):
             flush.zero_()  # L2 flush between timed steps (not inside the events)
             ev[k][0].record(stream)
-            query_mixed()
+            step()
             ev[k][1].record(stream)
         torch.cuda.synchronize()
         t_wall = time.perf_counter() - t_wall
@@ -385,6 +401,7 @@ def run_ours(args, rank, world, local):
                    "beta": wl.beta, "leaf_size": args.leaf,
                    "traversal": "warp" if trav == fwn.TRAVERSAL_WARP else "thread",
                    "block": args.block, "tuning": tuning, "autotuned": tuned,
+                   "step": "plain launches" if args.no_graph else "CUDA graph of one query call",
                    "l2": "flushed before every step (256 MB write)",
                    "parallelism": f"replicas x{world} (query shards, no collective)"},
         "build_ms": min(build_ms), "tree": {"nodes": info["num_nodes"], "leaves": info["num_leaves"],

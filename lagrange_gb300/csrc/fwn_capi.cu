@@ -116,6 +116,25 @@ struct OwnedStream {
     }
 };
 
+// The stream of the synchronous host-buffer queries: one non-blocking stream per (host thread,
+// device), created on first use and kept for the thread's lifetime; creating and destroying a
+// stream on every call costs more than a small query.
+cudaStream_t host_stream() {
+    struct Streams {
+        cudaStream_t s[kMaxDevices] = {};
+        ~Streams() {
+            for (cudaStream_t x : s)
+                if (x) cudaStreamDestroy(x);
+        }
+    };
+    thread_local Streams t;
+    int dev = 0;
+    FWN_CUDA_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) throw Error(FWN_INTERNAL, "device ordinal out of range");
+    if (!t.s[dev]) FWN_CUDA_CHECK(cudaStreamCreateWithFlags(&t.s[dev], cudaStreamNonBlocking));
+    return t.s[dev];
+}
+
 Engine* engine_of(fwn_handle h) {
     if (!h) throw Error(FWN_NOT_BUILT, "null handle (default-constructed or moved-from engine)");
     return reinterpret_cast<Engine*>(h);
@@ -278,16 +297,16 @@ FWN_API fwn_status fwn_query_host(fwn_handle h, const float* points, int64_t n, 
         if (e->nmeshes != 1) throw Error(FWN_INVALID_ARG, "forest handle: use fwn_forest_query");
         if (n == 0) return;
         QueryArgs a = resolve_query_args(*e, nullptr);
-        OwnedStream os;
-        Scratch dq(n * 3 * sizeof(float), os.s);
-        Scratch dw(omega ? n * sizeof(float) : 0, os.s);
-        Scratch di(inside ? n * sizeof(uint8_t) : 0, os.s);
-        FWN_CUDA_CHECK(cudaMemcpyAsync(dq.p, points, n * 3 * sizeof(float), cudaMemcpyHostToDevice, os.s));
+        const cudaStream_t st = host_stream();
+        Scratch dq(n * 3 * sizeof(float), st);
+        Scratch dw(omega ? n * sizeof(float) : 0, st);
+        Scratch di(inside ? n * sizeof(uint8_t) : 0, st);
+        FWN_CUDA_CHECK(cudaMemcpyAsync(dq.p, points, n * 3 * sizeof(float), cudaMemcpyHostToDevice, st));
         query_mesh(*e, 0, a, dq.as<float>(), n, dw.as<float>(), di.as<uint8_t>(), nullptr, nullptr,
-                   os.s, /*check=*/true);
-        if (omega) FWN_CUDA_CHECK(cudaMemcpyAsync(omega, dw.p, n * sizeof(float), cudaMemcpyDeviceToHost, os.s));
-        if (inside) FWN_CUDA_CHECK(cudaMemcpyAsync(inside, di.p, n, cudaMemcpyDeviceToHost, os.s));
-        FWN_CUDA_CHECK(cudaStreamSynchronize(os.s));
+                   st, /*check=*/true);
+        if (omega) FWN_CUDA_CHECK(cudaMemcpyAsync(omega, dw.p, n * sizeof(float), cudaMemcpyDeviceToHost, st));
+        if (inside) FWN_CUDA_CHECK(cudaMemcpyAsync(inside, di.p, n, cudaMemcpyDeviceToHost, st));
+        FWN_CUDA_CHECK(cudaStreamSynchronize(st));
     });
 }
 
