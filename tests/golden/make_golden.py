@@ -13,6 +13,9 @@ are produced by the oracle and by closed-form solid angles:
                       and the reference-restatement is_inside (O2).
 * ``displaced.npz``   displaced icosphere frequency 24 (11,520 triangles, seed 1) with 1,024
                       box and 1,024 near-surface queries and their O1 solid angles.
+* ``soup.npz``        the defective soup at frequency 20 (10% of the faces deleted, 1% flipped,
+                      0.5% duplicated with 1e-7 jitter), 1,024 box and 1,024 near-surface
+                      (within 1e-4) queries: O1, O3 at beta=2 leaf 8, and O2's is_inside.
 """
 from __future__ import annotations
 
@@ -74,6 +77,12 @@ def main():
     o1 = oracle.brute_f64(d.V, d.F, d.Q)
     np.savez_compressed(HERE / "displaced.npz", V=d.V, F=d.F, Q=d.Q, near=d.near_mask,
                         omega_exact=o1)
+    sp = W.defective_soup_workload(nu=20, n_queries=2048)
+    o1 = oracle.brute_f64(sp.V, sp.F, sp.Q)
+    o3 = oracle.LbvhTree(sp.V, sp.F, leaf_size=8).query_f64(sp.Q, beta=2.0)
+    _, ins = oracle.RefTree(sp.V, sp.F, 8).query(sp.Q, beta=2.0)
+    np.savez_compressed(HERE / "soup.npz", V=sp.V, F=sp.F, Q=sp.Q, near=sp.near_mask,
+                        omega_exact=o1, omega_lbvh_beta2=o3, inside_ref=ins)
     for p in sorted(HERE.glob("*.npz")):
         print(p.name, p.stat().st_size)
 

@@ -95,6 +95,24 @@ def test_displaced_near_surface(torch_cuda, oracle_mod, leaf):
     np.testing.assert_array_equal(ins[band].astype(bool), we[band] > 0.5)
 
 
+def test_golden_soup(torch_cuda, oracle_mod):
+    """The defective soup (holes, flips, 1e-7-jittered duplicates; near-surface queries within
+    1e-4): FP64 form vs the restated build's FP64 traversal, mixed vs FP64 form, beta -> infinity
+    vs the brute force, and is_inside vs the FP64 form outside the band."""
+    g = np.load(GOLDEN / "soup.npz")
+    eng = _engine(g["V"], g["F"], leaf_size=8)
+    w_mix, ins = _q(eng, torch_cuda, g["Q"])
+    _, _, w64 = _q(eng, torch_cuda, g["Q"], precision=fwn.PRECISION_FP64, omega_f64=True)
+    np.testing.assert_allclose(w64, g["omega_lbvh_beta2"], rtol=0, atol=1e-10 * FOUR_PI)
+    assert np.max(np.abs(w_mix - w64)) / FOUR_PI <= 2e-6
+    band = np.abs(w64 / FOUR_PI - 0.5) > 1e-3
+    np.testing.assert_array_equal(ins[band].astype(bool), (w64 / FOUR_PI)[band] > 0.5)
+    _, _, x64 = _q(eng, torch_cuda, g["Q"], precision=fwn.PRECISION_FP64, omega_f64=True, beta=1e30)
+    np.testing.assert_allclose(x64, g["omega_exact"], rtol=0, atol=1e-10 * FOUR_PI)
+    xm, _ = _q(eng, torch_cuda, g["Q"], beta=1e30)
+    assert np.max(np.abs(xm - g["omega_exact"])) / FOUR_PI <= 1e-5
+
+
 def test_schedules_and_sorting(torch_cuda):
     """Every schedule computes the same terms; only the Kahan summation order may differ (both
     schedules defer work in warp-dependent batches, so the Morton sort changes the order; the

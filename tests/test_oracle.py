@@ -77,6 +77,23 @@ def test_golden_uv_sphere_regression(oracle_mod):
     np.testing.assert_allclose(w[off], (r[off] < 1).astype(float), atol=1e-9)
 
 
+def test_golden_soup_regression(oracle_mod):
+    """The defective soup (holes, flipped and jittered duplicate faces): the generator is
+    bit-stable and O1 / O3 reproduce the committed values; O3 at beta=2 stays within the
+    truncation bound of O1, and the holes make the exact winding numbers fractional."""
+    g = np.load(GOLDEN / "soup.npz")
+    sp = W.defective_soup_workload(nu=20, n_queries=2048)
+    for k in ("V", "F", "Q"):
+        np.testing.assert_array_equal(g[k], getattr(sp, k))
+    o1 = oracle_mod.brute_f64(g["V"], g["F"], g["Q"])
+    np.testing.assert_allclose(o1, g["omega_exact"], rtol=0, atol=1e-12)
+    o3 = oracle_mod.LbvhTree(g["V"], g["F"], leaf_size=8).query_f64(g["Q"], beta=2.0)
+    np.testing.assert_allclose(o3, g["omega_lbvh_beta2"], rtol=0, atol=1e-12)
+    assert np.max(np.abs(o3 - o1)) / FOUR_PI < 2e-2
+    w = o1 / FOUR_PI
+    assert np.sum((w > 0.05) & (w < 0.95)) > 10  # fractional winding numbers exist
+
+
 def test_restated_reference_tree_accuracy(oracle_mod):
     """O2 (float Barill tree, beta=2) against the FP64 brute force, and its is_inside."""
     g = np.load(GOLDEN / "uv_sphere.npz")
