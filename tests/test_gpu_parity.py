@@ -393,3 +393,30 @@ def test_scale_and_translation(torch_cuda, scale, shift):
     # truncation differs by up to ~5e-3 in w; the side of the surface does not
     clear = np.abs(b64 / FOUR_PI - 0.5) > 0.05
     np.testing.assert_array_equal(ins[clear].astype(bool), (b64 / FOUR_PI)[clear] > 0.5)
+
+
+def test_non_finite_queries(torch_cuda):
+    """NaN / inf query points do not disturb the other points of the batch or the call: a NaN
+    point fails every far test, walks the whole tree and returns NaN (inside 0); the finite
+    points return what they return alone, with either schedule."""
+    torch = torch_cuda
+    V, F = W.icosphere(8)
+    eng = _engine(V.astype(np.float32), F)
+    Q = np.random.default_rng(2).uniform(-1.5, 1.5, (256, 3)).astype(np.float32)
+    bad = Q.copy()
+    bad[::7, 0] = np.nan
+    bad[3::11, 1] = np.inf
+    bad[5::13, 2] = -np.inf
+    nonfin = ~np.isfinite(bad).all(1)
+    for trav in (fwn.TRAVERSAL_WARP, fwn.TRAVERSAL_THREAD):
+        ref, iref = _q(eng, torch, Q, traversal=trav, sort_queries=0)
+        w, ins = _q(eng, torch, bad, traversal=trav, sort_queries=0)
+        if trav == fwn.TRAVERSAL_WARP:  # a lane's path and sum order ignore its neighbours
+            np.testing.assert_array_equal(w[~nonfin], ref[~nonfin])
+        else:  # the thread schedule batches leaves across lanes: only the sum order may move
+            np.testing.assert_allclose(w[~nonfin], ref[~nonfin], rtol=0, atol=1e-5)
+        clear = ~nonfin & (np.abs(ref / FOUR_PI - 0.5) > 1e-3)
+        np.testing.assert_array_equal(ins[clear], iref[clear])
+        assert np.all(ins[np.isnan(w)] == 0)
+    w, ins = _q(eng, torch, bad)  # sorted: NaN keys fall in one cell, no error
+    assert np.all(np.isfinite(w[~nonfin]))
