@@ -83,8 +83,10 @@ typedef struct fwn_config {
     float fp64_cond;       /* ... and its FP32 evaluation is ill-conditioned: |a||b||c| >
                               fp64_cond * |(det, D)|, or det is within rounding of 0 with D <= 0.
                               0 = every triangle within the distance. Default 4 */
-    int32_t tuning;        /* schedule variant (0 = default; set by fwn_autotune). Warp schedule:
-                              register cap 64 (0), 72 (1) or none (2) */
+    int32_t tuning;        /* warp-schedule variant (set by fwn_autotune): queries per lane and
+                              register cap. 1: 1 query per lane, 72 registers; 2: 1, no cap;
+                              3: 1, 64 registers; 4: 2 queries per lane, 64 registers; 5: 2, 80.
+                              0 (default): 4 for batches that fill the GPU, else 3 */
     int32_t reserved[6];
 } fwn_config;
 
@@ -217,8 +219,8 @@ FWN_API fwn_status fwn_export_moments(fwn_handle h, double* moments);
 
 /* Autotuner (no reference counterpart: the reference has no tunable parameters). For one mesh
  * (DEVICE arrays) and a representative DEVICE sample of query points, builds the tree for leaf
- * sizes 4, 8, 12 and 16 and times every query schedule (warp cursor with a 64- or 72-register cap
- * or none; thread per query with blocks of 64/128/256) with CUDA events; returns the fastest. Apply it
+ * sizes 4, 8, 12 and 16 and times every query schedule (the warp cursor's variants 1-5; thread per
+ * query with blocks of 64/128/256) with CUDA events; returns the fastest. Apply it
  * with cfg.leaf_size, cfg.traversal, cfg.block_size, cfg.tuning. `base` gives beta and the
  * precision knobs (NULL = defaults). cache_path (may be NULL) names a text file keyed by GPU name
  * and log2 of the triangle and query counts: a hit returns without timing, a miss appends.
@@ -231,7 +233,7 @@ FWN_API fwn_status fwn_autotune(const float* d_vertices, int64_t num_vertices,
 /* Forest autotuner (no reference counterpart). The mixed forest query is one persistent kernel,
  * so its knobs are the leaf size and the register cap: builds the forest (DEVICE vertex/triangle
  * arrays, HOST offset arrays as in fwn_forest_build_device) for leaf sizes 4, 8, 12 and 16 and
- * times the forest query with tuning 0 and 1 on the DEVICE points with HOST query_offsets
+ * times the forest query with tuning 3, 1, 4 and 5 on the DEVICE points with HOST query_offsets
  * [num_meshes + 1]. Returns the fastest (leaf size, tuning; traversal WARP, block 128). Cache as
  * in fwn_autotune, keyed also by log2 of the mesh count. Synchronous on `stream`. */
 FWN_API fwn_status fwn_forest_autotune(const float* d_vertices, const int64_t* vertex_offsets,

@@ -27,9 +27,11 @@ struct Candidate {
 };
 
 const Candidate kCandidates[] = {
-    {FWN_TRAVERSAL_WARP, 128, 0},    // warp cursor, 64-register cap
-    {FWN_TRAVERSAL_WARP, 128, 1},    // warp cursor, 72-register cap
-    {FWN_TRAVERSAL_WARP, 128, 2},    // warp cursor, no register cap
+    {FWN_TRAVERSAL_WARP, 128, 3},    // warp cursor, 1 query per lane, 64-register cap
+    {FWN_TRAVERSAL_WARP, 128, 1},    // 1 query per lane, 72-register cap
+    {FWN_TRAVERSAL_WARP, 128, 2},    // 1 query per lane, no register cap
+    {FWN_TRAVERSAL_WARP, 128, 4},    // 2 queries per lane, 64-register cap
+    {FWN_TRAVERSAL_WARP, 128, 5},    // 2 queries per lane, 80-register cap
     {FWN_TRAVERSAL_THREAD, 64, 0},   // thread per query
     {FWN_TRAVERSAL_THREAD, 128, 0},
     {FWN_TRAVERSAL_THREAD, 256, 0},
@@ -175,8 +177,9 @@ extern "C" FWN_API fwn_status fwn_autotune(const float* d_V, int64_t nv, const i
 }
 
 // Forest form: the mixed forest query is one persistent kernel, so its knobs are the leaf size
-// and the register cap. Each leaf size builds the whole forest; each (leaf, cap) pair times the
-// forest query on the caller's queries (median of three after a warm-up).
+// and the warp-schedule variant (queries per lane, register cap). Each leaf size builds the whole
+// forest; each (leaf, variant) pair times the forest query on the caller's queries (median of
+// three after a warm-up).
 extern "C" FWN_API fwn_status fwn_forest_autotune(const float* d_V, const int64_t* vertex_offsets,
                                                   const int32_t* d_F,
                                                   const int64_t* triangle_offsets,
@@ -225,7 +228,7 @@ extern "C" FWN_API fwn_status fwn_forest_autotune(const float* d_V, const int64_
             e.cfg.leaf_size = leaf;
             FWN_CUDA_CHECK(cudaGetDevice(&e.device));
             build_forest(e, d_V, vertex_offsets, d_F, triangle_offsets, num_meshes, st);
-            for (int tuning = 0; tuning <= 1; ++tuning) {  // 64- and 72-register caps
+            for (int tuning : {3, 1, 4, 5}) {  // warp-schedule variants (queries per lane, cap)
                 QueryArgs a = resolve_query_args(e, nullptr);
                 a.precision = FWN_PRECISION_MIXED;
                 a.tuning = tuning;

@@ -371,22 +371,37 @@ constexpr int WARP_LEAF_MAX = 16;
 constexpr int WARP_BLOCK = 128;
 constexpr int DONE = INT_MAX;
 
-struct WarpSmem {
-    float4 leaf[WARP_LEAF_MAX * 3];
-    float4 q[32];
-    float res[32 * WARP_LEAF_MAX];
+// Per-lane state of one query slot. A lane holds QPL queries; slot j of lane l is query
+// j * 32 + l of the warp's group of 32 * QPL.
+struct Slot {
+    float qx, qy, qz;
+    float tau;   // FP64 near-field radius of the query's mesh
+    float s, c;  // Kahan sum
+    int resume;  // next node this query visits (DONE when finished)
+    int end;     // escape index of the query's mesh subtree
 };
 
-template <bool STATS>
+template <int QPL>
+struct WarpSmem {
+    float4 leaf[WARP_LEAF_MAX * 3];
+    float4 q[32 * QPL];  // (x, y, z, tau) of the queries that need the current leaf
+    float res[32 * QPL * WARP_LEAF_MAX];
+};
+
+template <bool STATS, int QPL>
 __device__ __forceinline__ void warp_walk(const NodeF32* __restrict__ nodes,
-                                          const TriF32* __restrict__ tris, int root, int lane_end,
-                                          float tau, float cond, float qx, float qy, float qz,
-                                          float beta, WarpSmem& sm, float& s, float& c,
+                                          const TriF32* __restrict__ tris, Slot (&sl)[QPL],
+                                          float cond, float beta, WarpSmem<QPL>& sm,
                                           QCounters& qc, unsigned* __restrict__ status) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = lanemask_lt();
-    int resume = root < lane_end ? root : DONE;
-    int cursor = __reduce_min_sync(0xffffffffu, resume);
+    int lo = DONE;
+#pragma unroll
+    for (int j = 0; j < QPL; ++j) {
+        if (sl[j].resume >= sl[j].end) sl[j].resume = DONE;
+        lo = min(lo, sl[j].resume);
+    }
+    int cursor = __reduce_min_sync(0xffffffffu, lo);
     float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
     int4 b = make_int4(0, 0, 0, 0);
     if (cursor != DONE) load_sector0(nodes + cursor, a, b);
@@ -396,36 +411,57 @@ __device__ __forceinline__ void warp_walk(const NodeF32* __restrict__ nodes,
         ld_v8(&nd->m0, m0, m1);
         ld_v8(&nd->m2, m2, m3);
         ld_v8(&nd->m4, m4, m5);
-        // far test on every lane (only lanes whose resume index is the cursor use the result),
-        // with no divergent branch around it and the resume update as selects
-        const bool active = resume == cursor;
-        float dx, dy, dz, d2;
-        const bool far = far_pred(a.x, a.y, a.z, a.w, qx, qy, qz, beta, dx, dy, dz, d2);
-        if (STATS && active) ++qc.nodes;
+        // far test of every slot on every lane (only slots whose resume index is the cursor use
+        // the result), with no divergent branch around it and the resume update as selects
         const bool leafnode = b.z > 0;
-        int nr = (far || leafnode) ? b.x : cursor + 1;
-        nr = nr >= lane_end ? DONE : nr;
-        resume = active ? nr : resume;
-        const bool do_far = active && far;
-        const bool need_leaf = active && !far && leafnode;
-        const int nc = __reduce_min_sync(0xffffffffu, resume);
+        bool do_far[QPL], need_leaf[QPL];
+        float dx[QPL], dy[QPL], dz[QPL], d2[QPL];
+        int lo2 = DONE;
+#pragma unroll
+        for (int j = 0; j < QPL; ++j) {
+            const bool active = sl[j].resume == cursor;
+            const bool far = far_pred(a.x, a.y, a.z, a.w, sl[j].qx, sl[j].qy, sl[j].qz, beta, dx[j],
+                                      dy[j], dz[j], d2[j]);
+            if (STATS && active) ++qc.nodes;
+            int nr = (far || leafnode) ? b.x : cursor + 1;
+            nr = nr >= sl[j].end ? DONE : nr;
+            sl[j].resume = active ? nr : sl[j].resume;
+            do_far[j] = active && far;
+            need_leaf[j] = active && !far && leafnode;
+            lo2 = min(lo2, sl[j].resume);
+        }
+        const int nc = __reduce_min_sync(0xffffffffu, lo2);
         float4 an = a;
         int4 bn = b;
         if (nc != DONE) load_sector0(nodes + nc, an, bn);  // next step's test sector, in flight
-        if (__any_sync(0xffffffffu, do_far)) {  // warp-uniform: every lane evaluates, far lanes add
-            const float t = taylor_f32(m0, m1, m2, m3, m4, m5, dx, dy, dz, d2, __int_as_float(b.w));
-            if (do_far) {
-                kahan_add(s, c, t);
-                if (STATS) ++qc.far;
+#pragma unroll
+        for (int j = 0; j < QPL; ++j) {
+            if (__any_sync(0xffffffffu, do_far[j])) {  // warp-uniform: all lanes evaluate
+                const float t = taylor_f32(m0, m1, m2, m3, m4, m5, dx[j], dy[j], dz[j], d2[j],
+                                           __int_as_float(b.w));
+                if (do_far[j]) {
+                    kahan_add(sl[j].s, sl[j].c, t);
+                    if (STATS) ++qc.far;
+                }
             }
         }
-        const unsigned lm = __ballot_sync(0xffffffffu, need_leaf);
-        if (lm) {
+        unsigned lm[QPL];
+        int off[QPL];
+        int nl = 0;
+#pragma unroll
+        for (int j = 0; j < QPL; ++j) {
+            lm[j] = __ballot_sync(0xffffffffu, need_leaf[j]);
+            off[j] = nl;
+            nl += __popc(lm[j]);
+        }
+        if (nl) {
             const int cnt = b.z;  // warp-uniform (same node for all lanes), <= WARP_LEAF_MAX
-            const int nl = __popc(lm);
             const float4* src = reinterpret_cast<const float4*>(tris + b.y);
-            for (int j = lane; j < 3 * cnt; j += 32) sm.leaf[j] = __ldg(src + j);
-            if (need_leaf) sm.q[__popc(lm & lt)] = make_float4(qx, qy, qz, 0.f);
+            for (int i = lane; i < 3 * cnt; i += 32) sm.leaf[i] = __ldg(src + i);
+#pragma unroll
+            for (int j = 0; j < QPL; ++j)
+                if (need_leaf[j])
+                    sm.q[off[j] + __popc(lm[j] & lt)] = make_float4(sl[j].qx, sl[j].qy, sl[j].qz, sl[j].tau);
             __syncwarp();
             const int np = nl * cnt;
             const float inv = 1.0f / (float)cnt;
@@ -438,14 +474,17 @@ __device__ __forceinline__ void warp_walk(const NodeF32* __restrict__ nodes,
                     const float4 t0 = sm.leaf[3 * t], t1 = sm.leaf[3 * t + 1], t2 = sm.leaf[3 * t + 2];
                     sm.res[p] = tri_omega_mixed<STATS>(t0.x, t0.y, t0.z, t0.w, t1.x, t1.y, t1.z,
                                                        t1.w, t2.x, t2.y, t2.z, qq.x, qq.y, qq.z,
-                                                       tau, cond, qc);
+                                                       qq.w, cond, qc);
                 }
             }
             __syncwarp();
-            if (need_leaf) {
-                const int r = __popc(lm & lt);
-                for (int t = 0; t < cnt; ++t) kahan_add(s, c, sm.res[r * cnt + t]);
-                if (STATS) qc.tri += cnt;
+#pragma unroll
+            for (int j = 0; j < QPL; ++j) {
+                if (need_leaf[j]) {
+                    const int r = off[j] + __popc(lm[j] & lt);
+                    for (int t = 0; t < cnt; ++t) kahan_add(sl[j].s, sl[j].c, sm.res[r * cnt + t]);
+                    if (STATS) qc.tri += cnt;
+                }
             }
             __syncwarp();
         }
@@ -460,34 +499,44 @@ __device__ __forceinline__ void warp_walk(const NodeF32* __restrict__ nodes,
     }
 }
 
-template <bool STATS, int MINB>
+__device__ __forceinline__ void write_result(const Slot& s, int64_t qi, float* __restrict__ omega,
+                                             uint8_t* __restrict__ inside) {
+    const float res = s.s - s.c;
+    if (omega) omega[qi] = res;
+    if (inside) inside[qi] = (double)res > TWO_PI_D ? 1 : 0;
+}
+
+// One mesh: each warp takes the next 32 * QPL queries of the (sorted) order.
+template <bool STATS, int MINB, int QPL>
 __global__ void __launch_bounds__(WARP_BLOCK, MINB)
 k_query_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
              const MeshInfo mi, const float* __restrict__ Q, const uint32_t* __restrict__ order,
              int64_t n, float beta, float* __restrict__ omega, uint8_t* __restrict__ inside,
              unsigned* __restrict__ status, unsigned long long* __restrict__ stats) {
-    __shared__ WarpSmem smem[WARP_BLOCK / 32];
+    __shared__ WarpSmem<QPL> smem[WARP_BLOCK / 32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k - lane >= n) return;  // whole warp out of range (warp-uniform)
-    const bool valid = k < n;
+    const int64_t base = ((int64_t)blockIdx.x * (WARP_BLOCK / 32) + w) * (32 * QPL);
+    if (base >= n) return;  // whole warp out of range (warp-uniform)
     QCounters qc;
-    float qx = 0.f, qy = 0.f, qz = 0.f;
-    int64_t qi = 0;
-    if (valid) {
-        qi = order ? (int64_t)order[k] : k;
-        qx = Q[3 * qi];
-        qy = Q[3 * qi + 1];
-        qz = Q[3 * qi + 2];
+    Slot sl[QPL];
+    int64_t qi[QPL];
+#pragma unroll
+    for (int j = 0; j < QPL; ++j) {
+        const int64_t k = base + 32 * j + lane;
+        const bool valid = k < n;
+        qi[j] = valid ? (order ? (int64_t)order[k] : k) : -1;
+        sl[j].qx = valid ? Q[3 * qi[j]] : 0.f;
+        sl[j].qy = valid ? Q[3 * qi[j] + 1] : 0.f;
+        sl[j].qz = valid ? Q[3 * qi[j] + 2] : 0.f;
+        sl[j].tau = mi.tau;
+        sl[j].s = sl[j].c = 0.f;
+        sl[j].resume = valid ? mi.root : DONE;
+        sl[j].end = mi.end;
     }
-    float s = 0.f, c = 0.f;
-    warp_walk<STATS>(nodes, tris, valid ? mi.root : DONE, mi.end, mi.tau, mi.cond, qx, qy, qz,
-                     beta, smem[w], s, c, qc, status);
-    if (valid) {
-        const float res = s - c;
-        if (omega) omega[qi] = res;
-        if (inside) inside[qi] = (double)res > TWO_PI_D ? 1 : 0;
-    }
+    warp_walk<STATS, QPL>(nodes, tris, sl, mi.cond, beta, smem[w], qc, status);
+#pragma unroll
+    for (int j = 0; j < QPL; ++j)
+        if (qi[j] >= 0) write_result(sl[j], qi[j], omega, inside);
     if (STATS) flush_stats(qc, stats);
 }
 
@@ -501,71 +550,71 @@ k_query_grid(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
              int64_t nx, int64_t ny, int64_t nz, int64_t bx, int64_t by, int64_t nbricks,
              float beta, float* __restrict__ omega, uint8_t* __restrict__ inside,
              unsigned* __restrict__ status) {
-    __shared__ WarpSmem smem[WARP_BLOCK / 32];
+    __shared__ WarpSmem<1> smem[WARP_BLOCK / 32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t brick = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (brick >= nbricks) return;  // warp-uniform
     const int64_t bi = brick % bx, bj = (brick / bx) % by, bk = brick / (bx * by);
     const int64_t i = bi * 4 + (lane & 3), j = bj * 4 + ((lane >> 2) & 3), k = bk * 2 + (lane >> 4);
     const bool valid = i < nx && j < ny && k < nz;
-    const float qx = fmaf((float)i + 0.5f, sx, ox);
-    const float qy = fmaf((float)j + 0.5f, sy, oy);
-    const float qz = fmaf((float)k + 0.5f, sz, oz);
+    Slot sl[1];
+    sl[0].qx = fmaf((float)i + 0.5f, sx, ox);
+    sl[0].qy = fmaf((float)j + 0.5f, sy, oy);
+    sl[0].qz = fmaf((float)k + 0.5f, sz, oz);
+    sl[0].tau = mi.tau;
+    sl[0].s = sl[0].c = 0.f;
+    sl[0].resume = valid ? mi.root : DONE;
+    sl[0].end = mi.end;
     QCounters qc;
-    float s = 0.f, c = 0.f;
-    warp_walk<false>(nodes, tris, valid ? mi.root : DONE, mi.end, mi.tau, mi.cond, qx, qy, qz,
-                     beta, smem[w], s, c, qc, status);
-    if (valid) {
-        const int64_t o = i + nx * (j + ny * k);
-        const float res = s - c;
-        if (omega) omega[o] = res;
-        if (inside) inside[o] = (double)res > TWO_PI_D ? 1 : 0;
-    }
+    warp_walk<false, 1>(nodes, tris, sl, mi.cond, beta, smem[w], qc, status);
+    if (valid) write_result(sl[0], i + nx * (j + ny * k), omega, inside);
 }
 
 // Forest: one persistent launch over all meshes. Queries are sorted by (mesh, Hilbert index); each
-// warp takes the next 32 sorted queries from a global work counter until none are left.
-template <int MINB>
+// warp takes the next 32 * QPL sorted queries from a global work counter until none are left. A
+// slot's walk ends at its own mesh's subtree end, so a warp may serve queries of two meshes.
+template <int MINB, int QPL>
 __global__ void __launch_bounds__(WARP_BLOCK, MINB)
 k_forest_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
               const MeshInfo* __restrict__ meshes, const float* __restrict__ Q,
               const uint64_t* __restrict__ sorted_keys, const uint32_t* __restrict__ order,
-              int64_t n, float beta, float* __restrict__ omega, uint8_t* __restrict__ inside,
-              unsigned* __restrict__ work, unsigned* __restrict__ status) {
-    __shared__ WarpSmem smem[WARP_BLOCK / 32];
+              int64_t n, float beta, float cond, float* __restrict__ omega,
+              uint8_t* __restrict__ inside, unsigned* __restrict__ work,
+              unsigned* __restrict__ status) {
+    __shared__ WarpSmem<QPL> smem[WARP_BLOCK / 32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int64_t nchunks = (n + 31) / 32;
+    const int64_t nchunks = (n + 32 * QPL - 1) / (32 * QPL);
     QCounters qc;
     while (true) {
         unsigned chunk = 0;
         if (lane == 0) chunk = atomicAdd(work, 1u);
         chunk = __shfl_sync(0xffffffffu, chunk, 0);
         if ((int64_t)chunk >= nchunks) break;
-        const int64_t k = (int64_t)chunk * 32 + lane;
-        const bool valid = k < n;
-        float qx = 0.f, qy = 0.f, qz = 0.f;
-        int64_t qi = 0;
-        int root = DONE, end = DONE;
-        float tau = 0.f, cond = 0.f;
-        if (valid) {
-            qi = order[k];
-            qx = Q[3 * qi];
-            qy = Q[3 * qi + 1];
-            qz = Q[3 * qi + 2];
-            const MeshInfo& mi = meshes[sorted_keys[k] >> 30];
-            root = mi.root < 0 ? DONE : mi.root;
-            end = mi.end;
-            tau = mi.tau;
-            cond = mi.cond;
+        Slot sl[QPL];
+        int64_t qi[QPL];
+#pragma unroll
+        for (int j = 0; j < QPL; ++j) {
+            const int64_t k = (int64_t)chunk * (32 * QPL) + 32 * j + lane;
+            sl[j].s = sl[j].c = 0.f;
+            if (k < n) {
+                qi[j] = order[k];
+                sl[j].qx = Q[3 * qi[j]];
+                sl[j].qy = Q[3 * qi[j] + 1];
+                sl[j].qz = Q[3 * qi[j] + 2];
+                const MeshInfo& mi = meshes[sorted_keys[k] >> 30];
+                sl[j].tau = mi.tau;
+                sl[j].resume = mi.root < 0 ? DONE : mi.root;
+                sl[j].end = mi.end;
+            } else {
+                qi[j] = -1;
+                sl[j].qx = sl[j].qy = sl[j].qz = sl[j].tau = 0.f;
+                sl[j].resume = sl[j].end = DONE;
+            }
         }
-        float s = 0.f, c = 0.f;
-        warp_walk<false>(nodes, tris, root, end, tau, cond, qx, qy, qz, beta, smem[w], s, c, qc,
-                         status);
-        if (valid) {
-            const float res = s - c;
-            if (omega) omega[qi] = res;
-            if (inside) inside[qi] = (double)res > TWO_PI_D ? 1 : 0;
-        }
+        warp_walk<false, QPL>(nodes, tris, sl, cond, beta, smem[w], qc, status);
+#pragma unroll
+        for (int j = 0; j < QPL; ++j)
+            if (qi[j] >= 0) write_result(sl[j], qi[j], omega, inside);
     }
 }
 
@@ -717,6 +766,41 @@ __global__ void k_fill_zero(float* omega, uint8_t* inside, double* omega64, int6
 
 inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
 
+// Warp-schedule variants (fwn_config::tuning): queries per lane and register cap.
+//   1: 1 query per lane, 72 registers      2: 1 per lane, no cap     3: 1 per lane, 64 registers
+//   4: 2 queries per lane, 64 registers    5: 2 per lane, 80 registers
+//   0 (default): 4 when the batch fills every SM's warp slots four times over at two queries per
+//   lane, else 3 (with fewer queries, two per lane would leave SMs idle)
+int warp_variant(int tuning, int64_t n) {
+    if (tuning != 0) return tuning;
+    int dev = 0, sms = 0;
+    FWN_CUDA_CHECK(cudaGetDevice(&dev));
+    FWN_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int64_t wave = (int64_t)sms * 32 * 64;  // 32 resident warps per SM, 64 queries each
+    return n >= 4 * wave ? 4 : 3;
+}
+
+template <int MINB, int QPL>
+void launch_query_warp(const Engine& e, const MeshInfo& mi, const float* d_points,
+                       const uint32_t* order, int64_t n, float beta, float* d_omega,
+                       uint8_t* d_inside, unsigned* d_status, cudaStream_t st) {
+    k_query_warp<false, MINB, QPL><<<grid_for(n, WARP_BLOCK * QPL), WARP_BLOCK, 0, st>>>(
+        e.nodes32, e.tris, mi, d_points, order, n, beta, d_omega, d_inside, d_status, nullptr);
+}
+
+void launch_query_warp_variant(int variant, const Engine& e, const MeshInfo& mi,
+                               const float* d_points, const uint32_t* order, int64_t n,
+                               float beta, float* d_omega, uint8_t* d_inside, unsigned* d_status,
+                               cudaStream_t st) {
+    switch (variant) {
+        case 1: launch_query_warp<7, 1>(e, mi, d_points, order, n, beta, d_omega, d_inside, d_status, st); break;
+        case 2: launch_query_warp<1, 1>(e, mi, d_points, order, n, beta, d_omega, d_inside, d_status, st); break;
+        case 4: launch_query_warp<8, 2>(e, mi, d_points, order, n, beta, d_omega, d_inside, d_status, st); break;
+        case 5: launch_query_warp<6, 2>(e, mi, d_points, order, n, beta, d_omega, d_inside, d_status, st); break;
+        default: launch_query_warp<8, 1>(e, mi, d_points, order, n, beta, d_omega, d_inside, d_status, st); break;
+    }
+}
+
 }  // namespace
 
 QueryArgs resolve_query_args(const Engine& e, const fwn_query_opts* o) {
@@ -735,6 +819,7 @@ QueryArgs resolve_query_args(const Engine& e, const fwn_query_opts* o) {
         if (o->beta > 0.f) a.beta = o->beta;
         if (o->tuning > 0) a.tuning = o->tuning;
     }
+    if (a.tuning < 0 || a.tuning > 5) throw Error(FWN_INVALID_ARG, "tuning must be in [0, 5]");
     if (a.precision != FWN_PRECISION_MIXED && a.precision != FWN_PRECISION_FP64)
         throw Error(FWN_INVALID_ARG, "unknown precision");
     if (a.traversal == FWN_TRAVERSAL_AUTO) a.traversal = FWN_TRAVERSAL_WARP;
@@ -808,17 +893,11 @@ void query_mesh(const Engine& e, int mesh, const QueryArgs& a, const float* d_po
         else
             k_query_f64<false><<<grid_for(n, 128), 128, 0, st>>>(e.nodes64, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_omega64, d_status, d_stats);
     } else if (a.traversal == FWN_TRAVERSAL_WARP) {
-        const dim3 g = grid_for(n, WARP_BLOCK);
-        // register caps: tuning 0 (default) 64 registers (8 blocks = 32 warps per SM), tuning 1
-        // 72 registers (7 blocks), tuning 2 none (more registers, fewer resident warps)
-        if (want_stats)
-            k_query_warp<true, 1><<<g, WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, d_stats);
-        else if (a.tuning == 2)
-            k_query_warp<false, 1><<<g, WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, d_stats);
-        else if (a.tuning == 1)
-            k_query_warp<false, 7><<<g, WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, d_stats);
+        if (want_stats)  // counters: one query per lane, no register cap
+            k_query_warp<true, 1, 1><<<grid_for(n, WARP_BLOCK), WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, d_stats);
         else
-            k_query_warp<false, 8><<<g, WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, d_stats);
+            launch_query_warp_variant(warp_variant(a.tuning, n), e, mi, d_points, order, n, a.beta,
+                                      d_omega, d_inside, d_status, st);
     } else {
         if (want_stats)
             k_query_thread<true><<<grid_for(n, bs), bs, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, d_stats);
@@ -861,7 +940,8 @@ void query_grid(const Engine& e, int mesh, const QueryArgs& a, const float origi
     Scratch status(sizeof(unsigned), st);
     FWN_CUDA_CHECK(cudaMemsetAsync(status.p, 0, sizeof(unsigned), st));
     const int64_t threads = nbricks * 32;
-    // register caps as in the point query: tuning 0 -> 64, 1 -> 72, 2 -> none
+    // register caps as in the point query (one query per lane): tuning 1 -> 72, 2 -> none,
+    // otherwise 64
     auto kern = a.tuning == 2 ? k_query_grid<1> : a.tuning == 1 ? k_query_grid<7> : k_query_grid<8>;
     kern<<<grid_for(threads, WARP_BLOCK), WARP_BLOCK, 0, st>>>(
         e.nodes32, e.tris, mi, origin[0], origin[1], origin[2], spacing[0], spacing[1], spacing[2],
@@ -911,14 +991,17 @@ void query_forest(const Engine& e, const QueryArgs& a, const float* d_points,
     int dev = 0, sms = 0, per_sm = 0;
     FWN_CUDA_CHECK(cudaGetDevice(&dev));
     FWN_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    // register caps as in the point query: tuning 0 -> 64, 1 -> 72, 2 -> none
-    auto kern = a.tuning == 2 ? k_forest_warp<1> : a.tuning == 1 ? k_forest_warp<7> : k_forest_warp<8>;
+    // schedule variants as in the point query (warp_variant)
+    const int v = warp_variant(a.tuning, n);
+    const int qpl = v >= 4 ? 2 : 1;
+    auto kern = v == 1 ? k_forest_warp<7, 1> : v == 2 ? k_forest_warp<1, 1> : v == 4 ? k_forest_warp<8, 2>
+              : v == 5 ? k_forest_warp<6, 2> : k_forest_warp<8, 1>;
     FWN_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, WARP_BLOCK, 0));
-    const int64_t chunks = (n + 31) / 32;
+    const int64_t chunks = (n + 32 * qpl - 1) / (32 * qpl);
     const int64_t want = (chunks + WARP_BLOCK / 32 - 1) / (WARP_BLOCK / 32);
     const unsigned grid = (unsigned)std::min<int64_t>(want, (int64_t)sms * std::max(per_sm, 1));
     kern<<<grid, WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, e.meshes, d_points, keys, order, n, a.beta,
-                                      d_omega, d_inside, d_status + 1, d_status);
+                                      e.meshes_h[0].cond, d_omega, d_inside, d_status + 1, d_status);
     FWN_CUDA_CHECK(cudaGetLastError());
 }
 
@@ -963,13 +1046,8 @@ void query_mesh_prealloc(const Engine& e, int mesh, const QueryArgs& a, const fl
     if (a.precision == FWN_PRECISION_FP64) {
         k_query_f64<false><<<grid_for(n, 128), 128, 0, st>>>(e.nodes64, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, nullptr, d_status, nullptr);
     } else if (a.traversal == FWN_TRAVERSAL_WARP) {
-        const dim3 g = grid_for(n, WARP_BLOCK);
-        if (a.tuning == 2)
-            k_query_warp<false, 1><<<g, WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, nullptr);
-        else if (a.tuning == 1)
-            k_query_warp<false, 7><<<g, WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, nullptr);
-        else
-            k_query_warp<false, 8><<<g, WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, nullptr);
+        launch_query_warp_variant(warp_variant(a.tuning, n), e, mi, d_points, order, n, a.beta,
+                                  d_omega, d_inside, d_status, st);
     } else {
         k_query_thread<false><<<grid_for(n, bs), bs, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, nullptr);
     }
