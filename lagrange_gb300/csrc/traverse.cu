@@ -541,33 +541,42 @@ k_query_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
 }
 
 // Regular grid: voxel (i, j, k) has centre fmaf(i + 0.5, spacing, origin) per axis and output
-// index i + nx (j + ny k). Each warp takes one 4 x 4 x 2 brick of voxels (bricks in raster order),
-// so a warp's 32 queries are spatially compact without a sort; no point array is read.
-template <int MINB>
+// index i + nx (j + ny k). Each warp takes one 4 x 4 x (2 QPL) brick of voxels (bricks in raster
+// order; slot q of a lane holds layer pair q), so a warp's queries are spatially compact without
+// a sort; no point array is read.
+template <int MINB, int QPL>
 __global__ void __launch_bounds__(WARP_BLOCK, MINB)
 k_query_grid(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
              const MeshInfo mi, float ox, float oy, float oz, float sx, float sy, float sz,
              int64_t nx, int64_t ny, int64_t nz, int64_t bx, int64_t by, int64_t nbricks,
              float beta, float* __restrict__ omega, uint8_t* __restrict__ inside,
              unsigned* __restrict__ status) {
-    __shared__ WarpSmem<1> smem[WARP_BLOCK / 32];
+    __shared__ WarpSmem<QPL> smem[WARP_BLOCK / 32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t brick = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (brick >= nbricks) return;  // warp-uniform
     const int64_t bi = brick % bx, bj = (brick / bx) % by, bk = brick / (bx * by);
-    const int64_t i = bi * 4 + (lane & 3), j = bj * 4 + ((lane >> 2) & 3), k = bk * 2 + (lane >> 4);
-    const bool valid = i < nx && j < ny && k < nz;
-    Slot sl[1];
-    sl[0].qx = fmaf((float)i + 0.5f, sx, ox);
-    sl[0].qy = fmaf((float)j + 0.5f, sy, oy);
-    sl[0].qz = fmaf((float)k + 0.5f, sz, oz);
-    sl[0].tau = mi.tau;
-    sl[0].s = sl[0].c = 0.f;
-    sl[0].resume = valid ? mi.root : DONE;
-    sl[0].end = mi.end;
+    const int64_t i = bi * 4 + (lane & 3), j = bj * 4 + ((lane >> 2) & 3);
+    Slot sl[QPL];
+    int64_t out[QPL];
+#pragma unroll
+    for (int q = 0; q < QPL; ++q) {
+        const int64_t k = bk * (2 * QPL) + 2 * q + (lane >> 4);
+        const bool valid = i < nx && j < ny && k < nz;
+        out[q] = valid ? i + nx * (j + ny * k) : -1;
+        sl[q].qx = fmaf((float)i + 0.5f, sx, ox);
+        sl[q].qy = fmaf((float)j + 0.5f, sy, oy);
+        sl[q].qz = fmaf((float)k + 0.5f, sz, oz);
+        sl[q].tau = mi.tau;
+        sl[q].s = sl[q].c = 0.f;
+        sl[q].resume = valid ? mi.root : DONE;
+        sl[q].end = mi.end;
+    }
     QCounters qc;
-    warp_walk<false, 1>(nodes, tris, sl, mi.cond, beta, smem[w], qc, status);
-    if (valid) write_result(sl[0], i + nx * (j + ny * k), omega, inside);
+    warp_walk<false, QPL>(nodes, tris, sl, mi.cond, beta, smem[w], qc, status);
+#pragma unroll
+    for (int q = 0; q < QPL; ++q)
+        if (out[q] >= 0) write_result(sl[q], out[q], omega, inside);
 }
 
 // Forest: one persistent launch over all meshes. Queries are sorted by (mesh, Hilbert index); each
@@ -935,14 +944,17 @@ void query_grid(const Engine& e, int mesh, const QueryArgs& a, const float origi
         return;
     }
     if (!e.nodes32) throw Error(FWN_INVALID_ARG, "engine was built without FP32 records (FWN_RECORDS_F32)");
-    const int64_t bx = (nx + 3) / 4, by = (ny + 3) / 4, bz = (nz + 1) / 2;
+    // schedule variants as in the point query (warp_variant); two voxels per lane stack two
+    // 4 x 4 x 2 layers in one brick
+    const int v = warp_variant(a.tuning, nx * ny * nz);
+    const int qpl = v >= 4 ? 2 : 1;
+    const int64_t bx = (nx + 3) / 4, by = (ny + 3) / 4, bz = (nz + 2 * qpl - 1) / (2 * qpl);
     const int64_t nbricks = bx * by * bz;
     Scratch status(sizeof(unsigned), st);
     FWN_CUDA_CHECK(cudaMemsetAsync(status.p, 0, sizeof(unsigned), st));
     const int64_t threads = nbricks * 32;
-    // register caps as in the point query (one query per lane): tuning 1 -> 72, 2 -> none,
-    // otherwise 64
-    auto kern = a.tuning == 2 ? k_query_grid<1> : a.tuning == 1 ? k_query_grid<7> : k_query_grid<8>;
+    auto kern = v == 1 ? k_query_grid<7, 1> : v == 2 ? k_query_grid<1, 1> : v == 4 ? k_query_grid<8, 2>
+              : v == 5 ? k_query_grid<6, 2> : k_query_grid<8, 1>;
     kern<<<grid_for(threads, WARP_BLOCK), WARP_BLOCK, 0, st>>>(
         e.nodes32, e.tris, mi, origin[0], origin[1], origin[2], spacing[0], spacing[1], spacing[2],
         nx, ny, nz, bx, by, nbricks, a.beta, d_omega, d_inside, status.as<unsigned>());

@@ -23,11 +23,12 @@ def torch_cuda():
     return torch
 
 
-def test_grid_equals_explicit_points(torch_cuda):
+@pytest.mark.parametrize("tuning", [0, 4])  # one voxel per lane (auto at this size), two per lane
+def test_grid_equals_explicit_points(torch_cuda, tuning):
     torch = torch_cuda
     V, F = W.displaced_icosphere(40, 5)
-    eng = fwn.FastWindingNumber(V, F)
-    dims = (37, 29, 23)  # not multiples of the 4x4x2 brick
+    eng = fwn.FastWindingNumber(V, F, tuning=tuning)
+    dims = (37, 29, 23)  # not multiples of the 4x4x2 or 4x4x4 brick
     lo, hi = V.min(0).astype(np.float64), V.max(0).astype(np.float64)
     c, h = (lo + hi) / 2, (hi - lo) / 2 * 1.05
     origin = (c - h).astype(np.float32)
