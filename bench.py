@@ -52,11 +52,13 @@ BYTES_NODE_FAR = 96    # sectors 1-3 (far-field coefficients)
 BYTES_TRI = 48
 BYTES_QUERY_IO = 12 + 4 + 1 + 4  # point in, Omega + inside out, sort index
 CPU_LEAF = 8  # leaf size of the CPU restatement of the reference tree, in every CPU timing
-# DRAM bytes (read + write) of one traversal launch, keyed by (workload, leaf size), from the
+# DRAM bytes (read + write) of one traversal launch, keyed by (workload, leaf size, warp-schedule
+# variant), from the
 # one-pass ncu captures of the same command lines (profiles/k_query_warp_traffic_icosphere2m_q10m.md);
 # other workloads and leaf sizes: not captured (traffic null)
-NCU_TRAFFIC = {("displaced_icosphere_nu316_q10000000", 12): 1.34e9 + 299.45e6,
-               ("displaced_icosphere_nu316_q10000000", 16): 1.31e9 + 294.86e6}
+NCU_TRAFFIC = {("displaced_icosphere_nu316_q10000000", 8, 4): 1.44e9 + 351.02e6,
+               ("displaced_icosphere_nu316_q10000000", 12, 4): 1.37e9 + 334.33e6,
+               ("displaced_icosphere_nu316_q10000000", 16, 4): 1.35e9 + 330.50e6}
 
 
 def parse():
@@ -70,6 +72,7 @@ def parse():
     p.add_argument("--nu", type=int, default=None)
     p.add_argument("--queries", type=int, default=None)
     p.add_argument("--leaf", type=int, default=0)  # 0: the autotuner picks (untimed)
+    p.add_argument("--tuning", type=int, default=0)  # with --leaf: warp-schedule variant (0 auto)
     p.add_argument("--traversal", default="warp", choices=["thread", "warp"])
     p.add_argument("--block", type=int, default=128)
     p.add_argument("--fp64-steps", type=int, default=2)
@@ -320,7 +323,7 @@ def run_ours(args, rank, world, local):
     Fd = torch.from_numpy(wl.F).to(dev)
     Qd = torch.from_numpy(wl.Q).to(dev)
     stream = torch.cuda.current_stream(dev)
-    leaf, block, tuning, tuned = args.leaf, args.block, 0, None
+    leaf, block, tuning, tuned = args.leaf, args.block, args.tuning, None
     if leaf == 0:  # the autotuner's choice for this mesh and query distribution (untimed)
         leaf, trav, block, tuning, tuned = autotune_choice(fwn, Vd, Fd, Qd)
         leaf, trav, block, tuning = rank0_choice(dist, (leaf, trav, block, tuning), dev)
@@ -447,12 +450,15 @@ def run_ours(args, rank, world, local):
     sm_max = clocks.get("sm_max_mhz") or measured_peaks().get("sm_max_mhz") or 2070.0
     peak_fp32 = props.multi_processor_count * 128 * 2 * sm_max * 1e6 / 1e12
     achieved = flops / (kernel_ms / 1e3) / 1e12
-    traffic = NCU_TRAFFIC.get((wl.name, args.leaf)) if world == 1 else None
+    # the warp-schedule variant the traversal ran (tuning 0 resolves by batch size, as in the
+    # library: two queries per lane once the batch fills every SM's warp slots four times)
+    variant = tuning or (4 if n >= 4 * props.multi_processor_count * 32 * 64 else 3)
+    traffic = NCU_TRAFFIC.get((wl.name, args.leaf, variant)) if world == 1 else None
     hbm_peak = measured_peaks().get("hbm_gbs")
     result["roofline"] = {
         "bound": "fp32", "achieved": achieved, "peak": peak_fp32, "unit": "TFLOP/s",
         "frac": achieved / peak_fp32, "traffic": traffic,
-        "kernel": "k_query_warp (traversal)", "kernel_ms": kernel_ms,
+        "kernel": "k_query_warp (traversal)", "variant": variant, "kernel_ms": kernel_ms,
         "kernel_share_of_step": kernel_ms / ms,
         "peak_source": f"nominal FP32: {props.multi_processor_count} SMs x 128 lanes x 2 x "
                        f"{sm_max:.0f} MHz (no FP32 figure in MEASURED_PEAKS.json)",
