@@ -18,9 +18,9 @@
 //   mixed / thread : one thread per query, FP32 far field and near field with a Kahan sum;
 //                    triangles within tau = fp64_near_scale * bbox diagonal get det and the
 //                    Van Oosterom denominator in FP64.
-//   mixed / warp   : 32 queries share one cursor (warp-uniform node loads, lanes inactive until
-//                    the cursor reaches their own resume index); the leaf's triangles are staged
-//                    in shared memory once per warp.
+//   mixed / warp   : 32 or 64 queries (one or two per lane) share one cursor (warp-uniform
+//                    node loads, query slots inactive until the cursor reaches their own resume
+//                    index); the leaf's triangles are staged in shared memory once per warp.
 //   fp64           : the plain comparison form, FP64 everywhere (including atan2).
 #include <climits>
 #include <cmath>
@@ -356,17 +356,20 @@ k_query_thread(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tri
 }
 
 // ---- mixed, warp-shared cursor ------------------------------------------------------------------
-// 32 queries share one cursor over the DFS node order: the cursor is the smallest "resume" index
-// of the warp's lanes, and a lane takes part in a step only when the cursor equals its own resume
-// index. Node loads are therefore warp-uniform (one L1 wavefront each), while every lane still
-// visits exactly its own path, in DFS order (so the result does not depend on which queries share
-// the warp). A lane is done when its resume index reaches the end of its own mesh's subtree, so
-// one warp may serve queries of consecutive meshes of a forest (their subtrees are consecutive
-// ranges of the DFS order). The walk is software-pipelined: the next cursor is reduced right
+// 32 * QPL queries (QPL = 1 or 2 per lane) share one cursor over the DFS node order: the cursor
+// is the smallest "resume" index of the warp's query slots, and a slot takes part in a step only
+// when the cursor equals its own resume index. Node loads are therefore warp-uniform (one L1
+// wavefront each, serving every slot), while every query still visits exactly its own path, in
+// DFS order (so the result does not depend on which queries share the warp). With two slots per
+// lane a node record serves 64 queries and each lane has two independent far tests to issue. A
+// slot is done when its resume index reaches the end of its own mesh's subtree, so one warp may
+// serve queries of consecutive meshes of a forest (their subtrees are consecutive ranges of the
+// DFS order). The walk is software-pipelined: the next cursor is reduced right
 // after the far test and its 32 B test sector is loaded before this step's Taylor / leaf work,
 // and the coefficient sectors of the current node are requested before its far test.
 // Near leaves: the (query, triangle) pairs of the leaf under the cursor are spread over all 32
-// lanes (triangles staged in shared memory) and each owner adds its results in triangle order.
+// lanes (triangles staged in shared memory, each query with its mesh's FP64 near-field radius)
+// and each owning slot adds its results in triangle order.
 constexpr int WARP_LEAF_MAX = 16;
 constexpr int WARP_BLOCK = 128;
 constexpr int DONE = INT_MAX;
