@@ -30,6 +30,7 @@ import json
 import math
 import os
 import statistics
+import tempfile
 import subprocess
 import sys
 import time
@@ -43,7 +44,7 @@ sys.path.insert(0, str(ROOT))
 METRIC = "winding queries/s @2M tris (mixed precision, |dw|<=1e-4 vs plain FP64 GPU form)"
 FOUR_PI = 4.0 * math.pi
 
-# Algorithmic work per unit (constants of the traversal kernel):
+# Algorithmic work per unit (constants of the traversal kernel, counted from its source):
 FLOPS_FAR = 82      # order-0/1/2 Taylor term incl. far test and Kahan add (FMA = 2)
 FLOPS_TRI = 95      # Van Oosterom triangle incl. FP64-band test and Kahan add (atan2/sqrt on SFU)
 FLOPS_TEST = 12     # far test of a near node (d = P - q, |d|^2, beta r, compare)
@@ -151,7 +152,7 @@ class Clocks:
         self.enabled = enabled
         self.index = index
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+        self.path = Path(tempfile.gettempdir()) / f"fwn_clocks_{os.getpid()}.csv"
 
     def __enter__(self):
         if not self.enabled:
