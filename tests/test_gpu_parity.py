@@ -420,3 +420,32 @@ def test_non_finite_queries(torch_cuda):
         assert np.all(ins[np.isnan(w)] == 0)
     w, ins = _q(eng, torch, bad)  # sorted: NaN keys fall in one cell, no error
     assert np.all(np.isfinite(w[~nonfin]))
+
+
+def test_warp_schedule_variants_agree(torch_cuda):
+    """Every warp-schedule variant (1-5: one or two queries per lane, register caps) computes
+    the same terms: within 1e-6 of variant 3 and of the FP64 form, identical is_inside outside the
+    band. The allocation-free entry point follows the handle's variant too."""
+    torch = torch_cuda
+    wl = W.displaced_icosphere_workload(nu=40, n_queries=50_000)
+    Q = torch.from_numpy(wl.Q).cuda()
+    ref = None
+    for tuning in (3, 1, 2, 4, 5):
+        eng = _engine(wl.V, wl.F, tuning=tuning)
+        w, ins = _q(eng, torch, wl.Q)
+        if ref is None:
+            ref, iref = w, ins
+            _, _, w64 = _q(eng, torch, wl.Q, precision=fwn.PRECISION_FP64, omega_f64=True)
+            assert np.max(np.abs(w - w64)) / FOUR_PI <= 2e-6
+        assert np.max(np.abs(w - ref)) / FOUR_PI <= 1e-6, tuning
+        band = np.abs(ref / FOUR_PI - 0.5) > 1e-3
+        np.testing.assert_array_equal(ins[band], iref[band])
+        if tuning == 4:
+            L = fwn.library()
+            wn = torch.empty_like(Q[:, 0])
+            inn = torch.empty(len(Q), dtype=torch.uint8, device=Q.device)
+            fwn._check(L.fwn_query_noalloc(eng.handle, C.c_void_p(Q.data_ptr()), len(Q),
+                                           C.c_void_p(wn.data_ptr()), C.c_void_p(inn.data_ptr()),
+                                           None))
+            torch.cuda.synchronize()
+            np.testing.assert_array_equal(wn.cpu().numpy(), w)
