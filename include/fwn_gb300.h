@@ -167,7 +167,9 @@ FWN_API fwn_status fwn_get_info(fwn_handle h, fwn_info* info);
 
 /* Queries on DEVICE buffers: points [n x 3] float; omega [n] float (solid angle, steradians) and
  * inside [n] uint8 (Omega/(4*pi) > 0.5, FastWindingNumber.cpp:66), either output may be NULL.
- * Asynchronous on `stream`; scratch is stream-ordered. */
+ * Asynchronous on `stream`; scratch is stream-ordered. The device-side consistency check of the
+ * walk (a skip link that does not advance, i.e. a corrupt tree) is read back only by the
+ * synchronous calls (fwn_query_host, and fwn_query_ex with work counters). */
 FWN_API fwn_status fwn_query(fwn_handle h, const float* d_points, int64_t n,
                              float* d_omega, uint8_t* d_inside, void* stream);
 
