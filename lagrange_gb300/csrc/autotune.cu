@@ -1,6 +1,6 @@
-// Autotuner: picks the leaf size (build), the traversal schedule, block size and register-cap
-// variant (query) for one mesh and a representative query sample, by timing every candidate with
-// CUDA events on the device. beta does not enter the choice (the schedule and block shape are
+// Autotuner: picks the leaf size (build), the traversal schedule, block size and warp-schedule
+// variant (queries per lane, register cap) for one mesh and a representative query sample, by
+// timing every candidate with CUDA events on the device. beta does not enter the choice (the schedule and block shape are
 // tuned at the caller's beta, which only changes how deep the walk goes).
 //
 // Optional cache: a text file with one line per (GPU name, log2 triangles, log2 queries) key:
