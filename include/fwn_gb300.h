@@ -46,7 +46,7 @@ typedef enum fwn_status {
     FWN_INVALID_ARG = 1,   /* bad sizes, null pointers, out-of-range indices, non-finite vertices */
     FWN_OOM = 2,           /* device allocation failed */
     FWN_CUDA_ERROR = 3,    /* a CUDA runtime call or kernel failed */
-    FWN_TIMEOUT = 4,       /* a bounded device-side wait gave up */
+    FWN_TIMEOUT = 4,       /* reserved: no kernel of this library waits on a flag or a peer */
     FWN_INTERNAL = 5,      /* a device-side consistency check failed (corrupt tree links) */
     FWN_NOT_BUILT = 6      /* handle is null / default-constructed */
 } fwn_status;
