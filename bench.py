@@ -728,26 +728,35 @@ def run_forest(args, rank, world, local):
         Qe = torch.empty_like(Qd)
         sp = C.c_void_p(stream.cuda_stream)
 
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+
         def e2e_call():
+            ev[0].record(stream)
             Qe.copy_(Qh, non_blocking=True)
+            ev[1].record(stream)
             fwn._check(L.fwn_forest_query(forest.handle, C.c_void_p(Qe.data_ptr()),
                                           C.c_void_p(qoff.data_ptr()), C.c_void_p(w.data_ptr()),
                                           C.c_void_p(ins.data_ptr()), C.byref(opts), sp))
+            ev[2].record(stream)
             wh.copy_(w, non_blocking=True)
             ih.copy_(ins, non_blocking=True)
+            ev[3].record(stream)
             stream.synchronize()
         e2e_call()
-        te = []
+        te, phases = [], {"h2d": [], "query": [], "d2h": []}
         for _ in range(args.steps):
             flush.zero_()
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             e2e_call()
             te.append(time.perf_counter() - t0)
+            for k, (i, j) in zip(phases, ((0, 1), (1, 2), (2, 3))):
+                phases[k].append(ev[i].elapsed_time(ev[j]))
         e2e_s = max_over_ranks(dist, sum(te) / len(te), dev)
         result["e2e"] = {"value": job_value(n, world, e2e_s), "unit": "queries/s",
                          "h2d_bytes_per_step": n * 12, "d2h_bytes_per_step": n * 5,
                          "ms_per_step": e2e_s * 1e3, "ms_each": [t * 1e3 for t in te],
+                         "phases_ms_each": phases,
                          "api": "fwn_forest_query (pinned host points copied in, results out)"}
         del Qe
     # ---- CPU restatement of the reference path on a few meshes (rank 0, N=1) ---------------
