@@ -23,6 +23,10 @@
  * host threads are safe (each call allocates its own stream-ordered scratch), matching the
  * reference's const query methods called from OpenVDB worker threads
  * (modules/volume/src/mesh_to_volume.cpp:175-183).
+ *
+ * Devices: an engine lives on the device that was current when it was built. Every query call
+ * (fwn_query*, fwn_forest_query, fwn_query_grid, fwn_orientation_criterion) must be made with
+ * that device current and returns FWN_INVALID_ARG otherwise; fwn_destroy may be called from any.
  */
 #ifndef FWN_GB300_H
 #define FWN_GB300_H

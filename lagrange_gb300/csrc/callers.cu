@@ -90,7 +90,9 @@ template <class Fn> fwn_status guarded(Fn&& fn) {
 
 const Engine& engine_ref(fwn_handle h) {
     if (!h) throw Error(FWN_NOT_BUILT, "null handle (default-constructed or moved-from engine)");
-    return *reinterpret_cast<const Engine*>(h);
+    const Engine& e = *reinterpret_cast<const Engine*>(h);
+    require_engine_device(e);
+    return e;
 }
 
 }  // namespace

@@ -59,12 +59,17 @@ void* scratch_alloc(size_t bytes, cudaStream_t st) {
 }
 
 Engine::~Engine() {
+    // free on the engine's device, then give the caller back its current device
+    int cur = -1;
+    const bool swap = cudaGetDevice(&cur) == cudaSuccess && cur != device &&
+                      cudaSetDevice(device) == cudaSuccess;
     if (nodes32) cudaFree(nodes32);
     if (nodes64) cudaFree(nodes64);
     if (tris) cudaFree(tris);
     if (sorted_tri) cudaFree(sorted_tri);
     if (meshes) cudaFree(meshes);
     if (stage) cudaFree(stage);
+    if (swap) cudaSetDevice(cur);
     delete[] meshes_h;
     delete[] node_tri_begin_h;
 }
@@ -270,6 +275,7 @@ FWN_API fwn_status fwn_query_ex(fwn_handle h, const fwn_query_opts* opts, const 
                                 fwn_query_stats* stats, void* stream) {
     return guarded([&] {
         Engine* e = engine_of(h);
+        require_engine_device(*e);
         check_points(n, d_points);
         if (e->nmeshes != 1) throw Error(FWN_INVALID_ARG, "forest handle: use fwn_forest_query");
         QueryArgs a = resolve_query_args(*e, opts);
@@ -282,6 +288,7 @@ FWN_API fwn_status fwn_query_order(fwn_handle h, const float* d_points, int64_t 
                                    uint32_t* d_order, void* stream) {
     return guarded([&] {
         Engine* e = engine_of(h);
+        require_engine_device(*e);
         check_points(n, d_points);
         if (e->nmeshes != 1) throw Error(FWN_INVALID_ARG, "forest handle: build one engine per mesh");
         if (n > 0 && !d_order) throw Error(FWN_INVALID_ARG, "order pointer is null");
@@ -293,6 +300,7 @@ FWN_API fwn_status fwn_query_host(fwn_handle h, const float* points, int64_t n, 
                                   uint8_t* inside) {
     return guarded([&] {
         Engine* e = engine_of(h);
+        require_engine_device(*e);
         check_points(n, points);
         if (e->nmeshes != 1) throw Error(FWN_INVALID_ARG, "forest handle: use fwn_forest_query");
         if (n == 0) return;
@@ -414,6 +422,7 @@ FWN_API fwn_status fwn_forest_query(fwn_handle h, const float* d_points, const i
                                     void* stream) {
     return guarded([&] {
         Engine* e = engine_of(h);
+        require_engine_device(*e);
         if (!qoff) throw Error(FWN_INVALID_ARG, "query offsets are null");
         if (qoff[0] != 0) throw Error(FWN_INVALID_ARG, "query offsets must start at 0");
         for (int64_t m = 0; m < e->nmeshes; ++m)

@@ -189,6 +189,16 @@ struct Engine {
     ~Engine();
 };
 
+// Queries launch on the current device with the engine's device pointers, so the current device
+// must be the one the engine was built on (a stream passed by the caller belongs to it as well).
+inline void require_engine_device(const Engine& e) {
+    int dev = 0;
+    FWN_CUDA_CHECK(cudaGetDevice(&dev));
+    if (dev != e.device)
+        throw Error(FWN_INVALID_ARG, "the engine was built on device " + std::to_string(e.device) +
+                                         " but the current device is " + std::to_string(dev));
+}
+
 // lbvh_build.cu: builds the forest. d_vertices / d_triangles are device arrays with LOCAL
 // indices per mesh; offsets are host arrays of num_meshes+1 entries.
 void build_forest(Engine& e, const float* d_vertices, const int64_t* vertex_offsets,

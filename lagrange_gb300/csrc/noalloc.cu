@@ -74,12 +74,9 @@ extern "C" FWN_API fwn_status fwn_query_noalloc(fwn_handle h, const float* d_poi
                             std::to_string(n) + " (split the batch, or use fwn_query)");
         if (n > 0 && !d_points) throw Error(FWN_INVALID_ARG, "points pointer is null");
         if (e.nmeshes != 1) throw Error(FWN_INVALID_ARG, "forest handle: use fwn_forest_query");
-        int device = 0;
-        FWN_CUDA_CHECK(cudaGetDevice(&device));
-        if (device != e.device)
-            throw Error(FWN_INVALID_ARG, "the engine was built on another device than the current one");
+        require_engine_device(e);
         if (n == 0) return FWN_OK;
-        void* scratch = scratch_address(device);
+        void* scratch = scratch_address(e.device);
         const QueryArgs a = resolve_query_args(e, nullptr);
         query_mesh_prealloc(e, 0, a, d_points, n, d_omega, d_inside, scratch, kScratchBytes,
                             static_cast<cudaStream_t>(stream));
