@@ -202,8 +202,11 @@ def _host_mesh(vertices, facets):
 class FastWindingNumber:
     """Winding-number engine for one triangle mesh.
 
-    ``FastWindingNumber(vertices [nv,3], facets [nf,3], beta=2, leaf_size=4, ...)``.
-    Host numpy inputs use the synchronous host path; CUDA tensors stay on the device.
+    ``FastWindingNumber(vertices [nv,3], facets [nf,3], beta=2, leaf_size=8, ...)``.
+    Host numpy inputs use the synchronous host path; CUDA tensors stay on the device. The engine
+    lives on the device it was built on (the tensors' device, or the current device for host
+    inputs); CUDA-tensor calls run with the tensors' device made current, and the library rejects
+    a call whose device is not the engine's.
     """
 
     def __init__(self, vertices=None, facets=None, *, config: fwn_config | None = None,
@@ -219,9 +222,10 @@ class FastWindingNumber:
             F = facets.detach().to(torch.int32).contiguous()
             if V.dim() != 2 or V.shape[1] != 3:
                 raise WindingError(1, "Fast winding number engine only supports 3D meshes")
-            _check(L.fwn_build_device(C.c_void_p(V.data_ptr()), V.shape[0],
-                                      C.c_void_p(F.data_ptr()), F.shape[0] if F.numel() else 0,
-                                      C.byref(cfg), _stream_ptr(None), C.byref(self._h)))
+            with torch.cuda.device(V.device):
+                _check(L.fwn_build_device(C.c_void_p(V.data_ptr()), V.shape[0],
+                                          C.c_void_p(F.data_ptr()), F.shape[0] if F.numel() else 0,
+                                          C.byref(cfg), _stream_ptr(None), C.byref(self._h)))
         else:
             V, F = _host_mesh(vertices, facets)
             _check(L.fwn_build(V.ctypes.data_as(C.c_void_p), len(V),
@@ -272,8 +276,9 @@ class FastWindingNumber:
             w64 = torch.empty(n, dtype=torch.float64, device=dev) if omega_f64 else None
             st = fwn_query_stats() if stats else None
             ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else None  # noqa: E731
-            _check(L.fwn_query_ex(self._h, C.byref(o), ptr(Q), n, ptr(w), ptr(ins), ptr(w64),
-                                  C.byref(st) if st is not None else None, _stream_ptr(stream)))
+            with torch.cuda.device(dev):
+                _check(L.fwn_query_ex(self._h, C.byref(o), ptr(Q), n, ptr(w), ptr(ins), ptr(w64),
+                                      C.byref(st) if st is not None else None, _stream_ptr(stream)))
             out = (w, ins)
             if omega_f64:
                 out = out + (w64,)
@@ -306,8 +311,9 @@ class FastWindingNumber:
         Q = points.detach().to(torch.float32).contiguous().reshape(-1, 3)
         n = Q.shape[0]
         o = torch.empty(n, dtype=torch.int32, device=Q.device)  # uint32 bits, n < 2^31
-        _check(library().fwn_query_order(self._h, C.c_void_p(Q.data_ptr()), n,
-                                         C.c_void_p(o.data_ptr()), _stream_ptr(stream)))
+        with torch.cuda.device(Q.device):
+            _check(library().fwn_query_order(self._h, C.c_void_p(Q.data_ptr()), n,
+                                             C.c_void_p(o.data_ptr()), _stream_ptr(stream)))
         return o.long()
 
     def solid_angle(self, points):
@@ -359,10 +365,11 @@ class FastWindingNumber:
         nf = F.shape[0]
         crit = torch.empty(nf, dtype=torch.float32, device=V.device)
         flip = torch.empty(nf, dtype=torch.uint8, device=V.device)
-        _check(library().fwn_orientation_criterion(
-            self._h, C.c_void_p(V.data_ptr()), V.shape[0], C.c_void_p(F.data_ptr()), nf,
-            float(eps), float(threshold), C.c_void_p(crit.data_ptr()), C.c_void_p(flip.data_ptr()),
-            _stream_ptr(stream)))
+        with torch.cuda.device(V.device):
+            _check(library().fwn_orientation_criterion(
+                self._h, C.c_void_p(V.data_ptr()), V.shape[0], C.c_void_p(F.data_ptr()), nf,
+                float(eps), float(threshold), C.c_void_p(crit.data_ptr()),
+                C.c_void_p(flip.data_ptr()), _stream_ptr(stream)))
         return crit, flip
 
     def sample_inside(self, num_samples: int, *, seed: int = 0):
@@ -413,11 +420,12 @@ class Forest(FastWindingNumber):
             import torch
             V = vertices.detach().to(torch.float32).contiguous()
             F = facets.detach().to(torch.int32).contiguous()
-            _check(L.fwn_forest_build_device(C.c_void_p(V.data_ptr()),
-                                             self.voff.ctypes.data_as(C.c_void_p),
-                                             C.c_void_p(F.data_ptr()),
-                                             self.foff.ctypes.data_as(C.c_void_p), self.nmeshes,
-                                             C.byref(cfg), _stream_ptr(None), C.byref(self._h)))
+            with torch.cuda.device(V.device):
+                _check(L.fwn_forest_build_device(C.c_void_p(V.data_ptr()),
+                                                 self.voff.ctypes.data_as(C.c_void_p),
+                                                 C.c_void_p(F.data_ptr()),
+                                                 self.foff.ctypes.data_as(C.c_void_p), self.nmeshes,
+                                                 C.byref(cfg), _stream_ptr(None), C.byref(self._h)))
         else:
             V = np.ascontiguousarray(vertices, dtype=np.float32)
             F = np.ascontiguousarray(facets, dtype=np.int32)
@@ -437,10 +445,11 @@ class Forest(FastWindingNumber):
         w = torch.empty(n, dtype=torch.float32, device=Q.device)
         ins = torch.empty(n, dtype=torch.uint8, device=Q.device)
         o = _opts(precision, traversal, block_size, sort_queries, beta)
-        _check(library().fwn_forest_query(self._h, C.c_void_p(Q.data_ptr()),
-                                          qoff.ctypes.data_as(C.c_void_p),
-                                          C.c_void_p(w.data_ptr()), C.c_void_p(ins.data_ptr()),
-                                          C.byref(o), _stream_ptr(stream)))
+        with torch.cuda.device(Q.device):
+            _check(library().fwn_forest_query(self._h, C.c_void_p(Q.data_ptr()),
+                                              qoff.ctypes.data_as(C.c_void_p),
+                                              C.c_void_p(w.data_ptr()), C.c_void_p(ins.data_ptr()),
+                                              C.byref(o), _stream_ptr(stream)))
         return w, ins
 
 
