@@ -226,9 +226,11 @@ def make_workload(args):
     return W.displaced_icosphere_workload(nu=args.nu or 316, n_queries=args.queries or 10_000_000)
 
 
-def autotune_choice(fwn, Vd, Fd, Qd, sample: int = 2_000_000, seed: int = 5):
-    """fwn_autotune on a seeded sample of the workload's own queries: returns (leaf, traversal,
-    block, tuning, summary). Untimed; the bench then measures the chosen configuration."""
+def autotune_choice(fwn, Vd, Fd, Qd, sample: int = 16_000_000, seed: int = 5):
+    """fwn_autotune on the workload's own queries (a seeded subsample above `sample` points):
+    returns (leaf, traversal, block, tuning, summary). Untimed; the bench then measures the
+    chosen configuration. A subsample is sparser than the workload, so its warps are less
+    coherent and it can favour larger leaves than the full query set does."""
     import torch
     n = Qd.shape[0]
     if n > sample:

@@ -200,7 +200,7 @@ FWN_API fwn_status fwn_query_host(fwn_handle h, const float* points, int64_t n,
  * allocates nothing: for callers that must not allocate device memory while they query (a
  * voxelizer or renderer working under a fixed per-frame device budget, or code where a
  * cudaMalloc/cudaFree could fail or would synchronize the device). Its sort buffers live in one
- * fixed region built into the library (about 16.3 MB per GPU that loads it, held until exit),
+ * fixed region built into the library (about 17.3 MB per GPU that loads it, held until exit),
  * which limits a call to FWN_NOALLOC_MAX_POINTS points (larger n: FWN_INVALID_ARG; split the
  * batch). All calls share that region: calls whose GPU work overlaps (other streams or host
  * threads) race and must be serialized. The first call on each device looks up the region's

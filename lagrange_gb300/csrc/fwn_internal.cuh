@@ -156,8 +156,10 @@ struct Scratch {
 // ---------------------------------------------------------------------------------------------
 // Radix sort (radix_sort.cu): stable LSD sort of (key, value) pairs, 8-bit digits.
 // Sorts keys_a/vals_a using keys_b/vals_b as ping-pong buffers; returns true when the result
-// ended in the *_b buffers.
+// ended in the *_b buffers. temp holds 256 digit counts per tile of kSortTileKeys keys, plus the
+// 256 digit totals (radix_sort_temp_bytes).
 // ---------------------------------------------------------------------------------------------
+constexpr int kSortTileKeys = 2048;  // keys per sort tile: 256 threads x 8 keys
 size_t radix_sort_temp_bytes(int64_t n, int key_bytes);
 bool radix_sort_u32(uint32_t* keys_a, uint32_t* vals_a, uint32_t* keys_b, uint32_t* vals_b,
                     int64_t n, int key_bits, void* temp, cudaStream_t stream);

@@ -7,7 +7,7 @@
 // Morton-sort buffers per call (stream-ordered); this entry point uses a fixed region instead.
 //
 // The region is the file-scope device array below, sized for FWN_NOALLOC_MAX_POINTS points per
-// call (about 16.3 MB). Every GPU that loads the library keeps it until the process exits. All
+// call (about 17.3 MB). Every GPU that loads the library keeps it until the process exits. All
 // calls share it, and it keeps whatever the last call left there: the status word is cleared at
 // the start of every call; the sort buffers and the histogram are fully rewritten before they
 // are read. Two calls whose work overlaps on the GPU (different streams, or different host
@@ -27,11 +27,10 @@ namespace fwn {
 namespace {
 
 constexpr int64_t kMaxPoints = FWN_NOALLOC_MAX_POINTS;
-constexpr int64_t kSortTile = 4096;  // keys per sort tile for 32-bit keys
 // status word (256 B) + four n-entry u32 arrays + sort histogram (256 digits x tiles + totals)
 constexpr size_t kScratchBytes =
-    256 + 16 * (size_t)kMaxPoints + (256 * ((kMaxPoints + kSortTile - 1) / kSortTile) + 256) * 4 +
-    256;
+    256 + 16 * (size_t)kMaxPoints +
+    (256 * ((kMaxPoints + kSortTileKeys - 1) / kSortTileKeys) + 256) * 4 + 256;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 

@@ -3,8 +3,9 @@
 // Sort: 8-bit digits, three launches per pass (reduce-then-scan):
 //   upsweep   : per-tile digit histogram (per-warp shared counters), digit-major output
 //   scan      : one block per digit scans that digit's per-tile counts, writes digit totals
-//   downsweep : tile keys ranked stably with __match_any_sync, scattered into shared memory in
-//               digit order, then written out with runs of consecutive addresses
+//   downsweep : tile keys ranked stably within each warp (lanes holding the same digit found
+//               with one ballot per digit bit), scattered into shared memory in digit order,
+//               then written out with runs of consecutive addresses
 // Stability comes from the warp-striped load order (warp, round, lane) = input order.
 // Used for the triangle Morton keys (u64: mesh id above 30 Morton bits) and the query keys.
 #include "fwn_internal.cuh"
@@ -18,9 +19,13 @@ constexpr int SORT_THREADS = 256;  // == RADIX: one thread per digit in the digi
 constexpr int SORT_WARPS = SORT_THREADS / 32;
 static_assert(SORT_THREADS == RADIX, "digit loops assume one thread per digit");
 
+// 8 keys per thread for both key widths: the downsweep's per-thread key, value, rank and digit
+// arrays then fit in under 64 registers (4 blocks of 256 threads per SM). At 16 keys per thread
+// the 32-bit sort needed 114 registers, ran at 2 blocks per SM and was latency-bound.
 template <class K> struct TileCfg {
-    static constexpr int KPT = sizeof(K) == 8 ? 8 : 16;
+    static constexpr int KPT = 8;
     static constexpr int TILE = SORT_THREADS * KPT;
+    static_assert(TILE == kSortTileKeys, "tile size shared with the fixed no-alloc region");
 };
 
 __device__ __forceinline__ unsigned lanemask_lt() {
@@ -162,7 +167,15 @@ k_downsweep(const K* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
 #pragma unroll
     for (int j = 0; j < KPT; ++j) {
         unsigned d = dg[j];
-        unsigned peers = __match_any_sync(0xffffffffu, d);
+        // lanes holding the same digit: one ballot per bit of d (8 digit bits and the invalid
+        // flag d == RADIX), which is cheaper here than __match_any_sync
+        unsigned peers = 0xffffffffu;
+#pragma unroll
+        for (int bt = 0; bt <= RADIX_BITS; ++bt) {
+            const bool bit = (d >> bt) & 1u;
+            const unsigned m = __ballot_sync(0xffffffffu, bit);
+            peers &= bit ? m : ~m;
+        }
         int leader = __ffs(peers) - 1;
         int before = __popc(peers & lt);
         int cnt = d < RADIX ? wc[w][d] : 0;
