@@ -141,15 +141,8 @@ k_downsweep(const K* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
     const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
     for (int i = tid; i < SORT_WARPS * RADIX; i += SORT_THREADS) (&wc[0][0])[i] = 0;
 
-    // Global base of each digit for this tile: exclusive scan of the digit totals plus this
-    // tile's exclusive offset within the digit.
-    {
-        int dt = digit_totals[tid];
-        int ex = block_exclusive_scan_256(dt, warp_tot);
-        gbase[tid] = ex + hist[(int64_t)tid * nblocks + blockIdx.x];
-    }
-    __syncthreads();
-
+    // The tile's keys and values are requested first, so that their loads are in flight while
+    // the block computes the digits' global bases.
     const int64_t base = (int64_t)blockIdx.x * TILE;
     K k[KPT];
     uint32_t v[KPT];
@@ -161,7 +154,20 @@ k_downsweep(const K* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
         bool valid = idx < n;
         k[j] = valid ? keys_in[idx] : (K)0;
         v[j] = valid ? vals_in[idx] : 0u;
-        dg[j] = valid ? ((unsigned)(k[j] >> shift) & (RADIX - 1)) : (unsigned)RADIX;
+    }
+    // Global base of each digit for this tile: exclusive scan of the digit totals plus this
+    // tile's exclusive offset within the digit.
+    {
+        const int tile_off = hist[(int64_t)tid * nblocks + blockIdx.x];
+        int dt = digit_totals[tid];
+        int ex = block_exclusive_scan_256(dt, warp_tot);
+        gbase[tid] = ex + tile_off;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < KPT; ++j) {
+        int64_t idx = base + (int64_t)w * (KPT * 32) + j * 32 + lane;
+        dg[j] = idx < n ? ((unsigned)(k[j] >> shift) & (RADIX - 1)) : (unsigned)RADIX;
     }
     const unsigned lt = lanemask_lt();
 #pragma unroll
