@@ -707,7 +707,12 @@ def run_forest(args, rank, world, local):
     ms = max_over_ranks(dist, sum(ts) / len(ts), dev)
     build_ms = min(builds)
     mesh_bits = max(0, (M - 1).bit_length())
-    launches_per_query = 1 + 3 * math.ceil((30 + mesh_bits) / 8) + 1  # keys, sort passes, walk
+    # the library's forest sort key: 32 bits (mesh id + top hb Hilbert bits) while every mesh keeps
+    # >= 8 curve cells per query, else 64 bits (mesh id + 30 Hilbert bits)
+    hb = min(30, 32 - mesh_bits)
+    max_q = int(np.diff(fo.qoff).max())
+    key_bits = mesh_bits + hb if hb >= 30 or (hb >= 3 and max_q <= 1 << (hb - 3)) else 30 + mesh_bits
+    launches_per_query = 1 + 3 * math.ceil(key_bits / 8) + 1  # keys, sort passes, walk
     result = {
         "metric": f"winding queries/s, {M} meshes in one persistent CUDA-graph launch",
         "value": job_value(n, world, ms / 1e3), "unit": "queries/s", "n_gpus": world,
@@ -719,7 +724,7 @@ def run_forest(args, rank, world, local):
                    "l2": "flushed before every step (256 MB write)", "generation_s": gen_s},
         "build_ms": build_ms, "tree_nodes": forest.info()["num_nodes"],
         "meshes_per_s_build_plus_query": M / ((build_ms + ms) / 1e3),
-        "gpu_launches": launches_per_query * args.steps,
+        "gpu_launches": launches_per_query * args.steps, "sort_key_bits": key_bits,
         "clocks": clk.summary(),
     }
     # ---- end to end: pinned host points in, Omega + inside out, through fwn_forest_query ------

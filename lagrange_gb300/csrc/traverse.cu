@@ -355,6 +355,18 @@ k_query_thread(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tri
     if (STATS) flush_stats(qc, stats);
 }
 
+// Mesh of forest query k: the last mesh m with qoff[m] <= k (meshes without queries are skipped
+// over, since their offset equals the next mesh's). qoff has nmeshes + 1 entries, qoff[0] = 0.
+__device__ __forceinline__ int mesh_of_query(const int64_t* __restrict__ qoff, int nmeshes,
+                                             int64_t k) {
+    int lo = 0, hi = nmeshes - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (qoff[mid] <= k) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
 // ---- mixed, warp-shared cursor ------------------------------------------------------------------
 // 32 * QPL queries (QPL = 1 or 2 per lane) share one cursor over the DFS node order: the cursor
 // is the smallest "resume" index of the warp's query slots, and a slot takes part in a step only
@@ -589,7 +601,7 @@ template <int MINB, int QPL>
 __global__ void __launch_bounds__(WARP_BLOCK, MINB)
 k_forest_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
               const MeshInfo* __restrict__ meshes, const float* __restrict__ Q,
-              const uint64_t* __restrict__ sorted_keys, const uint32_t* __restrict__ order,
+              const int64_t* __restrict__ qoff, int nmeshes, const uint32_t* __restrict__ order,
               int64_t n, float beta, float cond, float* __restrict__ omega,
               uint8_t* __restrict__ inside, unsigned* __restrict__ work,
               unsigned* __restrict__ status) {
@@ -613,7 +625,7 @@ k_forest_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris
                 sl[j].qx = Q[3 * qi[j]];
                 sl[j].qy = Q[3 * qi[j] + 1];
                 sl[j].qz = Q[3 * qi[j] + 2];
-                const MeshInfo& mi = meshes[sorted_keys[k] >> 30];
+                const MeshInfo& mi = meshes[mesh_of_query(qoff, nmeshes, qi[j])];
                 sl[j].tau = mi.tau;
                 sl[j].resume = mi.root < 0 ? DONE : mi.root;
                 sl[j].end = mi.end;
@@ -753,18 +765,17 @@ __global__ void k_query_keys(const float* __restrict__ Q, int64_t n, const MeshI
     vals[k] = (uint32_t)k;
 }
 
+// Forest sort key of query k: its mesh id above the top `hb` bits of its 30-bit Hilbert index
+// (the same curve, hb < 30 being a coarser level of it).
+template <class K>
 __global__ void k_forest_keys(const float* __restrict__ Q, int64_t n,
                               const int64_t* __restrict__ qoff, int nmeshes,
-                              const MeshInfo* __restrict__ meshes, uint64_t* __restrict__ keys,
+                              const MeshInfo* __restrict__ meshes, int hb, K* __restrict__ keys,
                               uint32_t* __restrict__ vals) {
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
-    int lo = 0, hi = nmeshes - 1;  // last mesh with qoff[m] <= k
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (qoff[mid] <= k) lo = mid; else hi = mid - 1;
-    }
-    keys[k] = ((uint64_t)lo << 30) | query_key(meshes[lo], Q + 3 * k);
+    const int m = mesh_of_query(qoff, nmeshes, k);
+    keys[k] = ((K)m << hb) | (K)(query_key(meshes[m], Q + 3 * k) >> (30 - hb));
     vals[k] = (uint32_t)k;
 }
 
@@ -998,11 +1009,26 @@ void query_forest(const Engine& e, const QueryArgs& a, const float* d_points,
     FWN_CUDA_CHECK(cudaMemsetAsync(d_status, 0, 2 * sizeof(unsigned), st));
     FWN_CUDA_CHECK(cudaMemcpyAsync(d_qoff, query_offsets, (e.nmeshes + 1) * sizeof(int64_t),
                                    cudaMemcpyHostToDevice, st));
-    k_forest_keys<<<grid_for(n, 256), 256, 0, st>>>(d_points, n, d_qoff, (int)e.nmeshes, e.meshes,
-                                                   ka, va);
-    const bool in_b = radix_sort_u64(ka, va, kb, vb, n, 30 + mesh_bits, tmp, st);
-    const uint64_t* keys = in_b ? kb : ka;
-    const uint32_t* order = in_b ? vb : va;
+    // 32-bit keys (mesh id above the top hb bits of the Hilbert index) whenever every mesh keeps
+    // at least 8 curve cells per query at that level, else 64-bit keys with all 30 bits. A
+    // 32-bit pass moves 20 B per key against 32 B, and 39 key bits would need a fifth pass.
+    int64_t max_q = 0;
+    for (int64_t m = 0; m < e.nmeshes; ++m)
+        max_q = std::max(max_q, query_offsets[m + 1] - query_offsets[m]);
+    const int hb = std::min(30, 32 - mesh_bits);
+    const bool narrow = hb >= 30 || (hb >= 3 && max_q <= (int64_t(1) << (hb - 3)));
+    const uint32_t* order = nullptr;
+    if (narrow) {
+        uint32_t* ka32 = reinterpret_cast<uint32_t*>(ka);  // the 64-bit key areas hold n u32 each
+        uint32_t* kb32 = reinterpret_cast<uint32_t*>(kb);
+        k_forest_keys<uint32_t><<<grid_for(n, 256), 256, 0, st>>>(
+            d_points, n, d_qoff, (int)e.nmeshes, e.meshes, hb, ka32, va);
+        order = radix_sort_u32(ka32, va, kb32, vb, n, mesh_bits + hb, tmp, st) ? vb : va;
+    } else {
+        k_forest_keys<uint64_t><<<grid_for(n, 256), 256, 0, st>>>(
+            d_points, n, d_qoff, (int)e.nmeshes, e.meshes, 30, ka, va);
+        order = radix_sort_u64(ka, va, kb, vb, n, 30 + mesh_bits, tmp, st) ? vb : va;
+    }
     int dev = 0, sms = 0, per_sm = 0;
     FWN_CUDA_CHECK(cudaGetDevice(&dev));
     FWN_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -1015,8 +1041,9 @@ void query_forest(const Engine& e, const QueryArgs& a, const float* d_points,
     const int64_t chunks = (n + 32 * qpl - 1) / (32 * qpl);
     const int64_t want = (chunks + WARP_BLOCK / 32 - 1) / (WARP_BLOCK / 32);
     const unsigned grid = (unsigned)std::min<int64_t>(want, (int64_t)sms * std::max(per_sm, 1));
-    kern<<<grid, WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, e.meshes, d_points, keys, order, n, a.beta,
-                                      e.meshes_h[0].cond, d_omega, d_inside, d_status + 1, d_status);
+    kern<<<grid, WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, e.meshes, d_points, d_qoff,
+                                      (int)e.nmeshes, order, n, a.beta, e.meshes_h[0].cond,
+                                      d_omega, d_inside, d_status + 1, d_status);
     FWN_CUDA_CHECK(cudaGetLastError());
 }
 

@@ -301,6 +301,48 @@ def test_forest_matches_cpu_restatement(torch_cuda, oracle_mod):
     np.testing.assert_array_equal(ins[band].astype(bool), wr[band] > 0.5)
 
 
+def test_forest_sort_key_widths(torch_cuda):
+    """A forest query sorts on 32-bit keys (mesh id above a coarser level of the Hilbert index)
+    while every mesh keeps at least 8 curve cells per query, else on 64-bit keys. 300 unit
+    spheres (9 mesh bits, 23 Hilbert bits) with 1.1M queries on mesh 0 take the 64-bit path,
+    with 2^20 the 32-bit one. Both match the FP64 form (per-mesh launches), and every query
+    finds its own mesh: w is near 1 at its sphere's centre and near 0 outside it (the sanity
+    bounds are loose, 1e-2; the parity bound is the FP64 comparison)."""
+    torch = torch_cuda
+    V0, F0 = W.icosphere(4)
+    M = 300
+    shifts = np.zeros((M, 3), np.float64)
+    shifts[:, 0] = 3.0 * np.arange(M)
+    V = np.concatenate([V0 + shifts[m] for m in range(M)]).astype(np.float32)
+    F = np.tile(F0, (M, 1)).astype(np.int32)  # forest triangles index their own mesh's vertices
+    voff = np.arange(M + 1, dtype=np.int64) * len(V0)
+    foff = np.arange(M + 1, dtype=np.int64) * len(F0)
+    forest = fwn.Forest(V, voff, F, foff, records=BOTH)
+    rng = np.random.default_rng(12)
+    for n_big in (1_100_000, 1 << 20):
+        counts = np.full(M, 8)
+        counts[0] = n_big
+        qoff = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+        Q = np.concatenate([rng.uniform(-1.4, 1.4, (c, 3)) + shifts[m]
+                            for m, c in enumerate(counts)])
+        Q[qoff[1:-1]] = shifts[1:]  # first query of every small mesh: its sphere's centre
+        Q = Q.astype(np.float32)
+        Qd = torch.from_numpy(Q).cuda()
+        w, ins = forest.query_forest(Qd, qoff)
+        w64, _ = forest.query_forest(Qd, qoff, precision=fwn.PRECISION_FP64)
+        torch.cuda.synchronize()
+        w, w64, ins = w.cpu().numpy(), w64.cpu().numpy(), ins.cpu().numpy()
+        assert np.max(np.abs(w - w64)) / FOUR_PI <= 2e-6
+        band = np.abs(w64 / FOUR_PI - 0.5) > 1e-3
+        np.testing.assert_array_equal(ins[band].astype(bool), (w64 / FOUR_PI)[band] > 0.5)
+        centres = qoff[1:-1]
+        assert np.all(np.abs(w[centres] / FOUR_PI - 1.0) < 1e-2)
+        r = np.linalg.norm(Q.astype(np.float64) - np.repeat(shifts, counts, axis=0), axis=1)
+        outside = r > 1.2
+        assert np.all(np.abs(w[outside]) / FOUR_PI < 1e-2)
+        assert np.all(ins[r < 0.9] == 1) and np.all(ins[outside] == 0)
+
+
 def test_graph_capture_replay(torch_cuda):
     """Queries captured in a CUDA graph (scratch becomes graph memory nodes) replay to the same
     bits as direct calls: one mesh through fwn_query, and a forest through fwn_forest_query with
