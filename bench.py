@@ -129,6 +129,18 @@ def rank0_choice(dist, values, device=None):
     return [int(v) for v in t.tolist()]
 
 
+def forest_sort_key_bits(num_meshes: int, max_queries_per_mesh: int) -> int:
+    """Key bits of the forest query's radix sort (8 bits per pass), as the library chooses them:
+    32-bit keys (mesh id above the top hb bits of the 30-bit Hilbert index) while every mesh
+    keeps at least 8 curve cells per query at that level, else 64-bit keys (mesh id above all
+    30 bits)."""
+    mesh_bits = max(0, (num_meshes - 1).bit_length())
+    hb = min(30, 32 - mesh_bits)
+    if hb >= 30 or (hb >= 3 and max_queries_per_mesh <= 1 << (hb - 3)):
+        return mesh_bits + hb
+    return 30 + mesh_bits
+
+
 def rank_queries(Q, near_mask, rank: int):
     """The query set a rank answers (weak scaling: every rank has a full-size set). Rank 0 uses
     the workload as generated; rank r > 0 a seeded shuffle of it (different points per warp,
@@ -706,12 +718,7 @@ def run_forest(args, rank, world, local):
             ts.append(a.elapsed_time(b))
     ms = max_over_ranks(dist, sum(ts) / len(ts), dev)
     build_ms = min(builds)
-    mesh_bits = max(0, (M - 1).bit_length())
-    # the library's forest sort key: 32 bits (mesh id + top hb Hilbert bits) while every mesh keeps
-    # >= 8 curve cells per query, else 64 bits (mesh id + 30 Hilbert bits)
-    hb = min(30, 32 - mesh_bits)
-    max_q = int(np.diff(fo.qoff).max())
-    key_bits = mesh_bits + hb if hb >= 30 or (hb >= 3 and max_q <= 1 << (hb - 3)) else 30 + mesh_bits
+    key_bits = forest_sort_key_bits(M, int(np.diff(fo.qoff).max()))
     launches_per_query = 1 + 3 * math.ceil(key_bits / 8) + 1  # keys, sort passes, walk
     result = {
         "metric": f"winding queries/s, {M} meshes in one persistent CUDA-graph launch",
