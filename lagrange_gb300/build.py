@@ -31,11 +31,11 @@ SOURCES = [
     ("radix_sort.cu", []),
     ("lbvh_build.cu", ["-fmad=false"]),
     ("traverse.cu", []),
-    ("forest.cu", []),
     ("fwn_capi.cu", []),
     ("noalloc.cu", []),
     ("autotune.cu", []),
     ("callers.cu", []),
+    ("probe.cu", []),
 ]
 
 
