@@ -93,9 +93,8 @@ struct StageRec {
     double N[3];
     double M1[9];    // [i*3+j], i: normal component, j: offset component
     double M2[18];   // [i*6+s], s: xx yy zz xy xz yz
-    double r;        // bounding radius about P (a float value, rounded up)
-    float lo[3];
-    float hi[3];
+    double r;        // radius about P: farthest vertex of the node's triangles (a float value,
+                     // rounded up); internal nodes get it after the refit (k_node_radius)
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -231,6 +230,14 @@ void query_forest(const Engine& e, const QueryArgs& a, const float* d_points,
                   cudaStream_t stream);
 
 QueryArgs resolve_query_args(const Engine& e, const fwn_query_opts* opts);
+
+// Sort keys of the forest query for host query offsets [nmeshes + 1]: 32-bit keys (narrow) hold
+// the mesh id above the top hilbert_bits of the 30-bit Hilbert index, 64-bit keys all 30 bits.
+struct ForestKeys {
+    int mesh_bits = 0, hilbert_bits = 30, key_bits = 30;
+    bool narrow = true;
+};
+ForestKeys forest_keys(int64_t nmeshes, const int64_t* query_offsets);
 
 // The permutation query_mesh applies when sort_queries is set (Hilbert-curve order of the points in
 // mesh `mesh`'s frame): d_order[k] = index of the k-th point. Async.

@@ -323,7 +323,8 @@ __device__ __forceinline__ void load_tri_d(const float* __restrict__ V, const in
 // (x-X)_j (x-X)_k over the triangle divided by its area).
 // One pass accumulates the moments about X = the first triangle's centroid c0 together with the
 // area-weighted centroid; they are then moved to P with the same recentring formulas a parent
-// uses for its children (e = c0 - P). A second, vertex-only pass gives r = max |v - P|.
+// uses for its children (e = c0 - P). A second, vertex-only pass gives r = max |v - P|
+// (vertex_r2, the same bound k_node_radius computes for internal nodes).
 constexpr double kThird = 1.0 / 3.0;
 constexpr double kTwelfth = 1.0 / 12.0;
 
@@ -331,6 +332,14 @@ constexpr double kTwelfth = 1.0 / 12.0;
 // product is contracted implicitly; every fused operation of the refit is written out, at the
 // same places as in the oracle's restatement (C fma()), which keeps the two bit-identical.
 __device__ __forceinline__ double fmad(double a, double b, double c) { return __fma_rn(a, b, c); }
+
+// Squared distance of a vertex from P in FP64, fused at fixed places: the term whose maximum over
+// a node's vertices gives the node radius (leaves in leaf_moments, internal nodes in
+// k_node_radius; a maximum does not depend on the order of its terms).
+__device__ __forceinline__ double vertex_r2(double x, double y, double z, const double* P) {
+    const double dx = x - P[0], dy = y - P[1], dz = z - P[2];
+    return fmad(dx, dx, fmad(dy, dy, dz * dz));
+}
 
 __device__ void leaf_moments(const float* __restrict__ V, const int32_t* __restrict__ F,
                              const int64_t* __restrict__ voff, const uint64_t* __restrict__ keys,
@@ -340,7 +349,6 @@ __device__ void leaf_moments(const float* __restrict__ V, const int32_t* __restr
     double N[3] = {0.0, 0.0, 0.0}, M1[9], M2[18];
     for (int i = 0; i < 9; ++i) M1[i] = 0.0;
     for (int i = 0; i < 18; ++i) M2[i] = 0.0;
-    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
     const int SJ[6] = {0, 1, 2, 0, 0, 1};
     const int SK[6] = {0, 1, 2, 1, 2, 2};
     for (int s = f; s <= l; ++s) {
@@ -380,12 +388,6 @@ __device__ void leaf_moments(const float* __restrict__ V, const int32_t* __restr
 #pragma unroll
             for (int q = 0; q < 6; ++q) M2[6 * i + q] = fmad(nn[i], Q[q], M2[6 * i + q]);
         }
-        for (int j = 0; j < 3; ++j)
-            for (int a = 0; a < 3; ++a) {
-                const float x = (float)v[j][a];
-                lo[a] = fminf(lo[a], x);
-                hi[a] = fmaxf(hi[a], x);
-            }
     }
     const double cnt = (double)(l - f + 1);
     double P[3], e[3];
@@ -409,23 +411,17 @@ __device__ void leaf_moments(const float* __restrict__ V, const int32_t* __restr
         const int m = (int)(keys[s] >> MORTON_BITS);
         double v[3][3];
         load_tri_d(V, F, voff[m], t, v);
-        for (int j = 0; j < 3; ++j) {
-            const double dx = v[j][0] - P[0], dy = v[j][1] - P[1], dz = v[j][2] - P[2];
-            r2 = fmax(r2, fmad(dx, dx, fmad(dy, dy, dz * dz)));
-        }
+        for (int j = 0; j < 3; ++j) r2 = fmax(r2, vertex_r2(v[j][0], v[j][1], v[j][2], P));
     }
     for (int a = 0; a < 3; ++a) {
         R.P[a] = P[a];
         R.N[a] = N[a];
-        R.lo[a] = lo[a];
-        R.hi[a] = hi[a];
     }
     R.area = A;
     R.r = round_up_float(sqrt(r2));
 }
 
 __device__ __forceinline__ double ldcg_d(const double* p) { return __ldcg(p); }
-__device__ __forceinline__ float ldcg_f(const float* p) { return __ldcg(p); }
 
 __device__ void combine_moments(const StageRec* __restrict__ a_, const StageRec* __restrict__ b_,
                                 StageRec& R) {
@@ -468,26 +464,8 @@ __device__ void combine_moments(const StageRec* __restrict__ a_, const StageRec*
                                    fmad(M1b[3 * i + k], eb[j], fmad(M1b[3 * i + j], eb[k], ldcg_d(&b_->M2[6 * i + q]))));
             R.M2[6 * i + q] = ta + tb;
         }
-    double lo[3], hi[3];
-    for (int a = 0; a < 3; ++a) {
-        const float la = fminf(ldcg_f(&a_->lo[a]), ldcg_f(&b_->lo[a]));
-        const float ha = fmaxf(ldcg_f(&a_->hi[a]), ldcg_f(&b_->hi[a]));
-        R.lo[a] = la;
-        R.hi[a] = ha;
-        lo[a] = la;
-        hi[a] = ha;
-    }
     R.area = A;
-    // radius: min of (a) the sphere around both child spheres, (b) farthest bbox corner
-    const double ra = ldcg_d(&a_->r), rb = ldcg_d(&b_->r);
-    const double da = sqrt(fmad(ea[0], ea[0], fmad(ea[1], ea[1], ea[2] * ea[2]))) + ra;
-    const double db = sqrt(fmad(eb[0], eb[0], fmad(eb[1], eb[1], eb[2] * eb[2]))) + rb;
-    double c2 = 0.0;
-    for (int a = 0; a < 3; ++a) {
-        const double x = fmax(fabs(P[a] - lo[a]), fabs(P[a] - hi[a]));
-        c2 = fmad(x, x, c2);
-    }
-    R.r = round_up_float(fmin(fmax(da, db), sqrt(c2)));
+    R.r = 0.0;  // exact radius about P from the node's vertices: k_node_radius, after the refit
 }
 
 __device__ __forceinline__ void store_rec(StageRec* dst, const StageRec& R) {
@@ -537,6 +515,68 @@ __global__ void k_refit(int num_leaves, const int* __restrict__ leaf_list,
     }
 }
 
+// ---- K4a: exact node radii ------------------------------------------------------------------------
+// The far test of a node compares |q - P| with beta * r, so r must bound the distance from P to
+// every point of the node's triangles; the tightest such bound is the distance to the farthest
+// vertex (triangles are convex hulls of their vertices). Leaves compute it in leaf_moments. An
+// internal node's triangles are the contiguous run of sorted slots [first, last]: it is split into
+// chunks of kRadiusChunk slots, one warp per chunk, whose maxima meet in an atomicMax on the bit
+// pattern (non-negative doubles order like their bits). The result does not depend on the order,
+// so it equals the serial maximum bit for bit.
+constexpr int kRadiusChunk = 2048;
+
+__device__ __forceinline__ bool internal_emitted(const uint64_t* __restrict__ keys,
+                                                 const int* __restrict__ first,
+                                                 const int* __restrict__ last,
+                                                 const uint8_t* __restrict__ flags, int u) {
+    const uint8_t fl = flags[u];
+    return (fl & 1) && !(fl & 2) && !is_cross(keys, first, last, u);
+}
+
+// chunks[u] for the internal nodes u < n - 1 (0 when not an emitted single-mesh internal node);
+// chunks[n - 1] = 0 becomes the total after the exclusive scan.
+__global__ void k_radius_chunks(int n, const uint64_t* __restrict__ keys,
+                                const int* __restrict__ first, const int* __restrict__ last,
+                                const uint8_t* __restrict__ flags, int* __restrict__ chunks) {
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= n) return;
+    chunks[u] = (u < n - 1 && internal_emitted(keys, first, last, flags, u))
+                    ? (last[u] - first[u] + kRadiusChunk) / kRadiusChunk
+                    : 0;
+}
+
+// Grid-stride over the chunks: chunk c belongs to the last node u with off[u] <= c.
+__global__ void k_node_radius(int n, const int* __restrict__ off, const int* __restrict__ first,
+                              const int* __restrict__ last, const int* __restrict__ pos,
+                              const StageRec* __restrict__ stage, const TriF32* __restrict__ tris,
+                              unsigned long long* __restrict__ r2bits) {
+    const int lane = threadIdx.x & 31;
+    const int total = off[n - 1];
+    const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+    for (int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); c < total; c += nwarps) {
+        int lo = 0, hi = n - 2;  // off[n - 1] = total > c, so the node is in [0, n - 2]
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (off[mid] <= c) lo = mid; else hi = mid - 1;
+        }
+        const int u = lo;
+        const int s0 = first[u] + (c - off[u]) * kRadiusChunk;
+        const int s1 = min(last[u] + 1, s0 + kRadiusChunk);
+        const int i = pos[u];
+        const double P[3] = {stage[i].P[0], stage[i].P[1], stage[i].P[2]};
+        double r2 = 0.0;
+        for (int s = s0 + lane; s < s1; s += 32) {
+            const float4 t0 = tris[s].t0, t1 = tris[s].t1, t2 = tris[s].t2;
+            r2 = fmax(r2, vertex_r2(t0.x, t0.y, t0.z, P));
+            r2 = fmax(r2, vertex_r2(t0.w, t1.x, t1.y, P));
+            r2 = fmax(r2, vertex_r2(t1.z, t1.w, t2.x, P));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) r2 = fmax(r2, __shfl_xor_sync(0xffffffffu, r2, o));
+        if (lane == 0) atomicMax(&r2bits[i], (unsigned long long)__double_as_longlong(r2));
+    }
+}
+
 // ---- K4b: records -------------------------------------------------------------------------------
 struct Coeffs {
     double trM1, N[3], W[3], C[6], D[10];
@@ -582,8 +622,9 @@ __device__ void derive_coeffs(const StageRec& R, Coeffs& c) {
 __global__ void k_convert(int n, const uint64_t* __restrict__ keys, const int* __restrict__ first,
                           const int* __restrict__ last, const uint8_t* __restrict__ flags,
                           const int* __restrict__ pos, const int* __restrict__ skip,
-                          const StageRec* __restrict__ stage, NodeF32* __restrict__ n32,
-                          NodeF64* __restrict__ n64, int* __restrict__ leaf_count) {
+                          StageRec* __restrict__ stage, const unsigned long long* __restrict__ r2bits,
+                          NodeF32* __restrict__ n32, NodeF64* __restrict__ n64,
+                          int* __restrict__ leaf_count) {
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= 2 * n - 1) return;
     const uint8_t fl = flags[u];
@@ -598,6 +639,10 @@ __global__ void k_convert(int n, const uint64_t* __restrict__ keys, const int* _
     StageRec R;
     if (!cross) {
         R = stage[i];
+        if (!leaf) {  // internal: the exact radius of k_node_radius
+            R.r = round_up_float(sqrt(__longlong_as_double((long long)r2bits[i])));
+            stage[i].r = R.r;
+        }
         derive_coeffs(R, c);
     } else {
         memset(&R, 0, sizeof(R));
@@ -813,14 +858,29 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
                                                        right, pos, tri_of_slot, d_V, d_F, voff,
                                                        stage, visit, status);
         FWN_CUDA_CHECK(cudaGetLastError());
-        if (e.cfg.records & FWN_RECORDS_F32) FWN_CUDA_CHECK(cudaMalloc(&e.nodes32, E * sizeof(NodeF32)));
-        if (e.cfg.records & FWN_RECORDS_F64) FWN_CUDA_CHECK(cudaMalloc(&e.nodes64, E * sizeof(NodeF64)));
-        k_convert<<<grid_for(nn, 128), 128, 0, st>>>(n, keys, first, last, flags, pos, skip, stage,
-                                                     e.nodes32, e.nodes64, leaf_count);
         FWN_CUDA_CHECK(cudaMalloc(&e.tris, (size_t)n * sizeof(TriF32)));
         FWN_CUDA_CHECK(cudaMalloc(&e.sorted_tri, (size_t)n * sizeof(int)));
         k_tri_records<<<grid_for(n, 256), 256, 0, st>>>(n, tri_of_slot, keys, d_V, d_F, voff,
                                                         e.tris, e.sorted_tri);
+        // exact radii of the internal nodes from the triangle records (chunks of each node's
+        // slot run; the scan's last entry is the chunk total)
+        int* rchunk = (int*)track(dalloc<int>(n, st));
+        unsigned long long* r2bits = (unsigned long long*)track(dalloc<unsigned long long>(E, st));
+        FWN_CUDA_CHECK(cudaMemsetAsync(r2bits, 0, (size_t)E * sizeof(unsigned long long), st));
+        k_radius_chunks<<<grid_for(n, 256), 256, 0, st>>>(n, keys, first, last, flags, rchunk);
+        exclusive_scan_i32(rchunk, n, scan_tmp, st);
+        if (n > 1) {
+            int dev = 0, sms = 0;
+            FWN_CUDA_CHECK(cudaGetDevice(&dev));
+            FWN_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+            k_node_radius<<<sms * 8, 256, 0, st>>>(n, rchunk, first, last, pos, stage, e.tris,
+                                                   r2bits);
+        }
+        FWN_CUDA_CHECK(cudaGetLastError());
+        if (e.cfg.records & FWN_RECORDS_F32) FWN_CUDA_CHECK(cudaMalloc(&e.nodes32, E * sizeof(NodeF32)));
+        if (e.cfg.records & FWN_RECORDS_F64) FWN_CUDA_CHECK(cudaMalloc(&e.nodes64, E * sizeof(NodeF64)));
+        k_convert<<<grid_for(nn, 128), 128, 0, st>>>(n, keys, first, last, flags, pos, skip, stage,
+                                                     r2bits, e.nodes32, e.nodes64, leaf_count);
         FWN_CUDA_CHECK(cudaGetLastError());
         int lc = 0;
         FWN_CUDA_CHECK(cudaMemcpyAsync(&lc, leaf_count, sizeof(int), cudaMemcpyDeviceToHost, st));

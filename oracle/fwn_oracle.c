@@ -405,7 +405,6 @@ void oracle_ref_query(void* h, const float* Q, int64_t nq, float beta, float* om
 /* ========================================================================================== */
 typedef struct {
     double P[3], area, N[3], M1[9], M2[18], r;
-    float lo[3], hi[3];
 } lb_stage;
 
 typedef struct {
@@ -475,15 +474,31 @@ static void lb_tri_d(const lb_tree* T, int64_t s, double v[3][3]) {
 /* Leaf moments (same steps as the device refit): one pass accumulates the area-weighted
  * centroid and the moments about the first triangle's centroid c0; the moments are then moved to
  * P = float(area-weighted centroid) with the parent recentring formulas (e = c0 - P); a second,
- * vertex-only pass gives r = max |v - P| (rounded up to a float). */
+ * vertex-only pass gives r = max |v - P| (rounded up to a float, lb_node_r2). */
 /* The refit's fused multiply-adds are written out (C fma(), correctly rounded) at the same places
  * as in the device refit, which is compiled without implicit contraction. */
+/* Squared radius of the sphere about P through the farthest vertex of the triangles in sorted
+ * slots [f, l]: max fma(dx, dx, fma(dy, dy, dz * dz)) with d = v - P in FP64. A maximum does not
+ * depend on the order of its terms, so the device's chunked warp reduction gives the same value.
+ * Every node's radius, leaf or internal, is this exact bound, rounded up to a float. */
+static double lb_node_r2(const lb_tree* T, int64_t f, int64_t l, const double* P) {
+    double r2 = 0.0;
+    for (int64_t s = f; s <= l; ++s) {
+        double v[3][3];
+        lb_tri_d(T, s, v);
+        for (int j = 0; j < 3; ++j) {
+            const double dx = v[j][0] - P[0], dy = v[j][1] - P[1], dz = v[j][2] - P[2];
+            r2 = fmax(r2, fma(dx, dx, fma(dy, dy, dz * dz)));
+        }
+    }
+    return r2;
+}
+
 static void lb_leaf(const lb_tree* T, int64_t f, int64_t l, lb_stage* R) {
     static const double kThird = 1.0 / 3.0, kTwelfth = 1.0 / 12.0;
     static const int SJ[6] = {0, 1, 2, 0, 0, 1}, SK[6] = {0, 1, 2, 1, 2, 2};
     double A = 0.0, S[3] = {0, 0, 0}, Cs[3] = {0, 0, 0}, c0[3] = {0, 0, 0};
     double N[3] = {0, 0, 0}, M1[9] = {0}, M2[18] = {0};
-    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (int64_t s = f; s <= l; ++s) {
         double v[3][3], e1[3], e2[3], nn[3], c[3], d[3], w[3][3], Q[6];
         lb_tri_d(T, s, v);
@@ -516,12 +531,6 @@ static void lb_leaf(const lb_tree* T, int64_t f, int64_t l, lb_stage* R) {
             for (int j = 0; j < 3; ++j) M1[3 * i + j] = fma(nn[i], d[j], M1[3 * i + j]);
             for (int q = 0; q < 6; ++q) M2[6 * i + q] = fma(nn[i], Q[q], M2[6 * i + q]);
         }
-        for (int j = 0; j < 3; ++j)
-            for (int a = 0; a < 3; ++a) {
-                const float x = (float)v[j][a];
-                lo[a] = fminf(lo[a], x);
-                hi[a] = fmaxf(hi[a], x);
-            }
     }
     const double cnt = (double)(l - f + 1);
     double P[3], e[3];
@@ -538,23 +547,12 @@ static void lb_leaf(const lb_tree* T, int64_t f, int64_t l, lb_stage* R) {
         }
         for (int j = 0; j < 3; ++j) R->M1[3 * i + j] = fma(N[i], e[j], M1[3 * i + j]);
     }
-    double r2 = 0.0;
-    for (int64_t s = f; s <= l; ++s) {
-        double v[3][3];
-        lb_tri_d(T, s, v);
-        for (int j = 0; j < 3; ++j) {
-            const double dx = v[j][0] - P[0], dy = v[j][1] - P[1], dz = v[j][2] - P[2];
-            r2 = fmax(r2, fma(dx, dx, fma(dy, dy, dz * dz)));
-        }
-    }
     for (int a = 0; a < 3; ++a) {
         R->P[a] = P[a];
         R->N[a] = N[a];
-        R->lo[a] = lo[a];
-        R->hi[a] = hi[a];
     }
     R->area = A;
-    R->r = round_up_float(sqrt(r2));
+    R->r = round_up_float(sqrt(lb_node_r2(T, f, l, P)));
 }
 
 static void lb_combine(const lb_stage* a, const lb_stage* b, lb_stage* R) {
@@ -583,22 +581,8 @@ static void lb_combine(const lb_stage* a, const lb_stage* b, lb_stage* R) {
                                   fma(b->M1[3 * i + k], eb[j], fma(b->M1[3 * i + j], eb[k], b->M2[6 * i + q])));
             o.M2[6 * i + q] = ta + tb;
         }
-    double lo[3], hi[3];
-    for (int a2 = 0; a2 < 3; ++a2) {
-        o.lo[a2] = fminf(a->lo[a2], b->lo[a2]);
-        o.hi[a2] = fmaxf(a->hi[a2], b->hi[a2]);
-        lo[a2] = o.lo[a2];
-        hi[a2] = o.hi[a2];
-    }
     o.area = A;
-    const double da = sqrt(fma(ea[0], ea[0], fma(ea[1], ea[1], ea[2] * ea[2]))) + a->r;
-    const double db = sqrt(fma(eb[0], eb[0], fma(eb[1], eb[1], eb[2] * eb[2]))) + b->r;
-    double c2 = 0.0;
-    for (int a2 = 0; a2 < 3; ++a2) {
-        const double x = fmax(fabs(P[a2] - lo[a2]), fabs(P[a2] - hi[a2]));
-        c2 = fma(x, x, c2);
-    }
-    o.r = round_up_float(fmin(fmax(da, db), sqrt(c2)));
+    o.r = 0.0; /* set from the node's vertices once P is known (lb_node_r2) */
     *R = o;
 }
 
@@ -784,10 +768,12 @@ void* oracle_lbvh_build(const float* V, const int64_t* voff, const int32_t* F, c
         for (int64_t p = E - 1; p >= 0; --p) {
             const int32_t u = node_of_pos[p];
             if (CROSS(u)) continue;
-            if (flags[u] & 2)
+            if (flags[u] & 2) {
                 lb_leaf(T, first[u], last[u], &T->st[p]);
-            else
+            } else {
                 lb_combine(&T->st[pos[left[u]]], &T->st[pos[right[u]]], &T->st[p]);
+                T->st[p].r = round_up_float(sqrt(lb_node_r2(T, first[u], last[u], T->st[p].P)));
+            }
         }
 #undef BIG
 #undef CROSS
