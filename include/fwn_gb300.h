@@ -204,7 +204,9 @@ FWN_API fwn_status fwn_query_host(fwn_handle h, const float* points, int64_t n,
  * which limits a call to FWN_NOALLOC_MAX_POINTS points (larger n: FWN_INVALID_ARG; split the
  * batch). All calls share that region: calls whose GPU work overlaps (other streams or host
  * threads) race and must be serialized. The first call on each device looks up the region's
- * device address; make it before any stream capture. Asynchronous on `stream`. */
+ * device address; make it before any stream capture. Asynchronous on `stream`; like fwn_query,
+ * it does not read back the walk's device-side consistency check (that would need a
+ * synchronisation): use fwn_query_host or fwn_query_ex with work counters for that check. */
 #define FWN_NOALLOC_MAX_POINTS (1 << 20)
 FWN_API fwn_status fwn_query_noalloc(fwn_handle h, const float* d_points, int64_t n,
                                      float* d_omega, uint8_t* d_inside, void* stream);
@@ -287,11 +289,40 @@ FWN_API fwn_status fwn_forest_build_device(const float* d_vertices,
 
 /* Forest query on DEVICE buffers: points of mesh m are d_points[query_offsets[m] ..
  * query_offsets[m+1]) (host int64 offsets, num_meshes+1 entries). One persistent launch over
- * a work queue of (mesh, chunk) items. */
+ * a work queue of (mesh, chunk) items.
+ * Graph capture: the call reads query_offsets on the host when it is made (to choose the sort-key
+ * width and the persistent grid) and copies them to the device with an async copy. A captured
+ * call therefore replays with the offsets' values at capture time baked into those choices:
+ * keep the offsets unchanged between replays (the copy re-reads the pinned array, but the key
+ * width and grid would not follow a change), or capture again. */
 FWN_API fwn_status fwn_forest_query(fwn_handle h, const float* d_points,
                                     const int64_t* query_offsets, float* d_omega,
                                     uint8_t* d_inside, const fwn_query_opts* opts,
                                     void* stream);
+
+/* No counterpart in the reference (a diagnostic). Usage of the library's per-device pool of
+ * stream-ordered query scratch (zeros if no call has used the pool on `device` yet): bytes the
+ * pool holds from the driver, bytes handed out, and the high-water mark of handed-out bytes since
+ * the last reset (reset_high != 0 restarts it from the current value before reading). Any output
+ * may be NULL. Host-side; no device work. */
+FWN_API fwn_status fwn_scratch_pool_stats(int32_t device, int32_t reset_high,
+                                          uint64_t* reserved_bytes, uint64_t* used_bytes,
+                                          uint64_t* used_high_bytes);
+
+/* No counterpart in the reference (its per-point queries sort nothing). The key width, in bits,
+ * of the radix sort that fwn_forest_query runs for these HOST query offsets [num_meshes + 1]: the
+ * mesh id above the top bits of the 30-bit Hilbert index, 32-bit keys while every mesh keeps at
+ * least 8 curve cells per query at that level, else 64-bit keys with all 30 bits. The sort makes
+ * ceil(bits / 8) passes. Host-only (no device work). */
+FWN_API fwn_status fwn_forest_sort_key_bits(int64_t num_meshes, const int64_t* query_offsets,
+                                            int32_t* key_bits);
+
+/* No counterpart in the reference (a measurement aid). The device's FP32 fused-multiply-add
+ * throughput, which bounds the traversal kernels: a full-occupancy grid of independent FMA chains
+ * on the current device, timed with CUDA events (median of 5 launches after 2 warm-ups).
+ * form 0: scalar fma.rn.f32; form 1: paired fma.rn.f32x2. Writes the flops of one launch
+ * (FMA = 2) and its device milliseconds. Allocates 4 bytes. Synchronous on `stream`. */
+FWN_API fwn_status fwn_probe_fp32_peak(int32_t form, double* flops, double* ms, void* stream);
 
 #ifdef __cplusplus
 }

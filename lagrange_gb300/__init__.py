@@ -86,7 +86,8 @@ EXPORTS = ["fwn_config_default", "fwn_last_error", "fwn_version", "fwn_build", "
            "fwn_export_tree", "fwn_export_moments", "fwn_forest_build",
            "fwn_forest_build_device", "fwn_forest_query", "fwn_query_noalloc", "fwn_autotune",
            "fwn_query_grid", "fwn_orientation_criterion", "fwn_query_order",
-           "fwn_forest_autotune"]
+           "fwn_forest_autotune", "fwn_forest_sort_key_bits", "fwn_probe_fp32_peak",
+           "fwn_scratch_pool_stats"]
 
 
 def library():
@@ -128,11 +129,16 @@ def library():
                                C.POINTER(fwn_tune_result), P]
     L.fwn_forest_autotune.argtypes = [P, P, P, P, i64, P, P, C.POINTER(fwn_config), C.c_char_p,
                                       C.POINTER(fwn_tune_result), P]
+    L.fwn_forest_sort_key_bits.argtypes = [i64, P, C.POINTER(C.c_int32)]
+    L.fwn_probe_fp32_peak.argtypes = [C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double), P]
+    u64p = C.POINTER(C.c_uint64)
+    L.fwn_scratch_pool_stats.argtypes = [C.c_int32, C.c_int32, u64p, u64p, u64p]
     for name in ("fwn_build", "fwn_build_device", "fwn_destroy", "fwn_get_info", "fwn_query",
                  "fwn_query_ex", "fwn_query_host", "fwn_export_tree", "fwn_export_moments",
                  "fwn_forest_build", "fwn_forest_build_device", "fwn_forest_query",
                  "fwn_query_noalloc", "fwn_autotune", "fwn_query_grid",
-                 "fwn_orientation_criterion", "fwn_query_order", "fwn_forest_autotune"):
+                 "fwn_orientation_criterion", "fwn_query_order", "fwn_forest_autotune",
+                 "fwn_forest_sort_key_bits", "fwn_probe_fp32_peak", "fwn_scratch_pool_stats"):
         getattr(L, name).restype = st
     _lib = L
     return L
@@ -153,6 +159,33 @@ def config_default(**overrides) -> fwn_config:
             raise TypeError(f"unknown config field {k!r}")
         setattr(c, k, v)
     return c
+
+
+def forest_sort_key_bits(query_offsets) -> int:
+    """Key width (bits) of the radix sort fwn_forest_query runs for these query offsets
+    [num_meshes + 1]; the sort makes ceil(bits / 8) passes. Host-only."""
+    q = np.ascontiguousarray(np.asarray(query_offsets), dtype=np.int64)
+    out = C.c_int32(0)
+    _check(library().fwn_forest_sort_key_bits(len(q) - 1, q.ctypes.data_as(C.c_void_p),
+                                              C.byref(out)))
+    return int(out.value)
+
+
+def scratch_pool_stats(device: int = 0, reset_high: bool = False) -> dict:
+    """Bytes the library's query-scratch pool of `device` reserves, hands out, and has handed out
+    at most since the last reset (fwn_scratch_pool_stats)."""
+    r, u, h = C.c_uint64(0), C.c_uint64(0), C.c_uint64(0)
+    _check(library().fwn_scratch_pool_stats(int(device), 1 if reset_high else 0, C.byref(r),
+                                            C.byref(u), C.byref(h)))
+    return {"reserved": r.value, "used": u.value, "used_high": h.value}
+
+
+def probe_fp32_peak(form: int = 0, stream=None) -> dict:
+    """Measured FP32 FMA throughput of the current device (fwn_probe_fp32_peak): form 0 scalar
+    FMA, 1 paired f32x2 FMA. Returns {"tflops", "flops", "ms"}."""
+    fl, ms = C.c_double(0.0), C.c_double(0.0)
+    _check(library().fwn_probe_fp32_peak(int(form), C.byref(fl), C.byref(ms), _stream_ptr(stream)))
+    return {"tflops": fl.value / (ms.value * 1e-3) / 1e12, "flops": fl.value, "ms": ms.value}
 
 
 def _opts(precision=None, traversal=None, block_size=None, sort_queries=None, beta=None,

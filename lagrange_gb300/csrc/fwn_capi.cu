@@ -44,6 +44,31 @@ cudaMemPool_t scratch_pool(int dev) {
 }
 }  // namespace
 
+// Usage of the scratch pool of `dev` (zeros when no call has created it yet); reset_high
+// restarts the high-water mark of used bytes from the current value.
+void scratch_pool_stats(int dev, bool reset_high, uint64_t* reserved, uint64_t* used,
+                        uint64_t* used_high) {
+    if (dev < 0 || dev >= kMaxDevices) throw Error(FWN_INVALID_ARG, "device ordinal out of range");
+    cudaMemPool_t pool = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_pool_mutex);
+        pool = g_pools[dev];
+    }
+    uint64_t r = 0, u = 0, h = 0;
+    if (pool) {
+        if (reset_high) {
+            uint64_t zero = 0;
+            FWN_CUDA_CHECK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &zero));
+        }
+        FWN_CUDA_CHECK(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &r));
+        FWN_CUDA_CHECK(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &u));
+        FWN_CUDA_CHECK(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemHigh, &h));
+    }
+    if (reserved) *reserved = r;
+    if (used) *used = u;
+    if (used_high) *used_high = h;
+}
+
 void* scratch_alloc(size_t bytes, cudaStream_t st) {
     void* p = nullptr;
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -430,6 +455,25 @@ FWN_API fwn_status fwn_forest_query(fwn_handle h, const float* d_points, const i
         check_points(qoff[e->nmeshes], d_points);
         QueryArgs a = resolve_query_args(*e, opts);
         query_forest(*e, a, d_points, qoff, d_omega, d_inside, static_cast<cudaStream_t>(stream));
+    });
+}
+
+FWN_API fwn_status fwn_scratch_pool_stats(int32_t device, int32_t reset_high,
+                                          uint64_t* reserved_bytes, uint64_t* used_bytes,
+                                          uint64_t* used_high_bytes) {
+    return guarded([&] {
+        scratch_pool_stats(device, reset_high != 0, reserved_bytes, used_bytes, used_high_bytes);
+    });
+}
+
+FWN_API fwn_status fwn_forest_sort_key_bits(int64_t num_meshes, const int64_t* qoff,
+                                            int32_t* key_bits) {
+    return guarded([&] {
+        if (num_meshes < 1 || !qoff || !key_bits) throw Error(FWN_INVALID_ARG, "bad arguments");
+        if (qoff[0] != 0) throw Error(FWN_INVALID_ARG, "query offsets must start at 0");
+        for (int64_t m = 0; m < num_meshes; ++m)
+            if (qoff[m + 1] < qoff[m]) throw Error(FWN_INVALID_ARG, "query offsets must not decrease");
+        *key_bits = forest_keys(num_meshes, qoff).key_bits;
     });
 }
 

@@ -975,6 +975,22 @@ void query_grid(const Engine& e, int mesh, const QueryArgs& a, const float origi
     FWN_CUDA_CHECK(cudaGetLastError());
 }
 
+// 32-bit keys (mesh id above the top hb bits of the Hilbert index) whenever every mesh keeps at
+// least 8 curve cells per query at that level, else 64-bit keys with all 30 bits. A 32-bit pass
+// moves 20 B per key against 32 B, and 39 key bits would need a fifth pass.
+ForestKeys forest_keys(int64_t nmeshes, const int64_t* query_offsets) {
+    ForestKeys k;
+    while ((1ll << k.mesh_bits) < nmeshes) ++k.mesh_bits;
+    int64_t max_q = 0;
+    for (int64_t m = 0; m < nmeshes; ++m)
+        max_q = std::max(max_q, query_offsets[m + 1] - query_offsets[m]);
+    const int hb = std::min(30, 32 - k.mesh_bits);
+    k.narrow = hb >= 30 || (hb >= 3 && max_q <= (int64_t(1) << (hb - 3)));
+    k.hilbert_bits = k.narrow ? hb : 30;
+    k.key_bits = k.mesh_bits + k.hilbert_bits;
+    return k;
+}
+
 void query_forest(const Engine& e, const QueryArgs& a, const float* d_points,
                   const int64_t* query_offsets, float* d_omega, uint8_t* d_inside,
                   cudaStream_t st) {
@@ -992,8 +1008,9 @@ void query_forest(const Engine& e, const QueryArgs& a, const float* d_points,
     }
     if (!e.nodes32) throw Error(FWN_INVALID_ARG, "engine was built without FP32 records (FWN_RECORDS_F32)");
     if (n > (int64_t)UINT32_MAX) throw Error(FWN_INVALID_ARG, "too many forest queries");
-    int mesh_bits = 0;
-    while ((1ll << mesh_bits) < e.nmeshes) ++mesh_bits;
+    const ForestKeys fk = forest_keys(e.nmeshes, query_offsets);
+    const int mesh_bits = fk.mesh_bits, hb = fk.hilbert_bits;
+    const bool narrow = fk.narrow;
     const size_t nb = (size_t)n;
     const size_t bytes = 256 + (e.nmeshes + 1) * sizeof(int64_t) + 2 * nb * sizeof(uint64_t) +
                          2 * nb * sizeof(uint32_t) + radix_sort_temp_bytes(n, 8) + 1024;
@@ -1009,14 +1026,6 @@ void query_forest(const Engine& e, const QueryArgs& a, const float* d_points,
     FWN_CUDA_CHECK(cudaMemsetAsync(d_status, 0, 2 * sizeof(unsigned), st));
     FWN_CUDA_CHECK(cudaMemcpyAsync(d_qoff, query_offsets, (e.nmeshes + 1) * sizeof(int64_t),
                                    cudaMemcpyHostToDevice, st));
-    // 32-bit keys (mesh id above the top hb bits of the Hilbert index) whenever every mesh keeps
-    // at least 8 curve cells per query at that level, else 64-bit keys with all 30 bits. A
-    // 32-bit pass moves 20 B per key against 32 B, and 39 key bits would need a fifth pass.
-    int64_t max_q = 0;
-    for (int64_t m = 0; m < e.nmeshes; ++m)
-        max_q = std::max(max_q, query_offsets[m + 1] - query_offsets[m]);
-    const int hb = std::min(30, 32 - mesh_bits);
-    const bool narrow = hb >= 30 || (hb >= 3 && max_q <= (int64_t(1) << (hb - 3)));
     const uint32_t* order = nullptr;
     if (narrow) {
         uint32_t* ka32 = reinterpret_cast<uint32_t*>(ka);  // the 64-bit key areas hold n u32 each

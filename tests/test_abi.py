@@ -83,3 +83,25 @@ def test_host_mesh_validation():
         fwn.FastWindingNumber(np.zeros((4, 2), np.float32), np.zeros((1, 3), np.int32))
     with pytest.raises(fwn.WindingError, match="triangle"):
         fwn.FastWindingNumber(np.zeros((4, 3), np.float32), np.zeros((1, 4), np.int32))
+
+
+def test_forest_sort_key_bits(engine_lib):
+    """The forest query's sort-key width comes from the library itself (host-only entry point),
+    so the bench's launch count follows the rule the query applies."""
+    def offsets(counts):
+        return np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+
+    assert fwn.forest_sort_key_bits(offsets([10**9])) == 30            # one mesh: Hilbert index
+    assert fwn.forest_sort_key_bits(offsets([10**9, 0, 0, 0])) == 32   # 2 mesh bits + 30
+    big = [0] * 512
+    big[7] = 1 << 20                                                   # 9 mesh bits + 23 bits:
+    assert fwn.forest_sort_key_bits(offsets(big)) == 32                # 8 cells per query
+    big[7] = (1 << 20) + 1
+    assert fwn.forest_sort_key_bits(offsets(big)) == 39                # too coarse: 64-bit keys
+    assert fwn.forest_sort_key_bits(offsets([1 << 26, 0, 0, 0, 5])) == 32
+    assert fwn.forest_sort_key_bits(offsets([1 << 26, 0, 0, 0, (1 << 26) + 1])) == 33
+    L = fwn.library()
+    bad = np.array([0, 5, 3], np.int64)
+    kb = C.c_int32(0)
+    assert L.fwn_forest_sort_key_bits(2, bad.ctypes.data_as(C.c_void_p), C.byref(kb)) == 1
+    assert L.fwn_forest_sort_key_bits(0, bad.ctypes.data_as(C.c_void_p), C.byref(kb)) == 1

@@ -56,14 +56,3 @@ def test_two_gloo_ranks(tmp_path):
     assert r[0]["first"] != r[1]["first"]
     assert r[0]["near_ok"] and r[1]["near_ok"]  # masks follow their points
     assert r[0]["value"] == pytest.approx(2 * 64 / 1.5)
-
-
-def test_forest_sort_key_bits():
-    """The bench counts the forest query's sort passes with the library's key-width rule."""
-    import bench
-    assert bench.forest_sort_key_bits(1, 10**9) == 30         # one mesh: the Hilbert index alone
-    assert bench.forest_sort_key_bits(4, 10**9) == 32         # 2 mesh bits + all 30 bits
-    assert bench.forest_sort_key_bits(512, 1 << 20) == 32     # 9 mesh bits + 23, 8 cells per query
-    assert bench.forest_sort_key_bits(512, (1 << 20) + 1) == 39  # too coarse: 64-bit keys
-    assert bench.forest_sort_key_bits(5, 1 << 26) == 32
-    assert bench.forest_sort_key_bits(5, (1 << 26) + 1) == 33

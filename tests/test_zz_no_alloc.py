@@ -102,3 +102,39 @@ def test_noalloc_at_the_size_limit_and_beyond():
     assert "FWN_NOALLOC_MAX_POINTS" in buf.value.decode()
     # no handle: NOT_BUILT
     assert L.fwn_query_noalloc(None, _ptr(Qbig), 1, _ptr(out), None, stream) == 6
+
+
+def test_noalloc_allocates_nothing():
+    """A warm fwn_query_noalloc call takes no memory from anywhere: the device's free memory
+    (cudaMemGetInfo) and the library's scratch pool (reserved bytes, and the high-water mark of
+    handed-out bytes, restarted just before) are unchanged across two calls. fwn_query, which
+    does take stream-ordered scratch, moves the high-water mark: the check can see an allocation."""
+    import torch
+    torch.cuda.set_device(0)
+    L = fwn.library()
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    wl = W.displaced_icosphere_workload(nu=32, n_queries=200_000)
+    eng = fwn.FastWindingNumber(wl.V, wl.F)
+    Q = torch.from_numpy(wl.Q).cuda()
+    n = Q.shape[0]
+    w = torch.empty(n, dtype=torch.float32, device="cuda")
+    ins = torch.empty(n, dtype=torch.uint8, device="cuda")
+    fwn._check(L.fwn_query(eng.handle, _ptr(Q), n, _ptr(w), _ptr(ins), stream))  # pool exists
+    fwn._check(L.fwn_query_noalloc(eng.handle, _ptr(Q), n, _ptr(w), _ptr(ins), stream))  # warm
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    p0 = fwn.scratch_pool_stats(0, reset_high=True)
+    assert p0["reserved"] > 0 and p0["used_high"] == p0["used"]
+    for _ in range(2):
+        fwn._check(L.fwn_query_noalloc(eng.handle, _ptr(Q), n, _ptr(w), _ptr(ins), stream))
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    p1 = fwn.scratch_pool_stats(0)
+    assert free1 == free0
+    assert p1["reserved"] == p0["reserved"]
+    assert p1["used"] == p0["used"] and p1["used_high"] == p0["used"]
+    # the same probe sees the ordinary query's scratch
+    fwn._check(L.fwn_query(eng.handle, _ptr(Q), n, _ptr(w), _ptr(ins), stream))
+    torch.cuda.synchronize()
+    p2 = fwn.scratch_pool_stats(0)
+    assert p2["used_high"] > p0["used"]
