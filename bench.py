@@ -54,9 +54,8 @@ BYTES_TRI = 48
 BYTES_QUERY_IO = 12 + 4 + 1 + 4  # point in, Omega + inside out, sort index
 CPU_LEAF = 8  # leaf size of the CPU restatement of the reference tree, in every CPU timing
 # DRAM bytes (read + write) of one traversal launch, keyed by (workload, leaf size, warp-schedule
-# variant), from the
-# one-pass ncu captures of the same command lines (profiles/k_query_warp_traffic_icosphere2m_q10m.md);
-# other workloads and leaf sizes: not captured (traffic null)
+# variant), from one-pass ncu captures (gpu__time_duration, dram__bytes_read/write) of the same
+# bench command lines; other workloads and leaf sizes: not captured (traffic null)
 NCU_TRAFFIC = {("displaced_icosphere_nu316_q10000000", 8, 4): 1.44e9 + 351.02e6,
                ("displaced_icosphere_nu316_q10000000", 12, 4): 1.37e9 + 334.33e6,
                ("displaced_icosphere_nu316_q10000000", 16, 4): 1.35e9 + 330.50e6}
@@ -85,6 +84,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-clocks", action="store_true")
     p.add_argument("--no-graph", action="store_true")  # time plain launches instead of a graph
+    p.add_argument("--no-batched", action="store_true")  # default line without forest/soup parts
     return p.parse_args()
 
 
@@ -129,18 +129,6 @@ def rank0_choice(dist, values, device=None):
     return [int(v) for v in t.tolist()]
 
 
-def forest_sort_key_bits(num_meshes: int, max_queries_per_mesh: int) -> int:
-    """Key bits of the forest query's radix sort (8 bits per pass), as the library chooses them:
-    32-bit keys (mesh id above the top hb bits of the 30-bit Hilbert index) while every mesh
-    keeps at least 8 curve cells per query at that level, else 64-bit keys (mesh id above all
-    30 bits)."""
-    mesh_bits = max(0, (num_meshes - 1).bit_length())
-    hb = min(30, 32 - mesh_bits)
-    if hb >= 30 or (hb >= 3 and max_queries_per_mesh <= 1 << (hb - 3)):
-        return mesh_bits + hb
-    return 30 + mesh_bits
-
-
 def rank_queries(Q, near_mask, rank: int):
     """The query set a rank answers (weak scaling: every rank has a full-size set). Rank 0 uses
     the workload as generated; rank r > 0 a seeded shuffle of it (different points per warp,
@@ -157,12 +145,29 @@ def job_value(per_rank_units: int, world: int, max_seconds: float) -> float:
 
 
 # ---------------------------------------------------------------------------------------------
+def smi_gpu_id(local: int) -> str:
+    """nvidia-smi's --id for CUDA device `local` of this process. nvidia-smi numbers GPUs by
+    physical index, which differs from the CUDA ordinal under CUDA_VISIBLE_DEVICES or a leased
+    subset, so the device is named by its UUID (falling back to the visible-devices mapping)."""
+    try:
+        import torch
+        u = str(torch.cuda.get_device_properties(local).uuid)
+        if u and u != "None":
+            return u if u.startswith(("GPU-", "MIG-")) else "GPU-" + u
+    except Exception:
+        pass
+    vis = [x.strip() for x in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if x.strip()]
+    if local < len(vis):
+        return vis[local]
+    return str(local)
+
+
 class Clocks:
-    """nvidia-smi sampling (200 ms) during the timed region."""
+    """nvidia-smi sampling (200 ms) during the timed region, of the GPU this process runs on."""
 
     def __init__(self, enabled: bool, index: int):
         self.enabled = enabled
-        self.index = index
+        self.index = smi_gpu_id(index) if enabled else str(index)
         self.proc = None
         self.path = Path(tempfile.gettempdir()) / f"fwn_clocks_{os.getpid()}.csv"
 
@@ -258,6 +263,20 @@ def autotune_choice(fwn, Vd, Fd, Qd, sample: int = 16_000_000, seed: int = 5):
     return r["leaf_size"], r["traversal"], r["block_size"], r["tuning"], summary
 
 
+def percentiles(x):
+    """p50/p90/p99/p99.9/max of a device tensor (quantiles of a 4M-element sample above that)."""
+    import torch
+    if x.numel() == 0:
+        return None
+    mx = float(x.max())
+    if x.numel() > 4_000_000:
+        g = torch.Generator(device=x.device).manual_seed(3)
+        x = x[torch.randperm(x.numel(), device=x.device, generator=g)[:4_000_000]]
+    qs = torch.tensor([0.5, 0.9, 0.99, 0.999], dtype=x.dtype, device=x.device)
+    v = torch.quantile(x, qs).tolist()
+    return {"p50": v[0], "p90": v[1], "p99": v[2], "p99.9": v[3], "max": mx}
+
+
 def cpu_sample(wl, size: int, seed: int = 7):
     """A bounded sample of the workload's queries: half far/box, half near-surface when the
     workload has both kinds, else uniform."""
@@ -320,6 +339,132 @@ def run_reference(args, rank, world):
 
 
 # ---------------------------------------------------------------------------------------------
+def measure_soup(dev, *, steps=5, warmup=3, cpu=True):
+    """The defective soup (the displaced icosphere at frequency 224 with 10% of faces deleted, 1%
+    flipped, 0.5% duplicated with 1e-7 jitter; 5M queries, half in the box, half within 1e-4 of
+    the surface). Reports the mixed engine's queries/s, its |dw| distribution split near/far
+    against the plain FP64 form on every point and against the FP64 brute force on a stratified
+    sample, and is_inside against the CPU restatement of the reference on every point."""
+    import torch
+    import lagrange_gb300 as fwn
+    from lagrange_gb300 import workloads as W
+    t0 = time.perf_counter()
+    wl = W.defective_soup_workload()
+    gen_s = time.perf_counter() - t0
+    n = len(wl.Q)
+    Vd, Fd, Qd = (torch.from_numpy(a).to(dev) for a in (wl.V, wl.F, wl.Q))
+    leaf, trav, block, tuning, tuned = autotune_choice(fwn, Vd, Fd, Qd)
+    eng = fwn.FastWindingNumber(Vd, Fd, leaf_size=leaf, traversal=trav, block_size=block,
+                                tuning=tuning, records=fwn.RECORDS_F32 | fwn.RECORDS_F64)
+    L = fwn.library()
+    stream = torch.cuda.current_stream(dev)
+    sptr = C.c_void_p(stream.cuda_stream)
+    w = torch.empty(n, dtype=torch.float32, device=dev)
+    ins = torch.empty(n, dtype=torch.uint8, device=dev)
+    w64 = torch.empty(n, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    om = fwn._opts(precision=fwn.PRECISION_MIXED, traversal=trav, block_size=block, tuning=tuning)
+    o64 = fwn._opts(precision=fwn.PRECISION_FP64)
+
+    def q_mixed():
+        fwn._check(L.fwn_query_ex(eng.handle, C.byref(om), C.c_void_p(Qd.data_ptr()), n,
+                                  C.c_void_p(w.data_ptr()), C.c_void_p(ins.data_ptr()), None, None,
+                                  sptr))
+
+    def q_fp64():
+        fwn._check(L.fwn_query_ex(eng.handle, C.byref(o64), C.c_void_p(Qd.data_ptr()), n, None,
+                                  None, C.c_void_p(w64.data_ptr()), None, sptr))
+
+    def timed(fn, k):
+        ts = []
+        for _ in range(k):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        return sum(ts) / len(ts)
+
+    for _ in range(warmup):
+        q_mixed()
+    torch.cuda.synchronize()
+    ms = timed(q_mixed, steps)
+    q_fp64()
+    ms64 = timed(q_fp64, 1)
+    q_mixed()
+    torch.cuda.synchronize()
+    near = torch.from_numpy(wl.near_mask).to(dev)
+    dw = (w.double() - w64).abs() / FOUR_PI
+    band64 = (w64 / FOUR_PI - 0.5).abs() > 1e-3
+    out = {
+        "workload": wl.name, "triangles": int(len(wl.F)), "queries": n, "generation_s": gen_s,
+        "leaf_size": leaf, "tuning": tuning, "autotuned": tuned,
+        "value": n / (ms / 1e3), "unit": "queries/s", "ms_per_step": ms, "steps": steps,
+        "build_ms": eng.info()["build_ms"],
+        "plain_fp64": {"value": n / (ms64 / 1e3), "ms": ms64, "speedup_mixed_over_fp64": ms64 / ms,
+                       "max_dw": float(dw.max()), "rms_dw": float(dw.pow(2).mean().sqrt()),
+                       "dw_percentiles": {"near": percentiles(dw[near]), "far": percentiles(dw[~near])},
+                       "gate_1e-4": bool(float(dw.max()) <= 1e-4),
+                       "inside_disagree_band": int(((ins.bool() != (w64 > 2 * math.pi)) & band64).sum())},
+    }
+    if cpu:
+        import oracle
+        nthr = oracle.nthreads_default()
+        wg, ig = w.cpu().numpy(), ins.cpu().numpy()
+        # FP64 brute force over all triangles on a stratified sample (1,024 far + 1,024 near)
+        bs = cpu_sample(wl, 2048, seed=11)
+        exact = oracle.brute_f64(wl.V, wl.F, bs, nthreads=nthr)
+        wb, _ = eng.query(torch.from_numpy(bs).to(dev), traversal=trav)
+        torch.cuda.synchronize()
+        dwb = np.abs(wb.cpu().numpy().astype(np.float64) - exact) / FOUR_PI
+        h = len(bs) // 2
+
+        def npct(x):
+            q = np.quantile(x, [0.5, 0.9, 0.99])
+            return {"p50": float(q[0]), "p90": float(q[1]), "p99": float(q[2]), "max": float(x.max())}
+        out["vs_brute_force_fp64"] = {"sample": len(bs), "far": npct(dwb[:h]), "near": npct(dwb[h:]),
+                                      "note": "includes the beta=2 far-field truncation error"}
+        # is_inside against the CPU restatement of the reference tree on every point
+        t0 = time.perf_counter()
+        ref = oracle.RefTree(wl.V, wl.F, leaf_size=CPU_LEAF)
+        om_ref, in_ref = ref.query(wl.Q, beta=wl.beta, nthreads=nthr)
+        cpu_s = time.perf_counter() - t0
+        band = np.abs(om_ref / FOUR_PI - 0.5) > 1e-3
+        dref = np.abs(wg.astype(np.float64) - om_ref) / FOUR_PI
+        out["inside_vs_reference"] = {
+            "points": n, "outside_band": int(band.sum()),
+            "disagree_outside_band": int(np.sum(ig[band] != in_ref[band])),
+            "max_dw_vs_reference_restatement": float(dref.max()),
+            "rms_dw_vs_reference_restatement": float(np.sqrt(np.mean(dref ** 2))),
+            "cpu_s": cpu_s}
+    eng.close()
+    del Vd, Fd, Qd, w, ins, w64, flush
+    return out
+
+
+def batched_summary(dev, *, steps=5, warmup=3, cpu=True):
+    """The 512-mesh forest (seed 3) inside the default line: its persistent CUDA-graph query,
+    build, meshes/s, per-mesh FP64 launches with max |dw| over every query, and is_inside against
+    the CPU restatement of the reference on sampled meshes."""
+    from lagrange_gb300 import workloads as W
+    t0 = time.perf_counter()
+    fo = W.batched_forest_workload()
+    gen_s = time.perf_counter() - t0
+    r = measure_forest(fo, dev, None, 0, 1, leaf=0, steps=steps, warmup=warmup, e2e=True, cpu=cpu,
+                       fp64=True, clocks=False, grid=False)
+    keep = ("value", "unit", "ms_per_step", "build_ms", "meshes_per_s_build_plus_query",
+            "gpu_launches", "sort_key_bits", "plain_fp64_per_mesh_launches", "cpu_baseline",
+            "inside_vs_reference")
+    out = {"metric": r["metric"], **{k: r[k] for k in keep if k in r}}
+    out["config"] = {**r["config"], "generation_s": gen_s}
+    if "e2e" in r:
+        out["e2e"] = {k: r["e2e"][k] for k in ("value", "unit", "ms_per_step", "h2d_bytes_per_step",
+                                                "d2h_bytes_per_step", "api")}
+    return out
+
+
 def run_ours(args, rank, world, local):
     import torch
     torch.cuda.set_device(local)
@@ -463,7 +608,11 @@ def run_ours(args, rank, world, local):
     l2_bytes = nodes * BYTES_NODE_TEST + far * BYTES_NODE_FAR + tri * BYTES_TRI + n * BYTES_QUERY_IO
     props = torch.cuda.get_device_properties(dev)
     sm_max = clocks.get("sm_max_mhz") or measured_peaks().get("sm_max_mhz") or 2070.0
-    peak_fp32 = props.multi_processor_count * 128 * 2 * sm_max * 1e6 / 1e12
+    peak_nominal = props.multi_processor_count * 128 * 2 * sm_max * 1e6 / 1e12
+    # the denominator, measured in this process on this GPU: FMA-throughput kernels in both FP32
+    # instruction forms (scalar and paired f32x2); the faster one is the FP32 peak
+    probes = {name: fwn.probe_fp32_peak(form, stream) for name, form in (("f32", 0), ("f32x2", 1))}
+    peak_fp32 = max(p["tflops"] for p in probes.values())
     achieved = flops / (kernel_ms / 1e3) / 1e12
     # the warp-schedule variant the traversal ran (tuning 0 resolves by batch size, as in the
     # library: two queries per lane once the batch fills every SM's warp slots four times)
@@ -475,8 +624,15 @@ def run_ours(args, rank, world, local):
         "frac": achieved / peak_fp32, "traffic": traffic,
         "kernel": "k_query_warp (traversal)", "variant": variant, "kernel_ms": kernel_ms,
         "kernel_share_of_step": kernel_ms / ms,
-        "peak_source": f"nominal FP32: {props.multi_processor_count} SMs x 128 lanes x 2 x "
-                       f"{sm_max:.0f} MHz (no FP32 figure in MEASURED_PEAKS.json)",
+        "peak_source": "measured in this run: fwn_probe_fp32_peak (full-occupancy grid of "
+                       "independent FMA chains, CUDA events, median of 5), the faster of the "
+                       "scalar and paired-f32x2 forms (MEASURED_PEAKS.json has no FP32 figure)",
+        "peak_measured": {k: v["tflops"] for k, v in probes.items()},
+        "peak_nominal": peak_nominal,
+        "traffic_source": (f"one-pass ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) "
+                           f"of the traversal launch of this workload at leaf {args.leaf}, "
+                           f"variant {variant}" if traffic else
+                           "null: no capture for this workload / leaf / variant"),
         "hbm": ({"achieved_gbs": traffic / (kernel_ms / 1e3) / 1e9, "peak_gbs": hbm_peak,
                  "frac": traffic / (kernel_ms / 1e3) / 1e9 / hbm_peak,
                  "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)"}
@@ -511,15 +667,7 @@ def run_ours(args, rank, world, local):
         torch.cuda.synchronize()
         dw = (w_out.double() - w64).abs() / FOUR_PI
         near = torch.from_numpy(wl.near_mask).to(dev)
-
-        def pct(x):
-            if x.numel() == 0:
-                return None
-            x = x[torch.randperm(x.numel(), device=x.device)[:4_000_000]] if x.numel() > 4_000_000 else x
-            qs = torch.tensor([0.5, 0.9, 0.99, 0.999], dtype=x.dtype, device=x.device)
-            return {"p50": float(torch.quantile(x, qs[0])), "p90": float(torch.quantile(x, qs[1])),
-                    "p99": float(torch.quantile(x, qs[2])), "p99.9": float(torch.quantile(x, qs[3])),
-                    "max": float(x.max())}
+        pct = percentiles
         result["plain_fp64"] = {
             "value": n / (ms64 / 1e3), "unit": "queries/s", "ms_per_step": ms64,
             "speedup_mixed_over_fp64": ms64 / ms,
@@ -641,6 +789,15 @@ def run_ours(args, rank, world, local):
                 "note": "GPU FP64 all-triangle sums (FP64 form, beta=1e30); the mixed and FP64 "
                         "forms carry the same beta=2 truncation error"}
 
+    # ---- the batched and defective-soup workloads (rank 0, N=1), after the headline ------------
+    if rank == 0 and world == 1 and not args.no_batched and args.workload == "icosphere":
+        eng.close()  # the headline's engine is done; the sub-workloads build their own
+        torch.cuda.empty_cache()
+        result["batched"] = batched_summary(dev, steps=min(args.steps, 5),
+                                            warmup=max(3, min(args.warmup, 5)), cpu=not args.no_cpu)
+        torch.cuda.empty_cache()
+        result["soup"] = measure_soup(dev, steps=min(args.steps, 5),
+                                      warmup=max(3, min(args.warmup, 5)), cpu=not args.no_cpu)
     if rank == 0:
         print(json.dumps(result), flush=True)
     barrier(dist)
@@ -657,13 +814,25 @@ def run_forest(args, rank, world, local):
     torch.cuda.set_device(local)
     dist = init_dist(world, "nccl")
     dev = torch.device("cuda", local)
-    import lagrange_gb300 as fwn
     from lagrange_gb300 import workloads as W
 
     t0 = time.perf_counter()
     fo = W.batched_forest_workload() if args.workload == "forest" else W.voxel_workload(
         nu=args.nu or 500)
     gen_s = time.perf_counter() - t0
+    result = measure_forest(fo, dev, dist, rank, world, leaf=args.leaf, steps=args.steps,
+                            warmup=args.warmup, e2e=not args.no_e2e, cpu=not args.no_cpu,
+                            fp64=not args.no_fp64, clocks=not args.no_clocks,
+                            grid=args.workload == "voxel", local=local)
+    result["config"]["generation_s"] = gen_s
+    return result
+
+
+def measure_forest(fo, dev, dist, rank, world, *, leaf=0, steps=10, warmup=3, e2e=True, cpu=True,
+                   fp64=True, clocks=True, grid=False, local=0):
+    """Measures one forest workload (see run_forest) and returns its result dict."""
+    import torch
+    import lagrange_gb300 as fwn
     M = len(fo.voff) - 1
     n = len(fo.Q)
     Vd = torch.from_numpy(fo.V).to(dev)
@@ -671,18 +840,18 @@ def run_forest(args, rank, world, local):
     Qd = torch.from_numpy(fo.Q).to(dev)
     L = fwn.library()
     tuned, tuning = None, 0
-    if args.leaf == 0:  # leaf size picked by the forest autotuner on this forest (untimed)
+    if leaf == 0:  # leaf size picked by the forest autotuner on this forest (untimed)
         r = fwn.autotune_forest(Vd, fo.voff, Fd, fo.foff, Qd, fo.qoff)
-        args.leaf, tuning = rank0_choice(dist, (r["leaf_size"], r["tuning"]), dev)
+        leaf, tuning = rank0_choice(dist, (r["leaf_size"], r["tuning"]), dev)
         tuned = {"leaf_size": r["leaf_size"], "tuning": r["tuning"],
                  "forest_query_ms": r["ms"], "candidates": r["candidates"]}
     builds = []
     for _ in range(3):
-        f2 = fwn.Forest(Vd, fo.voff, Fd, fo.foff, leaf_size=args.leaf, records=fwn.RECORDS_F32)
+        f2 = fwn.Forest(Vd, fo.voff, Fd, fo.foff, leaf_size=leaf, records=fwn.RECORDS_F32)
         builds.append(f2.info()["build_ms"])
         f2.close()
-    forest = fwn.Forest(Vd, fo.voff, Fd, fo.foff, leaf_size=args.leaf, tuning=tuning,
-                        records=fwn.RECORDS_F32 | (0 if args.no_fp64 else fwn.RECORDS_F64))
+    forest = fwn.Forest(Vd, fo.voff, Fd, fo.foff, leaf_size=leaf, tuning=tuning,
+                        records=fwn.RECORDS_F32 | (fwn.RECORDS_F64 if fp64 else 0))
     qoff = torch.from_numpy(fo.qoff.astype(np.int64)).pin_memory()  # pinned: capturable copy
     w = torch.empty(n, dtype=torch.float32, device=dev)
     ins = torch.empty(n, dtype=torch.uint8, device=dev)
@@ -696,7 +865,7 @@ def run_forest(args, rank, world, local):
     side = torch.cuda.Stream(dev)
     side.wait_stream(torch.cuda.current_stream(dev))
     with torch.cuda.stream(side):
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             q_mixed(C.c_void_p(side.cuda_stream))
     torch.cuda.synchronize()
     graph = torch.cuda.CUDAGraph()
@@ -707,8 +876,8 @@ def run_forest(args, rank, world, local):
     torch.cuda.synchronize()
     stream = torch.cuda.current_stream(dev)
     ts = []
-    with Clocks(not args.no_clocks and rank == 0, local) as clk:
-        for _ in range(args.steps):
+    with Clocks(clocks and rank == 0, local) as clk:
+        for _ in range(steps):
             flush.zero_()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
@@ -718,24 +887,24 @@ def run_forest(args, rank, world, local):
             ts.append(a.elapsed_time(b))
     ms = max_over_ranks(dist, sum(ts) / len(ts), dev)
     build_ms = min(builds)
-    key_bits = forest_sort_key_bits(M, int(np.diff(fo.qoff).max()))
+    key_bits = fwn.forest_sort_key_bits(fo.qoff)  # the library's own choice for these offsets
     launches_per_query = 1 + 3 * math.ceil(key_bits / 8) + 1  # keys, sort passes, walk
     result = {
         "metric": f"winding queries/s, {M} meshes in one persistent CUDA-graph launch",
         "value": job_value(n, world, ms / 1e3), "unit": "queries/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "steps": steps, "warmup": warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 near field/refit)",
         "data": "synthetic",
         "config": {"workload": fo.name, "meshes": M, "triangles": int(fo.foff[-1]),
-                   "queries": n, "beta": fo.beta, "leaf_size": args.leaf, "autotuned": tuned,
-                   "l2": "flushed before every step (256 MB write)", "generation_s": gen_s},
+                   "queries": n, "beta": fo.beta, "leaf_size": leaf, "autotuned": tuned,
+                   "l2": "flushed before every step (256 MB write)"},
         "build_ms": build_ms, "tree_nodes": forest.info()["num_nodes"],
         "meshes_per_s_build_plus_query": M / ((build_ms + ms) / 1e3),
-        "gpu_launches": launches_per_query * args.steps, "sort_key_bits": key_bits,
+        "gpu_launches": launches_per_query * steps, "sort_key_bits": key_bits,
         "clocks": clk.summary(),
     }
     # ---- end to end: pinned host points in, Omega + inside out, through fwn_forest_query ------
-    if not args.no_e2e:
+    if e2e:
         Qh = torch.from_numpy(fo.Q).pin_memory()
         wh = torch.empty(n, dtype=torch.float32).pin_memory()
         ih = torch.empty(n, dtype=torch.uint8).pin_memory()
@@ -758,7 +927,7 @@ def run_forest(args, rank, world, local):
             stream.synchronize()
         e2e_call()
         te, phases = [], {"h2d": [], "query": [], "d2h": []}
-        for _ in range(args.steps):
+        for _ in range(steps):
             flush.zero_()
             torch.cuda.synchronize()
             t0 = time.perf_counter()
@@ -774,11 +943,11 @@ def run_forest(args, rank, world, local):
                          "api": "fwn_forest_query (pinned host points copied in, results out)"}
         del Qe
     # ---- CPU restatement of the reference path on a few meshes (rank 0, N=1) ---------------
-    if rank == 0 and world == 1 and not args.no_cpu:
+    if rank == 0 and world == 1 and cpu:
         import oracle
         nthr = oracle.nthreads_default()
         rng = np.random.default_rng(21)
-        picks = [0] if args.workload == "voxel" else sorted(rng.choice(M, 4, replace=False).tolist())
+        picks = [0] if grid else sorted(rng.choice(M, 4, replace=False).tolist())
         wh_all, ih_all = w.cpu().numpy(), ins.cpu().numpy()
         nq_cpu, t_cpu, dis, maxdw, build_s = 0, 0.0, 0, 0.0, 0.0
         for m in picks:
@@ -803,7 +972,7 @@ def run_forest(args, rank, world, local):
                       f"single-thread, not in the rate)"}
         result["inside_vs_reference"] = {"sample": nq_cpu, "disagree_outside_band": dis,
                                          "max_dw_vs_reference_restatement": maxdw}
-    if args.workload == "voxel":
+    if grid:
         # the same classification through the grid sign pass: centres generated on the device,
         # no point array and no sort (one launch per mesh)
         res = round((fo.qoff[1] - fo.qoff[0]) ** (1 / 3))
@@ -827,7 +996,7 @@ def run_forest(args, rank, world, local):
         q_grid()
         torch.cuda.synchronize()
         tg = []
-        for _ in range(args.steps):
+        for _ in range(steps):
             flush.zero_()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
@@ -842,7 +1011,7 @@ def run_forest(args, rank, world, local):
             "inside_fraction": float(ig.float().mean()),
             "inside_fraction_explicit_points": float(ins.float().mean()),
             "h2d_bytes_per_step": 0}
-    if not args.no_fp64:
+    if fp64:
         w64 = torch.empty(n, dtype=torch.float32, device=dev)
         o64 = fwn._opts(precision=fwn.PRECISION_FP64)
         torch.cuda.synchronize()
@@ -863,11 +1032,7 @@ def run_forest(args, rank, world, local):
             "note": "FP64 output rounded to float; |dw| includes that rounding (<= 4e-8)",
             "inside_disagree_band": int(((ins.bool() != (w64.double() > 2 * math.pi)) & band).sum()),
         }
-    if rank == 0:
-        print(json.dumps(result), flush=True)
-    barrier(dist)
-    if dist is not None:
-        dist.destroy_process_group()
+    return result
 
 
 def main():
