@@ -37,17 +37,23 @@ __global__ void k_orient_points(const float* __restrict__ V, int64_t nv,
         const float* a = V + 3 * (int64_t)id[0];
         const float* b = V + 3 * (int64_t)id[1];
         const float* c = V + 3 * (int64_t)id[2];
-        const float ux = b[0] - a[0], uy = b[1] - a[1], uz = b[2] - a[2];
-        const float vx = c[0] - a[0], vy = c[1] - a[1], vz = c[2] - a[2];
-        float nx = uy * vz - uz * vy, ny = uz * vx - ux * vz, nz = ux * vy - uy * vx;
-        const float len = sqrtf(nx * nx + ny * ny + nz * nz);
+        // every float operation is rounded on its own, in the order written (no contraction into
+        // fused multiply-adds), as the example's host code evaluates it, so that a host
+        // restatement gives the same points bit for bit
+        const float ux = __fsub_rn(b[0], a[0]), uy = __fsub_rn(b[1], a[1]), uz = __fsub_rn(b[2], a[2]);
+        const float vx = __fsub_rn(c[0], a[0]), vy = __fsub_rn(c[1], a[1]), vz = __fsub_rn(c[2], a[2]);
+        float nx = __fsub_rn(__fmul_rn(uy, vz), __fmul_rn(uz, vy));
+        float ny = __fsub_rn(__fmul_rn(uz, vx), __fmul_rn(ux, vz));
+        float nz = __fsub_rn(__fmul_rn(ux, vy), __fmul_rn(uy, vx));
+        const float len = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(nx, nx), __fmul_rn(ny, ny)),
+                                               __fmul_rn(nz, nz)));
         if (len > 0.f) {
-            nx /= len;
-            ny /= len;
-            nz /= len;
+            nx = __fdiv_rn(nx, len);
+            ny = __fdiv_rn(ny, len);
+            nz = __fdiv_rn(nz, len);
         }
         const float n3[3] = {nx, ny, nz};
-        for (int k = 0; k < 3; ++k) {  // each operation rounded separately, as on the host
+        for (int k = 0; k < 3; ++k) {
             const float bary = __fdiv_rn(__fadd_rn(__fadd_rn(a[k], b[k]), c[k]), 3.0f);
             p[k] = __fadd_rn(bary, __fmul_rn(eps, n3[k]));
             m[k] = __fsub_rn(bary, __fmul_rn(eps, n3[k]));
