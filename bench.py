@@ -364,7 +364,7 @@ def measure_soup(dev, *, steps=5, warmup=3, cpu=True):
     w64 = torch.empty(n, dtype=torch.float64, device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     om = fwn._opts(precision=fwn.PRECISION_MIXED, traversal=trav, block_size=block, tuning=tuning)
-    o64 = fwn._opts(precision=fwn.PRECISION_FP64)
+    o64 = fwn._opts(precision=fwn.PRECISION_FP64, traversal=fwn.TRAVERSAL_THREAD)
 
     def q_mixed():
         fwn._check(L.fwn_query_ex(eng.handle, C.byref(om), C.c_void_p(Qd.data_ptr()), n,
@@ -646,7 +646,7 @@ def run_ours(args, rank, world, local):
     # ---- plain FP64 form + accuracy gate ----------------------------------------------------
     if not args.no_fp64:
         w64 = torch.empty(n, dtype=torch.float64, device=dev)
-        o64 = fwn._opts(precision=fwn.PRECISION_FP64)
+        o64 = fwn._opts(precision=fwn.PRECISION_FP64, traversal=fwn.TRAVERSAL_THREAD)
 
         def query_fp64():
             fwn._check(L.fwn_query_ex(eng.handle, C.byref(o64), C.c_void_p(Qd.data_ptr()), n,
@@ -679,7 +679,34 @@ def run_ours(args, rank, world, local):
             "inside_disagree_band": int(((i_out.bool() != (w64 > 2 * math.pi)) &
                                          ((w64 / FOUR_PI - 0.5).abs() > 1e-3)).sum()),
         }
-        del w64
+        # like-for-like: the FP64 form on the mixed form's warp schedule (same cursor and leaf
+        # pairs), so that the speed-up from precision alone is separated from the schedule
+        w64w = torch.empty(n, dtype=torch.float64, device=dev)
+        o64w = fwn._opts(precision=fwn.PRECISION_FP64, traversal=fwn.TRAVERSAL_WARP)
+
+        def query_fp64_warp():
+            fwn._check(L.fwn_query_ex(eng.handle, C.byref(o64w), C.c_void_p(Qd.data_ptr()), n,
+                                      None, None, C.c_void_p(w64w.data_ptr()), None, sptr))
+        query_fp64_warp()
+        torch.cuda.synchronize()
+        t64w = []
+        for _ in range(max(1, args.fp64_steps)):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            query_fp64_warp()
+            b.record(stream)
+            torch.cuda.synchronize()
+            t64w.append(a.elapsed_time(b))
+        ms64w = sum(t64w) / len(t64w)
+        result["plain_fp64"]["warp_schedule"] = {
+            "value": n / (ms64w / 1e3), "unit": "queries/s", "ms_per_step": ms64w,
+            "speedup_mixed_over_fp64_warp": ms64w / ms,
+            "speedup_warp_over_thread_fp64": ms64 / ms64w,
+            "max_abs_domega_vs_thread_fp64": float((w64w - w64).abs().max()),
+            "note": "FP64 records, Taylor terms and triangles on the mixed form's warp cursor "
+                    "(one query per lane); same per-query sums as the thread FP64 form"}
+        del w64, w64w
 
     # ---- e2e through the C ABI with host buffers ---------------------------------------------
     if not args.no_e2e:
@@ -761,17 +788,20 @@ def run_ours(args, rank, world, local):
         # of every leaf exactly in FP64. Checked against O1 on the CPU sample, then run on a
         # larger stratified sample.
         if not args.no_fp64 and args.brute_gpu > 0:
-            _, _, xb = eng.query(bq, precision=fwn.PRECISION_FP64, beta=1e30, omega_f64=True)
+            _, _, xb = eng.query(bq, precision=fwn.PRECISION_FP64,
+                                  traversal=fwn.TRAVERSAL_THREAD, beta=1e30, omega_f64=True)
             torch.cuda.synchronize()
             check = float(np.max(np.abs(xb.cpu().numpy() - exact)) / FOUR_PI)
             gs = cpu_sample(wl, min(args.brute_gpu, len(wl.Q)), seed=12)
             gq = torch.from_numpy(gs).to(dev)
             t0 = time.perf_counter()
-            _, _, xg = eng.query(gq, precision=fwn.PRECISION_FP64, beta=1e30, omega_f64=True)
+            _, _, xg = eng.query(gq, precision=fwn.PRECISION_FP64,
+                                  traversal=fwn.TRAVERSAL_THREAD, beta=1e30, omega_f64=True)
             torch.cuda.synchronize()
             bt = time.perf_counter() - t0
             wmg, _ = eng.query(gq, traversal=trav)
-            _, _, w64g = eng.query(gq, precision=fwn.PRECISION_FP64, omega_f64=True)
+            _, _, w64g = eng.query(gq, precision=fwn.PRECISION_FP64,
+                                  traversal=fwn.TRAVERSAL_THREAD, omega_f64=True)
             torch.cuda.synchronize()
             xg = xg.cpu().numpy()
             dg = np.abs(wmg.cpu().numpy().astype(np.float64) - xg) / FOUR_PI
@@ -1013,7 +1043,7 @@ def measure_forest(fo, dev, dist, rank, world, *, leaf=0, steps=10, warmup=3, e2
             "h2d_bytes_per_step": 0}
     if fp64:
         w64 = torch.empty(n, dtype=torch.float32, device=dev)
-        o64 = fwn._opts(precision=fwn.PRECISION_FP64)
+        o64 = fwn._opts(precision=fwn.PRECISION_FP64, traversal=fwn.TRAVERSAL_THREAD)
         torch.cuda.synchronize()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)

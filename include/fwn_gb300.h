@@ -61,9 +61,11 @@ enum {
     FWN_PRECISION_FP64 = 1   /* plain form: FP64 everywhere */
 };
 
-/* Traversal schedules of the mixed form. */
+/* Traversal schedules. AUTO is the warp schedule for the mixed form and the thread schedule
+ * (the plain form) for the FP64 form; the FP64 form runs on the warp schedule when WARP is asked
+ * for explicitly (same cursor and leaf pairs, FP64 arithmetic, same sums as the thread form). */
 enum {
-    FWN_TRAVERSAL_AUTO = 0,   /* autotuned choice (warp schedule until tuned) */
+    FWN_TRAVERSAL_AUTO = 0,   /* mixed: autotuned warp schedule; FP64: thread schedule */
     FWN_TRAVERSAL_THREAD = 1, /* one thread per query, stackless skip-link walk */
     FWN_TRAVERSAL_WARP = 2    /* warp-shared cursor over 32 queries, leaf triangles in smem */
 };

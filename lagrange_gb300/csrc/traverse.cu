@@ -701,6 +701,94 @@ k_query_f64(const NodeF64* __restrict__ nodes, const TriF32* __restrict__ tris, 
     if (STATS) flush_stats(qc, stats);
 }
 
+// ---- plain FP64 form on the warp-shared cursor ------------------------------------------------
+// The FP64 form on the schedule of the mixed warp walk (one query per lane): the same cursor,
+// far predicate and leaf pair distribution, with FP64 records, FP64 Taylor terms and FP64
+// triangle solid angles summed in DFS order as k_query_f64 sums them. Against k_query_f64 it
+// isolates what precision costs on the warp schedule; against the mixed warp walk it is the
+// like-for-like FP64 comparison.
+struct WarpSmem64 {
+    float4 leaf[WARP_LEAF_MAX * 3];
+    float4 q[32];
+    double res[32 * WARP_LEAF_MAX];
+};
+
+__global__ void __launch_bounds__(WARP_BLOCK)
+k_query_warp_f64(const NodeF64* __restrict__ nodes, const TriF32* __restrict__ tris,
+                 const MeshInfo mi, const float* __restrict__ Q, const uint32_t* __restrict__ order,
+                 int64_t n, float beta, float* __restrict__ omega, uint8_t* __restrict__ inside,
+                 double* __restrict__ omega64, unsigned* __restrict__ status) {
+    __shared__ WarpSmem64 smem[WARP_BLOCK / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t k = ((int64_t)blockIdx.x * (WARP_BLOCK / 32) + w) * 32 + lane;
+    if (k - lane >= n) return;  // whole warp out of range (warp-uniform)
+    WarpSmem64& sm = smem[w];
+    const bool valid = k < n;
+    const int64_t qi = valid ? (order ? (int64_t)order[k] : k) : -1;
+    const float qx = valid ? Q[3 * qi] : 0.f, qy = valid ? Q[3 * qi + 1] : 0.f,
+                qz = valid ? Q[3 * qi + 2] : 0.f;
+    const double dqx = qx, dqy = qy, dqz = qz;
+    const unsigned lt = lanemask_lt();
+    double s = 0.0;
+    int resume = valid ? mi.root : DONE;
+    if (resume >= mi.end) resume = DONE;
+    int cursor = __reduce_min_sync(0xffffffffu, resume);
+    while (cursor != DONE) {
+        const NodeF64* nd = nodes + cursor;
+        const double px = nd->P[0], py = nd->P[1], pz = nd->P[2];
+        const int skip = nd->skip, tb = nd->tri_begin, tc = nd->tri_count;
+        const bool active = resume == cursor;
+        float fdx, fdy, fdz, fd2;  // P, r and q are float values: the shared predicate
+        const bool far = far_pred((float)px, (float)py, (float)pz, (float)nd->r, qx, qy, qz, beta,
+                                  fdx, fdy, fdz, fd2);
+        int nr = (far || tc > 0) ? skip : cursor + 1;
+        nr = nr >= mi.end ? DONE : nr;
+        const bool do_far = active && far, need_leaf = active && !far && tc > 0;
+        if (active) resume = nr;
+        const int nc = __reduce_min_sync(0xffffffffu, resume);
+        if (__any_sync(0xffffffffu, do_far)) {
+            const double dx = px - dqx, dy = py - dqy, dz = pz - dqz;
+            const double t = taylor_f64(nd, dx, dy, dz, dx * dx + dy * dy + dz * dz);
+            if (do_far) s += t;
+        }
+        const unsigned lm = __ballot_sync(0xffffffffu, need_leaf);
+        if (lm) {
+            const int nl = __popc(lm);
+            const float4* src = reinterpret_cast<const float4*>(tris + tb);
+            for (int i = lane; i < 3 * tc; i += 32) sm.leaf[i] = __ldg(src + i);
+            if (need_leaf) sm.q[__popc(lm & lt)] = make_float4(qx, qy, qz, 0.f);
+            __syncwarp();
+            const int np = nl * tc;
+            for (int p = lane; p < np; p += 32) {
+                const int r = p / tc, t = p - r * tc;
+                const float4 q = sm.q[r];
+                const float4 t0 = sm.leaf[3 * t], t1 = sm.leaf[3 * t + 1], t2 = sm.leaf[3 * t + 2];
+                const double x = q.x, y = q.y, z = q.z;
+                sm.res[p] = tri_omega_f64((double)t0.x - x, (double)t0.y - y, (double)t0.z - z,
+                                          (double)t0.w - x, (double)t1.x - y, (double)t1.y - z,
+                                          (double)t1.z - x, (double)t1.w - y, (double)t2.x - z);
+            }
+            __syncwarp();
+            if (need_leaf) {
+                const int r = __popc(lm & lt);
+                for (int t = 0; t < tc; ++t) s += sm.res[r * tc + t];
+            }
+            __syncwarp();
+        }
+        if (nc <= cursor) {  // cannot happen for a well-formed tree
+            if (lane == 0) atomicOr(status, ST_BAD_LINK);
+            break;
+        }
+        cursor = nc;
+    }
+    if (valid) {
+        const float res = (float)s;
+        if (omega) omega[qi] = res;
+        if (omega64) omega64[qi] = s;
+        if (inside) inside[qi] = (double)res > TWO_PI_D ? 1 : 0;
+    }
+}
+
 // ---- query sort keys -------------------------------------------------------------------------
 __device__ __forceinline__ unsigned spread3q(unsigned x) {
     x &= 0x3ffu;
@@ -845,7 +933,10 @@ QueryArgs resolve_query_args(const Engine& e, const fwn_query_opts* o) {
     if (a.tuning < 0 || a.tuning > 5) throw Error(FWN_INVALID_ARG, "tuning must be in [0, 5]");
     if (a.precision != FWN_PRECISION_MIXED && a.precision != FWN_PRECISION_FP64)
         throw Error(FWN_INVALID_ARG, "unknown precision");
-    if (a.traversal == FWN_TRAVERSAL_AUTO) a.traversal = FWN_TRAVERSAL_WARP;
+    // AUTO: the warp walk for the mixed form; for the FP64 form the plain thread-per-query walk
+    // (the warp-schedule FP64 form runs when FWN_TRAVERSAL_WARP is asked for explicitly)
+    if (a.traversal == FWN_TRAVERSAL_AUTO)
+        a.traversal = a.precision == FWN_PRECISION_FP64 ? FWN_TRAVERSAL_THREAD : FWN_TRAVERSAL_WARP;
     if (a.traversal != FWN_TRAVERSAL_THREAD && a.traversal != FWN_TRAVERSAL_WARP)
         throw Error(FWN_INVALID_ARG, "unknown traversal");
     if (a.block_size <= 0) a.block_size = 128;
@@ -911,8 +1002,10 @@ void query_mesh(const Engine& e, int mesh, const QueryArgs& a, const float* d_po
     const bool want_stats = stats != nullptr;
     const int bs = a.block_size;
     if (a.precision == FWN_PRECISION_FP64) {
-        if (want_stats)
+        if (want_stats)  // counters: the thread walk (the counts do not depend on the schedule)
             k_query_f64<true><<<grid_for(n, 128), 128, 0, st>>>(e.nodes64, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_omega64, d_status, d_stats);
+        else if (a.traversal == FWN_TRAVERSAL_WARP)
+            k_query_warp_f64<<<grid_for(n, WARP_BLOCK), WARP_BLOCK, 0, st>>>(e.nodes64, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_omega64, d_status);
         else
             k_query_f64<false><<<grid_for(n, 128), 128, 0, st>>>(e.nodes64, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_omega64, d_status, d_stats);
     } else if (a.traversal == FWN_TRAVERSAL_WARP) {
@@ -1095,7 +1188,10 @@ void query_mesh_prealloc(const Engine& e, int mesh, const QueryArgs& a, const fl
     }
     const int bs = a.block_size;
     if (a.precision == FWN_PRECISION_FP64) {
-        k_query_f64<false><<<grid_for(n, 128), 128, 0, st>>>(e.nodes64, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, nullptr, d_status, nullptr);
+        if (a.traversal == FWN_TRAVERSAL_WARP)
+            k_query_warp_f64<<<grid_for(n, WARP_BLOCK), WARP_BLOCK, 0, st>>>(e.nodes64, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, nullptr, d_status);
+        else
+            k_query_f64<false><<<grid_for(n, 128), 128, 0, st>>>(e.nodes64, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, nullptr, d_status, nullptr);
     } else if (a.traversal == FWN_TRAVERSAL_WARP) {
         launch_query_warp_variant(warp_variant(a.tuning, n), e, mi, d_points, order, n, a.beta,
                                   d_omega, d_inside, d_status, st);

@@ -491,3 +491,25 @@ def test_warp_schedule_variants_agree(torch_cuda):
                                            None))
             torch.cuda.synchronize()
             np.testing.assert_array_equal(wn.cpu().numpy(), w)
+
+
+@pytest.mark.parametrize("leaf", [4, 12])
+def test_fp64_warp_schedule_matches_thread_form(torch_cuda, oracle_mod, leaf):
+    """The FP64 form on the warp cursor sums the same terms in the same order as the plain
+    thread form: equal to it to 1e-12 in w and within 1e-10 of the FP64 restatement (O3), near
+    the surface and in the box; at beta -> infinity within 1e-10 of the brute force (O1)."""
+    g = np.load(GOLDEN / "displaced.npz")
+    eng = _engine(g["V"], g["F"], leaf_size=leaf)
+    Q = g["Q"]
+    _, _, thr = _q(eng, torch_cuda, Q, precision=fwn.PRECISION_FP64,
+                   traversal=fwn.TRAVERSAL_THREAD, omega_f64=True)
+    w32, ins, wrp = _q(eng, torch_cuda, Q, precision=fwn.PRECISION_FP64,
+                       traversal=fwn.TRAVERSAL_WARP, omega_f64=True)
+    assert np.max(np.abs(wrp - thr)) / FOUR_PI <= 1e-12
+    o3 = oracle_mod.LbvhTree(g["V"], g["F"], leaf_size=leaf).query_f64(Q, beta=2.0)
+    assert np.max(np.abs(wrp - o3)) / FOUR_PI <= 1e-10
+    np.testing.assert_array_equal(w32, wrp.astype(np.float32))
+    np.testing.assert_array_equal(ins, (w32.astype(np.float64) > 2 * math.pi).astype(np.uint8))
+    _, _, wx = _q(eng, torch_cuda, Q, precision=fwn.PRECISION_FP64, traversal=fwn.TRAVERSAL_WARP,
+                  beta=1e30, omega_f64=True)
+    assert np.max(np.abs(wx - g["omega_exact"])) / FOUR_PI <= 1e-10
