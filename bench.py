@@ -571,7 +571,8 @@ def run_ours(args, rank, world, local):
                                             "device_bytes": info["device_bytes"]},
         "step_ms_min": min(step_ms), "step_ms_median": statistics.median(step_ms),
         "wall_s_timed": t_wall,
-        "gpu_launches": (1 + (4 * 3 + 1)) * args.steps,  # per step: 4 sort passes x3 + keys + traversal
+        # per step: keys + 4 sort passes x 3 kernels + traversal + result scatter
+        "gpu_launches": (1 + 4 * 3 + 1 + 1) * args.steps,
         "clocks": clocks,
     }
 
@@ -918,7 +919,7 @@ def measure_forest(fo, dev, dist, rank, world, *, leaf=0, steps=10, warmup=3, e2
     ms = max_over_ranks(dist, sum(ts) / len(ts), dev)
     build_ms = min(builds)
     key_bits = fwn.forest_sort_key_bits(fo.qoff)  # the library's own choice for these offsets
-    launches_per_query = 1 + 3 * math.ceil(key_bits / 8) + 1  # keys, sort passes, walk
+    launches_per_query = 1 + 3 * math.ceil(key_bits / 8) + 1 + 1  # keys, sort, walk, scatter
     result = {
         "metric": f"winding queries/s, {M} meshes in one persistent CUDA-graph launch",
         "value": job_value(n, world, ms / 1e3), "unit": "queries/s", "n_gpus": world,

@@ -521,13 +521,16 @@ __device__ __forceinline__ void write_result(const Slot& s, int64_t qi, float* _
     if (inside) inside[qi] = (double)res > TWO_PI_D ? 1 : 0;
 }
 
-// One mesh: each warp takes the next 32 * QPL queries of the (sorted) order.
+// One mesh: each warp takes the next 32 * QPL queries of the (sorted) order. With sorted_omega
+// the results go, coalesced, to position k of the sorted order (k_scatter_results then writes
+// them to the callers' indices in one pass); otherwise to the callers' indices directly.
 template <bool STATS, int MINB, int QPL>
 __global__ void __launch_bounds__(WARP_BLOCK, MINB)
 k_query_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
              const MeshInfo mi, const float* __restrict__ Q, const uint32_t* __restrict__ order,
              int64_t n, float beta, float* __restrict__ omega, uint8_t* __restrict__ inside,
-             unsigned* __restrict__ status, unsigned long long* __restrict__ stats) {
+             float* __restrict__ sorted_omega, unsigned* __restrict__ status,
+             unsigned long long* __restrict__ stats) {
     __shared__ WarpSmem<QPL> smem[WARP_BLOCK / 32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t base = ((int64_t)blockIdx.x * (WARP_BLOCK / 32) + w) * (32 * QPL);
@@ -550,9 +553,27 @@ k_query_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
     }
     warp_walk<STATS, QPL>(nodes, tris, sl, mi.cond, beta, smem[w], qc, status);
 #pragma unroll
-    for (int j = 0; j < QPL; ++j)
-        if (qi[j] >= 0) write_result(sl[j], qi[j], omega, inside);
+    for (int j = 0; j < QPL; ++j) {
+        if (qi[j] < 0) continue;
+        if (sorted_omega) sorted_omega[base + 32 * j + lane] = sl[j].s - sl[j].c;
+        else write_result(sl[j], qi[j], omega, inside);
+    }
     if (STATS) flush_stats(qc, stats);
+}
+
+// Writes the traversal's sorted-order results to the callers' indices: omega[order[k]] and
+// inside[order[k]] from sorted_omega[k]. Reads are coalesced; the scattered 4 B and 1 B writes of a
+// whole batch meet in L2 (one pass, with no tree traffic beside them), so partial sectors merge
+// before they reach DRAM instead of being evicted half-written during the walk.
+__global__ void k_scatter_results(const float* __restrict__ sorted_omega,
+                                  const uint32_t* __restrict__ order, int64_t n,
+                                  float* __restrict__ omega, uint8_t* __restrict__ inside) {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float res = sorted_omega[k];
+    const int64_t qi = order[k];
+    if (omega) omega[qi] = res;
+    if (inside) inside[qi] = (double)res > TWO_PI_D ? 1 : 0;
 }
 
 // Regular grid: voxel (i, j, k) has centre fmaf(i + 0.5, spacing, origin) per axis and output
@@ -603,8 +624,8 @@ k_forest_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris
               const MeshInfo* __restrict__ meshes, const float* __restrict__ Q,
               const int64_t* __restrict__ qoff, int nmeshes, const uint32_t* __restrict__ order,
               int64_t n, float beta, float cond, float* __restrict__ omega,
-              uint8_t* __restrict__ inside, unsigned* __restrict__ work,
-              unsigned* __restrict__ status) {
+              uint8_t* __restrict__ inside, float* __restrict__ sorted_omega,
+              unsigned* __restrict__ work, unsigned* __restrict__ status) {
     __shared__ WarpSmem<QPL> smem[WARP_BLOCK / 32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t nchunks = (n + 32 * QPL - 1) / (32 * QPL);
@@ -637,8 +658,11 @@ k_forest_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris
         }
         warp_walk<false, QPL>(nodes, tris, sl, cond, beta, smem[w], qc, status);
 #pragma unroll
-        for (int j = 0; j < QPL; ++j)
-            if (qi[j] >= 0) write_result(sl[j], qi[j], omega, inside);
+        for (int j = 0; j < QPL; ++j) {
+            if (qi[j] < 0) continue;
+            if (sorted_omega) sorted_omega[(int64_t)chunk * (32 * QPL) + 32 * j + lane] = sl[j].s - sl[j].c;
+            else write_result(sl[j], qi[j], omega, inside);
+        }
     }
 }
 
@@ -894,22 +918,29 @@ int warp_variant(int tuning, int64_t n) {
 template <int MINB, int QPL>
 void launch_query_warp(const Engine& e, const MeshInfo& mi, const float* d_points,
                        const uint32_t* order, int64_t n, float beta, float* d_omega,
-                       uint8_t* d_inside, unsigned* d_status, cudaStream_t st) {
+                       uint8_t* d_inside, float* sorted_omega, unsigned* d_status,
+                       cudaStream_t st) {
     k_query_warp<false, MINB, QPL><<<grid_for(n, WARP_BLOCK * QPL), WARP_BLOCK, 0, st>>>(
-        e.nodes32, e.tris, mi, d_points, order, n, beta, d_omega, d_inside, d_status, nullptr);
+        e.nodes32, e.tris, mi, d_points, order, n, beta, d_omega, d_inside, sorted_omega,
+        d_status, nullptr);
 }
 
+// The warp walk of one mesh's queries. With a sort order and a free n-float buffer
+// (sorted_omega), the results are written in sorted order and scattered to the callers'
+// indices by one k_scatter_results pass.
 void launch_query_warp_variant(int variant, const Engine& e, const MeshInfo& mi,
                                const float* d_points, const uint32_t* order, int64_t n,
                                float beta, float* d_omega, uint8_t* d_inside, unsigned* d_status,
-                               cudaStream_t st) {
+                               cudaStream_t st, float* sorted_omega = nullptr) {
+    float* so = (order && (d_omega || d_inside)) ? sorted_omega : nullptr;
     switch (variant) {
-        case 1: launch_query_warp<7, 1>(e, mi, d_points, order, n, beta, d_omega, d_inside, d_status, st); break;
-        case 2: launch_query_warp<1, 1>(e, mi, d_points, order, n, beta, d_omega, d_inside, d_status, st); break;
-        case 4: launch_query_warp<8, 2>(e, mi, d_points, order, n, beta, d_omega, d_inside, d_status, st); break;
-        case 5: launch_query_warp<6, 2>(e, mi, d_points, order, n, beta, d_omega, d_inside, d_status, st); break;
-        default: launch_query_warp<8, 1>(e, mi, d_points, order, n, beta, d_omega, d_inside, d_status, st); break;
+        case 1: launch_query_warp<7, 1>(e, mi, d_points, order, n, beta, d_omega, d_inside, so, d_status, st); break;
+        case 2: launch_query_warp<1, 1>(e, mi, d_points, order, n, beta, d_omega, d_inside, so, d_status, st); break;
+        case 4: launch_query_warp<8, 2>(e, mi, d_points, order, n, beta, d_omega, d_inside, so, d_status, st); break;
+        case 5: launch_query_warp<6, 2>(e, mi, d_points, order, n, beta, d_omega, d_inside, so, d_status, st); break;
+        default: launch_query_warp<8, 1>(e, mi, d_points, order, n, beta, d_omega, d_inside, so, d_status, st); break;
     }
+    if (so) k_scatter_results<<<grid_for(n, 256), 256, 0, st>>>(so, order, n, d_omega, d_inside);
 }
 
 }  // namespace
@@ -987,6 +1018,7 @@ void query_mesh(const Engine& e, int mesh, const QueryArgs& a, const float* d_po
         return;
     }
     const uint32_t* order = nullptr;
+    float* sorted_omega = nullptr;  // the sorted keys' buffer, free once the sort is done
     const bool do_sort = a.sort_queries && n > 1;
     Scratch sortbuf(do_sort ? 4 * (size_t)n * sizeof(uint32_t) + radix_sort_temp_bytes(n, 4) + 256 : 0, st);
     if (do_sort) {
@@ -998,6 +1030,7 @@ void query_mesh(const Engine& e, int mesh, const QueryArgs& a, const float* d_po
         k_query_keys<<<grid_for(n, 256), 256, 0, st>>>(d_points, n, mi, ka, va);
         const bool in_b = radix_sort_u32(ka, va, kb, vb, n, 30, tmp, st);
         order = in_b ? vb : va;
+        sorted_omega = reinterpret_cast<float*>(in_b ? kb : ka);
     }
     const bool want_stats = stats != nullptr;
     const int bs = a.block_size;
@@ -1010,10 +1043,10 @@ void query_mesh(const Engine& e, int mesh, const QueryArgs& a, const float* d_po
             k_query_f64<false><<<grid_for(n, 128), 128, 0, st>>>(e.nodes64, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_omega64, d_status, d_stats);
     } else if (a.traversal == FWN_TRAVERSAL_WARP) {
         if (want_stats)  // counters: one query per lane, no register cap
-            k_query_warp<true, 1, 1><<<grid_for(n, WARP_BLOCK), WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, d_stats);
+            k_query_warp<true, 1, 1><<<grid_for(n, WARP_BLOCK), WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, nullptr, d_status, d_stats);
         else
             launch_query_warp_variant(warp_variant(a.tuning, n), e, mi, d_points, order, n, a.beta,
-                                      d_omega, d_inside, d_status, st);
+                                      d_omega, d_inside, d_status, st, sorted_omega);
     } else {
         if (want_stats)
             k_query_thread<true><<<grid_for(n, bs), bs, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, d_stats);
@@ -1120,6 +1153,8 @@ void query_forest(const Engine& e, const QueryArgs& a, const float* d_points,
     FWN_CUDA_CHECK(cudaMemcpyAsync(d_qoff, query_offsets, (e.nmeshes + 1) * sizeof(int64_t),
                                    cudaMemcpyHostToDevice, st));
     const uint32_t* order = nullptr;
+    // after the sort, the first key area (n u32 at least) holds the sorted-order results
+    float* sorted_omega = (d_omega || d_inside) ? reinterpret_cast<float*>(ka) : nullptr;
     if (narrow) {
         uint32_t* ka32 = reinterpret_cast<uint32_t*>(ka);  // the 64-bit key areas hold n u32 each
         uint32_t* kb32 = reinterpret_cast<uint32_t*>(kb);
@@ -1145,7 +1180,9 @@ void query_forest(const Engine& e, const QueryArgs& a, const float* d_points,
     const unsigned grid = (unsigned)std::min<int64_t>(want, (int64_t)sms * std::max(per_sm, 1));
     kern<<<grid, WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, e.meshes, d_points, d_qoff,
                                       (int)e.nmeshes, order, n, a.beta, e.meshes_h[0].cond,
-                                      d_omega, d_inside, d_status + 1, d_status);
+                                      d_omega, d_inside, sorted_omega, d_status + 1, d_status);
+    if (sorted_omega)
+        k_scatter_results<<<grid_for(n, 256), 256, 0, st>>>(sorted_omega, order, n, d_omega, d_inside);
     FWN_CUDA_CHECK(cudaGetLastError());
 }
 
@@ -1176,6 +1213,7 @@ void query_mesh_prealloc(const Engine& e, int mesh, const QueryArgs& a, const fl
         return;
     }
     const uint32_t* order = nullptr;
+    float* sorted_omega = nullptr;  // the sorted keys' slot of the region, free after the sort
     if (a.sort_queries && n > 1) {
         uint32_t* ka = reinterpret_cast<uint32_t*>(base + 256);
         uint32_t* va = ka + n;
@@ -1185,6 +1223,7 @@ void query_mesh_prealloc(const Engine& e, int mesh, const QueryArgs& a, const fl
         k_query_keys<<<grid_for(n, 256), 256, 0, st>>>(d_points, n, mi, ka, va);
         const bool in_b = radix_sort_u32(ka, va, kb, vb, n, 30, tmp, st);
         order = in_b ? vb : va;
+        sorted_omega = reinterpret_cast<float*>(in_b ? kb : ka);
     }
     const int bs = a.block_size;
     if (a.precision == FWN_PRECISION_FP64) {
@@ -1194,7 +1233,7 @@ void query_mesh_prealloc(const Engine& e, int mesh, const QueryArgs& a, const fl
             k_query_f64<false><<<grid_for(n, 128), 128, 0, st>>>(e.nodes64, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, nullptr, d_status, nullptr);
     } else if (a.traversal == FWN_TRAVERSAL_WARP) {
         launch_query_warp_variant(warp_variant(a.tuning, n), e, mi, d_points, order, n, a.beta,
-                                  d_omega, d_inside, d_status, st);
+                                  d_omega, d_inside, d_status, st, sorted_omega);
     } else {
         k_query_thread<false><<<grid_for(n, bs), bs, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_status, nullptr);
     }
