@@ -11,6 +11,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include <stdexcept>
@@ -124,6 +125,18 @@ enum : unsigned {
     ST_NONFINITE = 2u,       // referenced vertex coordinate is NaN/inf
     ST_BAD_LINK = 4u,        // traversal met a skip link that does not advance
     ST_REFIT_ORPHAN = 8u     // refit ascent inconsistency
+};
+
+// ---------------------------------------------------------------------------------------------
+// Tracing: an NVTX range over a host-side phase (build stages, query sort / walk). The ranges
+// mark when each phase is enqueued; a profiler such as Nsight Systems lines them up with the
+// kernels they launch. Without a profiler attached an NVTX call returns at once.
+// ---------------------------------------------------------------------------------------------
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
 };
 
 // ---------------------------------------------------------------------------------------------

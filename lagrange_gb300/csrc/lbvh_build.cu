@@ -744,6 +744,7 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
     e.nf = nf;
     e.nmeshes = nmeshes;
     const int K = e.cfg.leaf_size;
+    NvtxRange trace_build("fwn build");
 
     cudaEvent_t ev0, ev1;
     FWN_CUDA_CHECK(cudaEventCreate(&ev0));
@@ -796,6 +797,7 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
         uint32_t* vals_a = (uint32_t*)track(dalloc<uint32_t>(n, st));
         uint32_t* vals_b = (uint32_t*)track(dalloc<uint32_t>(n, st));
         void* sort_tmp = track(dalloc<char>(radix_sort_temp_bytes(n, 8), st));
+        NvtxRange trace_keys("fwn build: Morton keys + sort");
         k_tri_keys<<<grid_for(n, 256), 256, 0, st>>>(d_V, d_F, voff, foff, (int)nmeshes, nf,
                                                      e.meshes, keys_a, vals_a, status);
         FWN_CUDA_CHECK(cudaGetLastError());
@@ -826,6 +828,7 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
         int* leaf_list_len = (int*)track(dalloc<int>(1, st));
         int* leaf_count = (int*)track(dalloc<int>(1, st));
 
+        NvtxRange trace_tree("fwn build: Karras tree + DFS layout");
         FWN_CUDA_CHECK(cudaMemsetAsync(parent, 0xff, (size_t)nn * sizeof(int), st));  // -1
         k_leaf_init<<<grid_for(n, 256), 256, 0, st>>>(n, first, last);
         if (n == 1) {
@@ -848,6 +851,7 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
         FWN_CUDA_CHECK(cudaStreamSynchronize(st));
         e.num_nodes = E;
 
+        NvtxRange trace_refit("fwn build: FP64 refit, radii, records");
         StageRec* stage = dalloc<StageRec>(E, st);
         if (!(e.cfg.records & FWN_RECORDS_MOMENTS)) track(stage);
         else e.stage = stage;

@@ -1002,6 +1002,7 @@ void query_mesh(const Engine& e, int mesh, const QueryArgs& a, const float* d_po
         throw Error(FWN_INVALID_ARG, "engine was built without FP64 records (FWN_RECORDS_F64)");
     if (a.precision == FWN_PRECISION_MIXED && !e.nodes32 && e.num_nodes > 0)
         throw Error(FWN_INVALID_ARG, "engine was built without FP32 records (FWN_RECORDS_F32)");
+    NvtxRange trace("fwn query");
     if (d_omega64 && a.precision != FWN_PRECISION_FP64)
         throw Error(FWN_INVALID_ARG, "FP64 solid-angle output needs the FP64 form");
     const MeshInfo& mi = e.meshes_h[mesh];
@@ -1078,6 +1079,7 @@ void query_grid(const Engine& e, int mesh, const QueryArgs& a, const float origi
     if (nx <= 0 || ny <= 0 || nz <= 0) return;
     const MeshInfo& mi = e.meshes_h[mesh];
     const int64_t n = nx * ny * nz;
+    NvtxRange trace("fwn grid query");
     if (mi.root < 0) {
         k_fill_zero<<<grid_for(n, 256), 256, 0, st>>>(d_omega, d_inside, nullptr, n);
         FWN_CUDA_CHECK(cudaGetLastError());
@@ -1134,6 +1136,7 @@ void query_forest(const Engine& e, const QueryArgs& a, const float* d_points,
     }
     if (!e.nodes32) throw Error(FWN_INVALID_ARG, "engine was built without FP32 records (FWN_RECORDS_F32)");
     if (n > (int64_t)UINT32_MAX) throw Error(FWN_INVALID_ARG, "too many forest queries");
+    NvtxRange trace("fwn forest query");
     const ForestKeys fk = forest_keys(e.nmeshes, query_offsets);
     const int mesh_bits = fk.mesh_bits, hb = fk.hilbert_bits;
     const bool narrow = fk.narrow;
