@@ -73,6 +73,7 @@ def parse():
     p.add_argument("--queries", type=int, default=None)
     p.add_argument("--leaf", type=int, default=0)  # 0: the autotuner picks (untimed)
     p.add_argument("--tuning", type=int, default=0)  # with --leaf: warp-schedule variant (0 auto)
+    p.add_argument("--builder", type=int, default=0)  # with --leaf: 0 LBVH, 1 top-down splits
     p.add_argument("--traversal", default="warp", choices=["thread", "warp"])
     p.add_argument("--block", type=int, default=128)
     p.add_argument("--fp64-steps", type=int, default=2)
@@ -245,7 +246,7 @@ def make_workload(args):
 
 def autotune_choice(fwn, Vd, Fd, Qd, sample: int = 16_000_000, seed: int = 5):
     """fwn_autotune on the workload's own queries (a seeded subsample above `sample` points):
-    returns (leaf, traversal, block, tuning, summary). Untimed; the bench then measures the
+    returns (leaf, traversal, block, tuning, builder, summary). Untimed; the bench then measures the
     chosen configuration. A subsample is sparser than the workload, so its warps are less
     coherent and it can favour larger leaves than the full query set does."""
     import torch
@@ -258,9 +259,9 @@ def autotune_choice(fwn, Vd, Fd, Qd, sample: int = 16_000_000, seed: int = 5):
         Qs = Qd
     r = fwn.autotune(Vd, Fd, Qs)
     summary = {"leaf_size": r["leaf_size"], "traversal": r["traversal"],
-               "block_size": r["block_size"], "tuning": r["tuning"],
+               "block_size": r["block_size"], "tuning": r["tuning"], "builder": r["builder"],
                "sample_ms": r["ms"], "candidates": r["candidates"], "sample": int(Qs.shape[0])}
-    return r["leaf_size"], r["traversal"], r["block_size"], r["tuning"], summary
+    return r["leaf_size"], r["traversal"], r["block_size"], r["tuning"], r["builder"], summary
 
 
 def percentiles(x):
@@ -353,9 +354,10 @@ def measure_soup(dev, *, steps=5, warmup=3, cpu=True):
     gen_s = time.perf_counter() - t0
     n = len(wl.Q)
     Vd, Fd, Qd = (torch.from_numpy(a).to(dev) for a in (wl.V, wl.F, wl.Q))
-    leaf, trav, block, tuning, tuned = autotune_choice(fwn, Vd, Fd, Qd)
+    leaf, trav, block, tuning, builder, tuned = autotune_choice(fwn, Vd, Fd, Qd)
     eng = fwn.FastWindingNumber(Vd, Fd, leaf_size=leaf, traversal=trav, block_size=block,
-                                tuning=tuning, records=fwn.RECORDS_F32 | fwn.RECORDS_F64)
+                                tuning=tuning, builder=builder,
+                                records=fwn.RECORDS_F32 | fwn.RECORDS_F64)
     L = fwn.library()
     stream = torch.cuda.current_stream(dev)
     sptr = C.c_void_p(stream.cuda_stream)
@@ -400,7 +402,7 @@ def measure_soup(dev, *, steps=5, warmup=3, cpu=True):
     band64 = (w64 / FOUR_PI - 0.5).abs() > 1e-3
     out = {
         "workload": wl.name, "triangles": int(len(wl.F)), "queries": n, "generation_s": gen_s,
-        "leaf_size": leaf, "tuning": tuning, "autotuned": tuned,
+        "leaf_size": leaf, "tuning": tuning, "builder": builder, "autotuned": tuned,
         "value": n / (ms / 1e3), "unit": "queries/s", "ms_per_step": ms, "steps": steps,
         "build_ms": eng.info()["build_ms"],
         "plain_fp64": {"value": n / (ms64 / 1e3), "ms": ms64, "speedup_mixed_over_fp64": ms64 / ms,
@@ -483,20 +485,22 @@ def run_ours(args, rank, world, local):
     Fd = torch.from_numpy(wl.F).to(dev)
     Qd = torch.from_numpy(wl.Q).to(dev)
     stream = torch.cuda.current_stream(dev)
-    leaf, block, tuning, tuned = args.leaf, args.block, args.tuning, None
+    leaf, block, tuning, builder, tuned = args.leaf, args.block, args.tuning, args.builder, None
     if leaf == 0:  # the autotuner's choice for this mesh and query distribution (untimed)
-        leaf, trav, block, tuning, tuned = autotune_choice(fwn, Vd, Fd, Qd)
-        leaf, trav, block, tuning = rank0_choice(dist, (leaf, trav, block, tuning), dev)
+        leaf, trav, block, tuning, builder, tuned = autotune_choice(fwn, Vd, Fd, Qd)
+        leaf, trav, block, tuning, builder = rank0_choice(dist, (leaf, trav, block, tuning, builder),
+                                                          dev)
     args.leaf, args.block = leaf, block
     # the handle's defaults are the chosen schedule too, so the host-buffer path (e2e) runs it
     eng = fwn.FastWindingNumber(Vd, Fd, leaf_size=args.leaf, traversal=trav, block_size=block,
-                                tuning=tuning,
+                                tuning=tuning, builder=builder,
                                 records=fwn.RECORDS_F32 | (0 if args.no_fp64 else fwn.RECORDS_F64))
     torch.cuda.synchronize()
     # build timing (device, CUDA events inside the library): best of 3 extra builds
     build_ms = []
     for _ in range(3):
-        e2 = fwn.FastWindingNumber(Vd, Fd, leaf_size=args.leaf, records=fwn.RECORDS_F32)
+        e2 = fwn.FastWindingNumber(Vd, Fd, leaf_size=args.leaf, builder=builder,
+                                   records=fwn.RECORDS_F32)
         build_ms.append(e2.info()["build_ms"])
         e2.close()
     info = eng.info()
@@ -562,6 +566,7 @@ def run_ours(args, rank, world, local):
         "data": "synthetic",
         "config": {"workload": wl.name, "triangles": int(len(wl.F)), "queries_per_gpu": n,
                    "beta": wl.beta, "leaf_size": args.leaf,
+                   "builder": "split" if builder == fwn.BUILDER_SPLIT else "lbvh",
                    "traversal": "warp" if trav == fwn.TRAVERSAL_WARP else "thread",
                    "block": args.block, "tuning": tuning, "autotuned": tuned,
                    "step": "plain launches" if args.no_graph else "CUDA graph of one query call",
@@ -851,7 +856,8 @@ def run_forest(args, rank, world, local):
     fo = W.batched_forest_workload() if args.workload == "forest" else W.voxel_workload(
         nu=args.nu or 500)
     gen_s = time.perf_counter() - t0
-    result = measure_forest(fo, dev, dist, rank, world, leaf=args.leaf, steps=args.steps,
+    result = measure_forest(fo, dev, dist, rank, world, leaf=args.leaf, builder=args.builder,
+                            steps=args.steps,
                             warmup=args.warmup, e2e=not args.no_e2e, cpu=not args.no_cpu,
                             fp64=not args.no_fp64, clocks=not args.no_clocks,
                             grid=args.workload == "voxel", local=local)
@@ -859,8 +865,8 @@ def run_forest(args, rank, world, local):
     return result
 
 
-def measure_forest(fo, dev, dist, rank, world, *, leaf=0, steps=10, warmup=3, e2e=True, cpu=True,
-                   fp64=True, clocks=True, grid=False, local=0):
+def measure_forest(fo, dev, dist, rank, world, *, leaf=0, builder=0, steps=10, warmup=3, e2e=True,
+                   cpu=True, fp64=True, clocks=True, grid=False, local=0):
     """Measures one forest workload (see run_forest) and returns its result dict."""
     import torch
     import lagrange_gb300 as fwn
@@ -871,17 +877,18 @@ def measure_forest(fo, dev, dist, rank, world, *, leaf=0, steps=10, warmup=3, e2
     Qd = torch.from_numpy(fo.Q).to(dev)
     L = fwn.library()
     tuned, tuning = None, 0
-    if leaf == 0:  # leaf size picked by the forest autotuner on this forest (untimed)
+    if leaf == 0:  # builder and leaf size picked by the forest autotuner on this forest (untimed)
         r = fwn.autotune_forest(Vd, fo.voff, Fd, fo.foff, Qd, fo.qoff)
-        leaf, tuning = rank0_choice(dist, (r["leaf_size"], r["tuning"]), dev)
-        tuned = {"leaf_size": r["leaf_size"], "tuning": r["tuning"],
+        leaf, tuning, builder = rank0_choice(dist, (r["leaf_size"], r["tuning"], r["builder"]), dev)
+        tuned = {"leaf_size": r["leaf_size"], "tuning": r["tuning"], "builder": r["builder"],
                  "forest_query_ms": r["ms"], "candidates": r["candidates"]}
     builds = []
     for _ in range(3):
-        f2 = fwn.Forest(Vd, fo.voff, Fd, fo.foff, leaf_size=leaf, records=fwn.RECORDS_F32)
+        f2 = fwn.Forest(Vd, fo.voff, Fd, fo.foff, leaf_size=leaf, builder=builder,
+                        records=fwn.RECORDS_F32)
         builds.append(f2.info()["build_ms"])
         f2.close()
-    forest = fwn.Forest(Vd, fo.voff, Fd, fo.foff, leaf_size=leaf, tuning=tuning,
+    forest = fwn.Forest(Vd, fo.voff, Fd, fo.foff, leaf_size=leaf, tuning=tuning, builder=builder,
                         records=fwn.RECORDS_F32 | (fwn.RECORDS_F64 if fp64 else 0))
     qoff = torch.from_numpy(fo.qoff.astype(np.int64)).pin_memory()  # pinned: capturable copy
     w = torch.empty(n, dtype=torch.float32, device=dev)
@@ -927,7 +934,8 @@ def measure_forest(fo, dev, dist, rank, world, *, leaf=0, steps=10, warmup=3, e2
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 near field/refit)",
         "data": "synthetic",
         "config": {"workload": fo.name, "meshes": M, "triangles": int(fo.foff[-1]),
-                   "queries": n, "beta": fo.beta, "leaf_size": leaf, "autotuned": tuned,
+                   "queries": n, "beta": fo.beta, "leaf_size": leaf,
+                   "builder": "split" if builder == fwn.BUILDER_SPLIT else "lbvh", "autotuned": tuned,
                    "l2": "flushed before every step (256 MB write)"},
         "build_ms": build_ms, "tree_nodes": forest.info()["num_nodes"],
         "meshes_per_s_build_plus_query": M / ((build_ms + ms) / 1e3),

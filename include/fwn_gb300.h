@@ -70,6 +70,15 @@ enum {
     FWN_TRAVERSAL_WARP = 2    /* warp-shared cursor over 32 queries, leaf triangles in smem */
 };
 
+/* Tree builders. Both give a binary tree in DFS order with leaves of <= leaf_size triangles and
+ * the same refit; they differ in how the triangles are grouped. */
+enum {
+    FWN_BUILDER_LBVH = 0,  /* 30-bit Morton codes, device radix sort, Karras 2012 hierarchy */
+    FWN_BUILDER_SPLIT = 1  /* top-down: split each node's centroid box at the midpoint of its
+                              longest axis (level by level on the device); fewer, more compact
+                              nodes: ~15% fewer far tests per query, a slower build */
+};
+
 /* Which node-record sets a build keeps (bit mask). */
 enum {
     FWN_RECORDS_F32 = 1, /* 128 B FP32 records for the mixed form */
@@ -93,7 +102,8 @@ typedef struct fwn_config {
                               register cap. 1: 1 query per lane, 72 registers; 2: 1, no cap;
                               3: 1, 64 registers; 4: 2 queries per lane, 64 registers; 5: 2, 80.
                               0 (default): 4 for batches that fill the GPU, else 3 */
-    int32_t reserved[6];
+    int32_t builder;       /* FWN_BUILDER_*. Default FWN_BUILDER_LBVH */
+    int32_t reserved[5];
 } fwn_config;
 
 /* Per-query options (override the handle's defaults; pass NULL for defaults). */
@@ -117,7 +127,8 @@ typedef struct fwn_query_stats {
                                   nodes_tested / (32 * warp_steps) = lane utilisation */
 } fwn_query_stats;
 
-/* Result of fwn_autotune: the fastest (leaf_size, traversal, block_size, tuning) on the sample. */
+/* Result of fwn_autotune: the fastest (builder, leaf_size, traversal, block_size, tuning) on the
+ * sample. */
 typedef struct fwn_tune_result {
     int32_t leaf_size;
     int32_t traversal;
@@ -126,7 +137,8 @@ typedef struct fwn_tune_result {
     double ms;                 /* median device time of the winning configuration on the sample */
     int32_t candidates;        /* configurations timed (0 when the result came from the cache) */
     int32_t from_cache;
-    int32_t reserved[4];
+    int32_t builder;           /* FWN_BUILDER_* of the winning configuration */
+    int32_t reserved[3];
 } fwn_tune_result;
 
 typedef struct fwn_info {
@@ -228,10 +240,10 @@ FWN_API fwn_status fwn_export_tree(fwn_handle h, int32_t* skip, int32_t* tri_beg
 FWN_API fwn_status fwn_export_moments(fwn_handle h, double* moments);
 
 /* Autotuner (no reference counterpart: the reference has no tunable parameters). For one mesh
- * (DEVICE arrays) and a representative DEVICE sample of query points, builds the tree for leaf
- * sizes 4, 8, 12 and 16 and times every query schedule (the warp cursor's variants 1-5; thread per
+ * (DEVICE arrays) and a representative DEVICE sample of query points, builds the tree with both
+ * builders for leaf sizes 4, 8, 12 and 16 and times every query schedule (the warp cursor's variants 1-5; thread per
  * query with blocks of 64/128/256) with CUDA events; returns the fastest. Apply it
- * with cfg.leaf_size, cfg.traversal, cfg.block_size, cfg.tuning. `base` gives beta and the
+ * with cfg.builder, cfg.leaf_size, cfg.traversal, cfg.block_size, cfg.tuning. `base` gives beta and the
  * precision knobs (NULL = defaults). cache_path (may be NULL) names a text file keyed by GPU name
  * and log2 of the triangle and query counts: a hit returns without timing, a miss appends.
  * Synchronous on `stream`. */
@@ -241,10 +253,11 @@ FWN_API fwn_status fwn_autotune(const float* d_vertices, int64_t num_vertices,
                                 const char* cache_path, fwn_tune_result* out, void* stream);
 
 /* Forest autotuner (no reference counterpart). The mixed forest query is one persistent kernel,
- * so its knobs are the leaf size and the register cap: builds the forest (DEVICE vertex/triangle
- * arrays, HOST offset arrays as in fwn_forest_build_device) for leaf sizes 4, 8, 12 and 16 and
+ * so its knobs are the builder, the leaf size and the register cap: builds the forest (DEVICE
+ * vertex/triangle arrays, HOST offset arrays as in fwn_forest_build_device) with both builders
+ * for leaf sizes 4, 8, 12 and 16 and
  * times the forest query with tuning 3, 1, 4 and 5 on the DEVICE points with HOST query_offsets
- * [num_meshes + 1]. Returns the fastest (leaf size, tuning; traversal WARP, block 128). Cache as
+ * [num_meshes + 1]. Returns the fastest (builder, leaf size, tuning; traversal WARP, block 128). Cache as
  * in fwn_autotune, keyed also by log2 of the mesh count. Synchronous on `stream`. */
 FWN_API fwn_status fwn_forest_autotune(const float* d_vertices, const int64_t* vertex_offsets,
                                        const int32_t* d_triangles,

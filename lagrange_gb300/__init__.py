@@ -18,13 +18,15 @@ import numpy as np
 
 __all__ = ["FastWindingNumber", "Forest", "WindingError", "library", "config_default", "autotune",
            "PRECISION_MIXED", "PRECISION_FP64", "TRAVERSAL_AUTO", "TRAVERSAL_THREAD",
-           "TRAVERSAL_WARP", "RECORDS_F32", "RECORDS_F64", "RECORDS_MOMENTS"]
+           "TRAVERSAL_WARP", "RECORDS_F32", "RECORDS_F64", "RECORDS_MOMENTS", "BUILDER_LBVH",
+           "BUILDER_SPLIT"]
 
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libfwn_gb300.so"
 
 PRECISION_MIXED, PRECISION_FP64 = 0, 1
 TRAVERSAL_AUTO, TRAVERSAL_THREAD, TRAVERSAL_WARP = 0, 1, 2
 RECORDS_F32, RECORDS_F64, RECORDS_MOMENTS = 1, 2, 4
+BUILDER_LBVH, BUILDER_SPLIT = 0, 1
 
 STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA_ERROR", 4: "TIMEOUT", 5: "INTERNAL",
           6: "NOT_BUILT"}
@@ -43,7 +45,8 @@ class fwn_config(C.Structure):
     _fields_ = [("beta", C.c_float), ("leaf_size", C.c_int32), ("records", C.c_int32),
                 ("precision", C.c_int32), ("traversal", C.c_int32), ("block_size", C.c_int32),
                 ("sort_queries", C.c_int32), ("fp64_near_scale", C.c_float),
-                ("fp64_cond", C.c_float), ("tuning", C.c_int32), ("reserved", C.c_int32 * 6)]
+                ("fp64_cond", C.c_float), ("tuning", C.c_int32), ("builder", C.c_int32),
+                ("reserved", C.c_int32 * 5)]
 
 
 class fwn_query_opts(C.Structure):
@@ -64,7 +67,7 @@ class fwn_query_stats(C.Structure):
 class fwn_tune_result(C.Structure):
     _fields_ = [("leaf_size", C.c_int32), ("traversal", C.c_int32), ("block_size", C.c_int32),
                 ("tuning", C.c_int32), ("ms", C.c_double), ("candidates", C.c_int32),
-                ("from_cache", C.c_int32), ("reserved", C.c_int32 * 4)]
+                ("from_cache", C.c_int32), ("builder", C.c_int32), ("reserved", C.c_int32 * 3)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
@@ -506,14 +509,14 @@ def autotune(vertices, facets, points, *, cache_path=None, config: fwn_config | 
                                   C.byref(r), _stream_ptr(None)))
     d = r.as_dict()
     d["config"] = {"leaf_size": r.leaf_size, "traversal": r.traversal,
-                   "block_size": r.block_size, "tuning": r.tuning}
+                   "block_size": r.block_size, "tuning": r.tuning, "builder": r.builder}
     return d
 
 
 def autotune_forest(vertices, voff, facets, foff, points, qoff, *, cache_path=None,
                     config: fwn_config | None = None, **cfg_overrides) -> dict:
-    """Picks the leaf size and register-cap variant of a forest by building it for every
-    candidate leaf size and timing the persistent forest query on ``points`` (CUDA tensor or array, [sum Q, 3]) with host offsets
+    """Picks the builder, leaf size and register-cap variant of a forest by building it for
+    every candidate builder and leaf size and timing the persistent forest query on ``points`` (CUDA tensor or array, [sum Q, 3]) with host offsets
     ``qoff``; ``result["config"]`` can be passed to ``Forest``."""
     import torch
 
@@ -530,6 +533,6 @@ def autotune_forest(vertices, voff, facets, foff, points, qoff, *, cache_path=No
         qo.ctypes.data_as(C.c_void_p), C.byref(cfg), cache_path.encode() if cache_path else None,
         C.byref(r), _stream_ptr(None)))
     d = r.as_dict()
-    d["config"] = {"leaf_size": r.leaf_size, "tuning": r.tuning}
+    d["config"] = {"leaf_size": r.leaf_size, "tuning": r.tuning, "builder": r.builder}
     return d
 

@@ -1,10 +1,10 @@
-// Autotuner: picks the leaf size (build), the traversal schedule, block size and warp-schedule
-// variant (queries per lane, register cap) for one mesh and a representative query sample, by
-// timing every candidate with CUDA events on the device. beta does not enter the choice (the schedule and block shape are
+// Autotuner: picks the tree builder and leaf size (build), the traversal schedule, block size
+// and warp-schedule variant (queries per lane, register cap) for one mesh and a representative
+// query sample, by timing every candidate with CUDA events on the device. beta does not enter the choice (the schedule and block shape are
 // tuned at the caller's beta, which only changes how deep the walk goes).
 //
 // Optional cache: a text file with one line per (GPU name, log2 triangles, log2 queries) key:
-//   <gpu name>|<log2 nf>|<log2 n> <leaf> <traversal> <block> <tuning> <ms>
+//   t2|<gpu name>|<log2 nf>|<log2 n> <leaf> <traversal> <block> <tuning> <builder> <ms>
 // A hit skips the timing; a miss appends the new line.
 #include <algorithm>
 #include <cmath>
@@ -37,6 +37,7 @@ const Candidate kCandidates[] = {
     {FWN_TRAVERSAL_THREAD, 256, 0},
 };
 const int kLeafSizes[] = {4, 8, 12, 16};
+const int kBuilders[] = {FWN_BUILDER_LBVH, FWN_BUILDER_SPLIT};
 
 std::mutex g_cache_mutex;
 
@@ -57,7 +58,7 @@ std::string cache_key(int64_t nf, int64_t n) {
     std::string name(prop.name);
     for (char& ch : name)
         if (ch == ' ' || ch == '|') ch = '_';
-    return name + "|" + std::to_string(log2_bucket(nf)) + "|" + std::to_string(log2_bucket(n));
+    return "t2|" + name + "|" + std::to_string(log2_bucket(nf)) + "|" + std::to_string(log2_bucket(n));
 }
 
 bool cache_lookup(const char* path, const std::string& key, fwn_tune_result* out) {
@@ -70,7 +71,8 @@ bool cache_lookup(const char* path, const std::string& key, fwn_tune_result* out
         std::string k;
         fwn_tune_result r;
         std::memset(&r, 0, sizeof(r));
-        if (!(is >> k >> r.leaf_size >> r.traversal >> r.block_size >> r.tuning >> r.ms)) continue;
+        if (!(is >> k >> r.leaf_size >> r.traversal >> r.block_size >> r.tuning >> r.builder >> r.ms))
+            continue;
         if (k == key) {
             r.from_cache = 1;
             *out = r;
@@ -85,7 +87,7 @@ void cache_store(const char* path, const std::string& key, const fwn_tune_result
     std::ofstream f(path, std::ios::app);
     if (!f) return;  // a read-only cache location only loses the caching
     f << key << " " << r.leaf_size << " " << r.traversal << " " << r.block_size << " " << r.tuning
-      << " " << r.ms << "\n";
+      << " " << r.builder << " " << r.ms << "\n";
 }
 
 }  // namespace
@@ -124,10 +126,12 @@ extern "C" FWN_API fwn_status fwn_autotune(const float* d_V, int64_t nv, const i
         std::memset(&best, 0, sizeof(best));
         best.ms = 1e300;
         int evaluated = 0;
+        for (int builder : kBuilders)
         for (int leaf : kLeafSizes) {
             Engine e;
             e.cfg = cfg;
             e.cfg.leaf_size = leaf;
+            e.cfg.builder = builder;
             FWN_CUDA_CHECK(cudaGetDevice(&e.device));
             const int64_t voff[2] = {0, nv}, foff[2] = {0, nf};
             build_forest(e, d_V, voff, d_F, foff, 1, st);
@@ -157,6 +161,7 @@ extern "C" FWN_API fwn_status fwn_autotune(const float* d_V, int64_t nv, const i
                     best.traversal = a.traversal;
                     best.block_size = a.block_size;
                     best.tuning = a.tuning;
+                    best.builder = builder;
                 }
             }
         }
@@ -222,10 +227,12 @@ extern "C" FWN_API fwn_status fwn_forest_autotune(const float* d_V, const int64_
         std::memset(&best, 0, sizeof(best));
         best.ms = 1e300;
         int evaluated = 0;
+        for (int builder : kBuilders)
         for (int leaf : kLeafSizes) {
             Engine e;
             e.cfg = cfg;
             e.cfg.leaf_size = leaf;
+            e.cfg.builder = builder;
             FWN_CUDA_CHECK(cudaGetDevice(&e.device));
             build_forest(e, d_V, vertex_offsets, d_F, triangle_offsets, num_meshes, st);
             for (int tuning : {3, 1, 4, 5}) {  // warp-schedule variants (queries per lane, cap)
@@ -249,6 +256,7 @@ extern "C" FWN_API fwn_status fwn_forest_autotune(const float* d_V, const int64_
                     best.traversal = FWN_TRAVERSAL_WARP;
                     best.block_size = 128;
                     best.tuning = tuning;
+                    best.builder = builder;
                 }
             }
         }

@@ -136,6 +136,8 @@ void validate_config(const fwn_config& c) {
     if (!(c.fp64_cond >= 0.f) || !std::isfinite(c.fp64_cond))
         throw Error(FWN_INVALID_ARG, "fp64_cond must be finite and >= 0");
     if (c.tuning < 0 || c.tuning > 5) throw Error(FWN_INVALID_ARG, "tuning must be in [0, 5]");
+    if (c.builder != FWN_BUILDER_LBVH && c.builder != FWN_BUILDER_SPLIT)
+        throw Error(FWN_INVALID_ARG, "builder must be FWN_BUILDER_LBVH or FWN_BUILDER_SPLIT");
 }
 
 struct OwnedStream {

@@ -253,12 +253,12 @@ __global__ void k_emit_count(int n, int K, const uint64_t* __restrict__ keys,
         leaf_list[atomicAdd(leaf_list_len, 1)] = u;
 }
 
-__global__ void k_positions(int n, const int* __restrict__ parent, const int* __restrict__ first,
-                            const int* __restrict__ last, const uint8_t* __restrict__ flags,
-                            const int* __restrict__ base, int* __restrict__ pos,
-                            int* __restrict__ skip) {
+__global__ void k_positions(int num_nodes, const int* __restrict__ parent,
+                            const int* __restrict__ first, const int* __restrict__ last,
+                            const uint8_t* __restrict__ flags, const int* __restrict__ base,
+                            int* __restrict__ pos, int* __restrict__ skip) {
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
-    if (u >= 2 * n - 1) return;
+    if (u >= num_nodes) return;
     if (!(flags[u] & 1)) {
         pos[u] = -1;
         skip[u] = -1;
@@ -296,6 +296,249 @@ __global__ void k_mesh_roots(int nmeshes, const int64_t* __restrict__ foff, int 
     }
     mi[m].root = pos[u];
     mi[m].end = skip[u];
+}
+
+// ---- K1-K3 (builder 1): top-down splitting build ----------------------------------------------
+// Level-synchronous, all meshes at once. Every active segment (a node of > leaf_size triangles)
+// splits the bounding box of its triangles' centroids at the midpoint of its longest axis (ties:
+// the lowest axis), split = (lo + hi) * 0.5f; the left child takes the centroids below the split,
+// both children keeping the segment's order (a stable partition by one scan of the left flags).
+// When every centroid coincides, or the midpoint rounds down to the low end, the segment splits
+// by position instead (the first m / 2 left). A child of <= leaf_size triangles is a leaf and its
+// triangles take their final slots. Roots (one per non-empty mesh) are nodes 0.., the children of
+// active segment s at a level are nodes base + 2s and base + 2s + 1; DFS positions and skip links
+// come from the node ranges afterwards with the same formula as for the LBVH (k_positions).
+// Below level kSpatialLevels every split is by position, which bounds the depth by
+// kSpatialLevels + log2(n) whatever the geometry (midpoint splits of float boxes could otherwise
+// go on for hundreds of levels on adversarial inputs).
+constexpr int kSpatialLevels = 96;
+
+struct SplitSlots {
+    int* perm;  // triangle id per slot
+    float* cx;  // its centroid
+    float* cy;
+    float* cz;
+    int* seg;   // active segment of the slot at this level (-1: in a leaf)
+};
+
+__global__ void k_split_init(const float* __restrict__ V, const int32_t* __restrict__ F,
+                             const int64_t* __restrict__ voff, const int64_t* __restrict__ foff,
+                             int nmeshes, int64_t nf, const int* __restrict__ mesh_seg,
+                             SplitSlots out, int* __restrict__ final_perm,
+                             uint64_t* __restrict__ keys, unsigned* __restrict__ status) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nf) return;
+    const int m = find_mesh(foff, nmeshes, t);
+    const int64_t nvm = voff[m + 1] - voff[m];
+    float c[3] = {0.f, 0.f, 0.f};
+    bool ok = true;
+    int32_t idx[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        idx[j] = F[3 * t + j];
+        if (idx[j] < 0 || (int64_t)idx[j] >= nvm) ok = false;
+    }
+    if (!ok) {
+        atomicOr(status, ST_BAD_INDEX);
+    } else {
+        float v[3][3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const float* p = V + 3 * (voff[m] + idx[j]);
+            v[j][0] = p[0];
+            v[j][1] = p[1];
+            v[j][2] = p[2];
+            if (!isfinite(v[j][0]) || !isfinite(v[j][1]) || !isfinite(v[j][2])) ok = false;
+        }
+        if (!ok) atomicOr(status, ST_NONFINITE);
+#pragma unroll
+        for (int a = 0; a < 3; ++a) c[a] = ((v[0][a] + v[1][a]) + v[2][a]) / 3.0f;
+    }
+    const int sg = mesh_seg[m];
+    out.perm[t] = (int)t;
+    out.cx[t] = c[0];
+    out.cy[t] = c[1];
+    out.cz[t] = c[2];
+    out.seg[t] = sg;
+    if (sg < 0) final_perm[t] = (int)t;  // the whole mesh is one leaf
+    keys[t] = (uint64_t)m << MORTON_BITS;
+}
+
+__global__ void k_split_box_init(int nact, unsigned* __restrict__ box) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 6 * nact) box[i] = (i % 6) < 3 ? 0xffffffffu : 0u;
+}
+
+// Centroid box per active segment: lanes of a warp that hold the same segment reduce together
+// (ordered-int encodings, so min / max are integer reductions), one atomic per group and axis.
+__global__ void k_split_box(int64_t n, SplitSlots cur, unsigned* __restrict__ box) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int sg = i < n ? cur.seg[i] : -1;
+    const unsigned act = __ballot_sync(0xffffffffu, sg >= 0);
+    if (sg < 0) return;
+    const unsigned peers = __match_any_sync(act, sg);
+    const bool leader = (threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1);
+    const float c[3] = {cur.cx[i], cur.cy[i], cur.cz[i]};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const unsigned e = enc_float(c[a]);
+        const unsigned lo = __reduce_min_sync(peers, e), hi = __reduce_max_sync(peers, e);
+        if (leader) {
+            atomicMin(&box[6 * sg + a], lo);
+            atomicMax(&box[6 * sg + 3 + a], hi);
+        }
+    }
+}
+
+__global__ void k_split_decide(int nact, bool by_position, const unsigned* __restrict__ box,
+                               int* __restrict__ axis_of, float* __restrict__ split_of,
+                               int* __restrict__ spatial_of) {
+    const int sg = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sg >= nact) return;
+    float lo[3], hi[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        lo[a] = dec_float(box[6 * sg + a]);
+        hi[a] = dec_float(box[6 * sg + 3 + a]);
+    }
+    int axis = 0;
+    float ext = hi[0] - lo[0];
+#pragma unroll
+    for (int a = 1; a < 3; ++a) {
+        const float x = hi[a] - lo[a];
+        if (x > ext) {
+            ext = x;
+            axis = a;
+        }
+    }
+    const float split = (lo[axis] + hi[axis]) * 0.5f;
+    axis_of[sg] = axis;
+    split_of[sg] = split;
+    spatial_of[sg] = (!by_position && ext > 0.f && split > lo[axis]) ? 1 : 0;
+}
+
+__global__ void k_split_flags(int64_t n, SplitSlots cur, const int* __restrict__ s_start,
+                              const int* __restrict__ s_end, const int* __restrict__ axis_of,
+                              const float* __restrict__ split_of,
+                              const int* __restrict__ spatial_of, int* __restrict__ flags) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > n) return;
+    int f = 0;
+    if (i < n) {
+        const int sg = cur.seg[i];
+        if (sg >= 0) {
+            if (spatial_of[sg]) {
+                const int a = axis_of[sg];
+                const float c = a == 0 ? cur.cx[i] : a == 1 ? cur.cy[i] : cur.cz[i];
+                f = c < split_of[sg] ? 1 : 0;
+            } else {
+                f = (i - s_start[sg]) < (s_end[sg] - s_start[sg]) / 2 ? 1 : 0;
+            }
+        }
+    }
+    flags[i] = f;  // flags[n] = 0: the scan's total entry
+}
+
+// Children of every active segment (lf = exclusive scan of the left flags); cact[c] = 1 when
+// child c (2s left, 2s + 1 right) stays active; cact[2 nact] = 0 for the scan's total.
+__global__ void k_split_children(int nact, int node_base, int K, const int* __restrict__ s_start,
+                                 const int* __restrict__ s_end, const int* __restrict__ s_node,
+                                 const int* __restrict__ lf, int* __restrict__ nfirst,
+                                 int* __restrict__ nlast, int* __restrict__ nparent,
+                                 int* __restrict__ nleft, int* __restrict__ nright,
+                                 int* __restrict__ cact) {
+    const int sg = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sg > nact) return;
+    if (sg == nact) {
+        cact[2 * nact] = 0;
+        return;
+    }
+    const int b = s_start[sg], e = s_end[sg], nl = lf[e] - lf[b];
+    const int l = node_base + 2 * sg, r = l + 1, p = s_node[sg];
+    nfirst[l] = b;
+    nlast[l] = b + nl - 1;
+    nfirst[r] = b + nl;
+    nlast[r] = e - 1;
+    nparent[l] = p;
+    nparent[r] = p;
+    nleft[l] = nright[l] = nleft[r] = nright[r] = -1;
+    nleft[p] = l;
+    nright[p] = r;
+    cact[2 * sg] = nl > K ? 1 : 0;
+    cact[2 * sg + 1] = (e - b - nl) > K ? 1 : 0;
+}
+
+// The next level's active segments (cs = exclusive scan of cact).
+__global__ void k_split_next(int nact, int node_base, const int* __restrict__ s_start,
+                             const int* __restrict__ s_end, const int* __restrict__ lf,
+                             const int* __restrict__ cs, int* __restrict__ n_start,
+                             int* __restrict__ n_end, int* __restrict__ n_node) {
+    const int sg = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sg >= nact) return;
+    const int b = s_start[sg], e = s_end[sg], mid = b + (lf[e] - lf[b]);
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+        const int ch = 2 * sg + c;
+        if (cs[ch + 1] == cs[ch]) continue;
+        const int k = cs[ch];
+        n_start[k] = c == 0 ? b : mid;
+        n_end[k] = c == 0 ? mid : e;
+        n_node[k] = node_base + ch;
+    }
+}
+
+// Stable partition of every active segment: left-flagged slots first, each side in its order.
+// Slots of children that stay active go to the next level's buffers; those of leaves are final.
+__global__ void k_split_scatter(int64_t n, SplitSlots cur, SplitSlots nxt,
+                                const int* __restrict__ lf, const int* __restrict__ s_start,
+                                const int* __restrict__ s_end, const int* __restrict__ cs,
+                                int* __restrict__ final_perm) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int sg = cur.seg[i];
+    if (sg < 0) {
+        nxt.seg[i] = -1;
+        return;
+    }
+    const int b = s_start[sg], e = s_end[sg];
+    const int fb = lf[b], nl = lf[e] - fb, left_before = lf[i] - fb;
+    const bool left = lf[i + 1] != lf[i];  // the exclusive scan steps where the flag is set
+    const int64_t dest = left ? b + left_before : b + nl + ((int)(i - b) - left_before);
+    const int ch = 2 * sg + (left ? 0 : 1);
+    if (cs[ch + 1] != cs[ch]) {
+        nxt.perm[dest] = cur.perm[i];
+        nxt.cx[dest] = cur.cx[i];
+        nxt.cy[dest] = cur.cy[i];
+        nxt.cz[dest] = cur.cz[i];
+        nxt.seg[dest] = cs[ch];
+    } else {
+        final_perm[dest] = cur.perm[i];
+        nxt.seg[dest] = -1;
+    }
+}
+
+// Node flags of the split tree (every node emitted; leaves = no children), the per-first-slot
+// node counts of the position scan, and the refit's leaf list.
+__global__ void k_split_emit(int num_nodes, const int* __restrict__ nfirst,
+                             const int* __restrict__ nleft, uint8_t* __restrict__ flags,
+                             int* __restrict__ cnt_first, int* __restrict__ leaf_list,
+                             int* __restrict__ leaf_list_len) {
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= num_nodes) return;
+    const bool leaf = nleft[u] < 0;
+    flags[u] = (uint8_t)(1 | (leaf ? 2 : 0));
+    atomicAdd(&cnt_first[nfirst[u]], 1);
+    if (leaf) leaf_list[atomicAdd(leaf_list_len, 1)] = u;
+}
+
+__global__ void k_split_mesh_roots(int nmeshes, const int* __restrict__ root_node,
+                                   const int* __restrict__ pos, const int* __restrict__ skip,
+                                   MeshInfo* __restrict__ mi) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nmeshes) return;
+    const int r = root_node[m];
+    mi[m].root = r < 0 ? -1 : pos[r];
+    mi[m].end = r < 0 ? -1 : skip[r];
 }
 
 // ---- K4: FP64 refit ---------------------------------------------------------------------------
@@ -481,7 +724,7 @@ __global__ void k_refit(int num_leaves, const int* __restrict__ leaf_list,
                         const uint32_t* __restrict__ tri_of_slot, const float* __restrict__ V,
                         const int32_t* __restrict__ F, const int64_t* __restrict__ voff,
                         StageRec* __restrict__ stage, int* __restrict__ visit,
-                        unsigned* __restrict__ status) {
+                        unsigned* __restrict__ status, bool multi_root) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= num_leaves) return;
     const int e = leaf_list[k];  // one emitted leaf per thread
@@ -492,8 +735,8 @@ __global__ void k_refit(int num_leaves, const int* __restrict__ leaf_list,
     int guard = 0;
     while (v != 0) {
         const int p = parent[v];
-        if (p < 0) {
-            atomicOr(status, ST_REFIT_ORPHAN);
+        if (p < 0) {  // a mesh root of a split tree; in the LBVH only node 0 has no parent
+            if (!multi_root) atomicOr(status, ST_REFIT_ORPHAN);
             return;
         }
         if (is_cross(keys, first, last, p)) break;  // v is a mesh root
@@ -533,28 +776,29 @@ __device__ __forceinline__ bool internal_emitted(const uint64_t* __restrict__ ke
     return (fl & 1) && !(fl & 2) && !is_cross(keys, first, last, u);
 }
 
-// chunks[u] for the internal nodes u < n - 1 (0 when not an emitted single-mesh internal node);
-// chunks[n - 1] = 0 becomes the total after the exclusive scan.
-__global__ void k_radius_chunks(int n, const uint64_t* __restrict__ keys,
+// chunks[u] for the nodes u < num_nodes (0 unless an emitted single-mesh internal node);
+// chunks[num_nodes] = 0 becomes the total after the exclusive scan.
+__global__ void k_radius_chunks(int num_nodes, const uint64_t* __restrict__ keys,
                                 const int* __restrict__ first, const int* __restrict__ last,
                                 const uint8_t* __restrict__ flags, int* __restrict__ chunks) {
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
-    if (u >= n) return;
-    chunks[u] = (u < n - 1 && internal_emitted(keys, first, last, flags, u))
+    if (u > num_nodes) return;
+    chunks[u] = (u < num_nodes && internal_emitted(keys, first, last, flags, u))
                     ? (last[u] - first[u] + kRadiusChunk) / kRadiusChunk
                     : 0;
 }
 
 // Grid-stride over the chunks: chunk c belongs to the last node u with off[u] <= c.
-__global__ void k_node_radius(int n, const int* __restrict__ off, const int* __restrict__ first,
-                              const int* __restrict__ last, const int* __restrict__ pos,
-                              const StageRec* __restrict__ stage, const TriF32* __restrict__ tris,
+__global__ void k_node_radius(int num_nodes, const int* __restrict__ off,
+                              const int* __restrict__ first, const int* __restrict__ last,
+                              const int* __restrict__ pos, const StageRec* __restrict__ stage,
+                              const TriF32* __restrict__ tris,
                               unsigned long long* __restrict__ r2bits) {
     const int lane = threadIdx.x & 31;
-    const int total = off[n - 1];
+    const int total = off[num_nodes];
     const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
     for (int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); c < total; c += nwarps) {
-        int lo = 0, hi = n - 2;  // off[n - 1] = total > c, so the node is in [0, n - 2]
+        int lo = 0, hi = num_nodes - 1;  // off[num_nodes] = total > c
         while (lo < hi) {
             const int mid = (lo + hi + 1) >> 1;
             if (off[mid] <= c) lo = mid; else hi = mid - 1;
@@ -619,14 +863,14 @@ __device__ void derive_coeffs(const StageRec& R, Coeffs& c) {
     for (int i = 0; i < 10; ++i) c.D[i] = 7.5 * mono[i];
 }
 
-__global__ void k_convert(int n, const uint64_t* __restrict__ keys, const int* __restrict__ first,
+__global__ void k_convert(int num_nodes, const uint64_t* __restrict__ keys, const int* __restrict__ first,
                           const int* __restrict__ last, const uint8_t* __restrict__ flags,
                           const int* __restrict__ pos, const int* __restrict__ skip,
                           StageRec* __restrict__ stage, const unsigned long long* __restrict__ r2bits,
                           NodeF32* __restrict__ n32, NodeF64* __restrict__ n64,
                           int* __restrict__ leaf_count) {
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
-    if (u >= 2 * n - 1) return;
+    if (u >= num_nodes) return;
     const uint8_t fl = flags[u];
     if (!(fl & 1)) return;
     const int i = pos[u];
@@ -790,61 +1034,195 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
 
     if (nf > 0) {
         const int n = (int)nf;
-        int mesh_bits = 0;
-        while ((1ll << mesh_bits) < nmeshes) ++mesh_bits;
-        uint64_t* keys_a = (uint64_t*)track(dalloc<uint64_t>(n, st));
-        uint64_t* keys_b = (uint64_t*)track(dalloc<uint64_t>(n, st));
-        uint32_t* vals_a = (uint32_t*)track(dalloc<uint32_t>(n, st));
-        uint32_t* vals_b = (uint32_t*)track(dalloc<uint32_t>(n, st));
-        void* sort_tmp = track(dalloc<char>(radix_sort_temp_bytes(n, 8), st));
-        NvtxRange trace_keys("fwn build: Morton keys + sort");
-        k_tri_keys<<<grid_for(n, 256), 256, 0, st>>>(d_V, d_F, voff, foff, (int)nmeshes, nf,
-                                                     e.meshes, keys_a, vals_a, status);
-        FWN_CUDA_CHECK(cudaGetLastError());
-        unsigned st_h = 0;
-        FWN_CUDA_CHECK(cudaMemcpyAsync(&st_h, status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
-        FWN_CUDA_CHECK(cudaStreamSynchronize(st));
-        if (st_h & ST_BAD_INDEX) throw Error(FWN_INVALID_ARG, "triangle vertex index out of range");
-        if (st_h & ST_NONFINITE)
-            throw Error(FWN_INVALID_ARG, "non-finite vertex coordinate referenced by a triangle");
-        const bool in_b = radix_sort_u64(keys_a, vals_a, keys_b, vals_b, n,
-                                         MORTON_BITS + mesh_bits, sort_tmp, st);
-        const uint64_t* keys = in_b ? keys_b : keys_a;
-        const uint32_t* tri_of_slot = in_b ? vals_b : vals_a;
-
-        const int nn = 2 * n - 1;
-        int* parent = (int*)track(dalloc<int>(nn, st));
-        int* first = (int*)track(dalloc<int>(nn, st));
-        int* last = (int*)track(dalloc<int>(nn, st));
-        int* left = (int*)track(dalloc<int>(std::max(n - 1, 1), st));
-        int* right = (int*)track(dalloc<int>(std::max(n - 1, 1), st));
+        const bool split = e.cfg.builder == FWN_BUILDER_SPLIT;
+        // node arrays: the LBVH's Karras tree has 2n - 1 nodes (internal 0..n-2, leaves after);
+        // a split tree at most 2n - 1 as well, ids in creation order
+        const int cap = split ? 2 * n : 2 * n - 1;
+        const int nint = split ? cap : std::max(n - 1, 1);  // left / right / visit entries
+        int* parent = (int*)track(dalloc<int>(cap, st));
+        int* first = (int*)track(dalloc<int>(cap, st));
+        int* last = (int*)track(dalloc<int>(cap, st));
+        int* left = (int*)track(dalloc<int>(nint, st));
+        int* right = (int*)track(dalloc<int>(nint, st));
         int* cnt = (int*)track(dalloc<int>(n + 1, st));
-        uint8_t* flags = (uint8_t*)track(dalloc<uint8_t>(nn, st));
-        int* pos = (int*)track(dalloc<int>(nn, st));
-        int* skip = (int*)track(dalloc<int>(nn, st));
-        void* scan_tmp = track(dalloc<char>(exclusive_scan_temp_bytes(n + 1), st));
-        int* visit = (int*)track(dalloc<int>(std::max(n - 1, 1), st));
+        uint8_t* flags = (uint8_t*)track(dalloc<uint8_t>(cap, st));
+        int* pos = (int*)track(dalloc<int>(cap, st));
+        int* skip = (int*)track(dalloc<int>(cap, st));
+        void* scan_tmp = track(dalloc<char>(exclusive_scan_temp_bytes(cap + 1), st));
+        int* visit = (int*)track(dalloc<int>(nint, st));
         int* leaf_list = (int*)track(dalloc<int>(n, st));
         int* leaf_list_len = (int*)track(dalloc<int>(1, st));
         int* leaf_count = (int*)track(dalloc<int>(1, st));
+        const uint64_t* keys = nullptr;
+        const uint32_t* tri_of_slot = nullptr;
+        int num_nodes = 0;
+        unsigned st_h = 0;
+        auto check_input = [&]() {
+            FWN_CUDA_CHECK(cudaMemcpyAsync(&st_h, status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+            FWN_CUDA_CHECK(cudaStreamSynchronize(st));
+            if (st_h & ST_BAD_INDEX) throw Error(FWN_INVALID_ARG, "triangle vertex index out of range");
+            if (st_h & ST_NONFINITE)
+                throw Error(FWN_INVALID_ARG, "non-finite vertex coordinate referenced by a triangle");
+        };
 
-        NvtxRange trace_tree("fwn build: Karras tree + DFS layout");
-        FWN_CUDA_CHECK(cudaMemsetAsync(parent, 0xff, (size_t)nn * sizeof(int), st));  // -1
-        k_leaf_init<<<grid_for(n, 256), 256, 0, st>>>(n, first, last);
-        if (n == 1) {
-            int m1 = -1;
-            FWN_CUDA_CHECK(cudaMemcpyAsync(parent, &m1, sizeof(int), cudaMemcpyHostToDevice, st));
+        if (!split) {
+            int mesh_bits = 0;
+            while ((1ll << mesh_bits) < nmeshes) ++mesh_bits;
+            uint64_t* keys_a = (uint64_t*)track(dalloc<uint64_t>(n, st));
+            uint64_t* keys_b = (uint64_t*)track(dalloc<uint64_t>(n, st));
+            uint32_t* vals_a = (uint32_t*)track(dalloc<uint32_t>(n, st));
+            uint32_t* vals_b = (uint32_t*)track(dalloc<uint32_t>(n, st));
+            void* sort_tmp = track(dalloc<char>(radix_sort_temp_bytes(n, 8), st));
+            NvtxRange trace_keys("fwn build: Morton keys + sort");
+            k_tri_keys<<<grid_for(n, 256), 256, 0, st>>>(d_V, d_F, voff, foff, (int)nmeshes, nf,
+                                                         e.meshes, keys_a, vals_a, status);
+            FWN_CUDA_CHECK(cudaGetLastError());
+            check_input();
+            const bool in_b = radix_sort_u64(keys_a, vals_a, keys_b, vals_b, n,
+                                             MORTON_BITS + mesh_bits, sort_tmp, st);
+            keys = in_b ? keys_b : keys_a;
+            tri_of_slot = in_b ? vals_b : vals_a;
+
+            const int nn = 2 * n - 1;
+            num_nodes = nn;
+            NvtxRange trace_tree("fwn build: Karras tree + DFS layout");
+            FWN_CUDA_CHECK(cudaMemsetAsync(parent, 0xff, (size_t)nn * sizeof(int), st));  // -1
+            k_leaf_init<<<grid_for(n, 256), 256, 0, st>>>(n, first, last);
+            if (n == 1) {
+                int m1 = -1;
+                FWN_CUDA_CHECK(cudaMemcpyAsync(parent, &m1, sizeof(int), cudaMemcpyHostToDevice, st));
+            } else {
+                k_karras<<<grid_for(n - 1, 256), 256, 0, st>>>(keys, n, left, right, parent, first, last);
+            }
+            FWN_CUDA_CHECK(cudaMemsetAsync(cnt, 0, (n + 1) * sizeof(int), st));
+            FWN_CUDA_CHECK(cudaMemsetAsync(leaf_list_len, 0, sizeof(int), st));
+            k_emit_count<<<grid_for(nn, 256), 256, 0, st>>>(n, K, keys, parent, first, last, cnt, flags,
+                                                            leaf_list, leaf_list_len);
+            exclusive_scan_i32(cnt, n + 1, scan_tmp, st);
+            k_positions<<<grid_for(nn, 256), 256, 0, st>>>(nn, parent, first, last, flags, cnt, pos, skip);
+            k_mesh_roots<<<grid_for(nmeshes, 128), 128, 0, st>>>((int)nmeshes, foff, n, parent, first,
+                                                                 last, pos, skip, e.meshes);
         } else {
-            k_karras<<<grid_for(n - 1, 256), 256, 0, st>>>(keys, n, left, right, parent, first, last);
+            NvtxRange trace_tree("fwn build: top-down splits + DFS layout");
+            // roots: one node per non-empty mesh; a mesh of > K triangles is an active segment
+            std::vector<int> root_node(nmeshes, -1), mesh_seg(nmeshes, -1);
+            std::vector<int> h_first, h_last, s_start, s_end, s_node;
+            for (int64_t m = 0; m < nmeshes; ++m) {
+                const int64_t b = foff_h[m], en = foff_h[m + 1];
+                if (en <= b) continue;
+                const int id = (int)h_first.size();
+                root_node[m] = id;
+                h_first.push_back((int)b);
+                h_last.push_back((int)(en - 1));
+                if (en - b > K) {
+                    mesh_seg[m] = (int)s_start.size();
+                    s_start.push_back((int)b);
+                    s_end.push_back((int)en);
+                    s_node.push_back(id);
+                }
+            }
+            const int nroots = (int)h_first.size();
+            const int smax = n / 2 + (int)nmeshes + 1;  // active segments hold >= 2 triangles
+            uint64_t* skeys = (uint64_t*)track(dalloc<uint64_t>(n, st));
+            int* final_perm = (int*)track(dalloc<int>(n, st));
+            SplitSlots A, B;
+            for (SplitSlots* X : {&A, &B}) {
+                X->perm = (int*)track(dalloc<int>(n, st));
+                X->cx = (float*)track(dalloc<float>(n, st));
+                X->cy = (float*)track(dalloc<float>(n, st));
+                X->cz = (float*)track(dalloc<float>(n, st));
+                X->seg = (int*)track(dalloc<int>(n, st));
+            }
+            int* lflags = (int*)track(dalloc<int>(n + 1, st));
+            int* cact = (int*)track(dalloc<int>(2 * smax + 1, st));
+            int* seg_a[3], *seg_b[3];  // start, end, node of this level / the next
+            for (int k = 0; k < 3; ++k) {
+                seg_a[k] = (int*)track(dalloc<int>(smax, st));
+                seg_b[k] = (int*)track(dalloc<int>(smax, st));
+            }
+            unsigned* box = (unsigned*)track(dalloc<unsigned>(6 * (size_t)smax, st));
+            int* axis_of = (int*)track(dalloc<int>(smax, st));
+            float* split_of = (float*)track(dalloc<float>(smax, st));
+            int* spatial_of = (int*)track(dalloc<int>(smax, st));
+            int* d_mesh_seg = (int*)track(dalloc<int>(nmeshes, st));
+            int* d_root_node = (int*)track(dalloc<int>(nmeshes, st));
+            FWN_CUDA_CHECK(cudaMemcpyAsync(d_mesh_seg, mesh_seg.data(), nmeshes * sizeof(int),
+                                           cudaMemcpyHostToDevice, st));
+            FWN_CUDA_CHECK(cudaMemcpyAsync(d_root_node, root_node.data(), nmeshes * sizeof(int),
+                                           cudaMemcpyHostToDevice, st));
+            FWN_CUDA_CHECK(cudaMemcpyAsync(first, h_first.data(), nroots * sizeof(int),
+                                           cudaMemcpyHostToDevice, st));
+            FWN_CUDA_CHECK(cudaMemcpyAsync(last, h_last.data(), nroots * sizeof(int),
+                                           cudaMemcpyHostToDevice, st));
+            FWN_CUDA_CHECK(cudaMemsetAsync(parent, 0xff, (size_t)nroots * sizeof(int), st));
+            FWN_CUDA_CHECK(cudaMemsetAsync(left, 0xff, (size_t)nroots * sizeof(int), st));
+            FWN_CUDA_CHECK(cudaMemsetAsync(right, 0xff, (size_t)nroots * sizeof(int), st));
+            int nact = (int)s_start.size();
+            if (nact) {
+                FWN_CUDA_CHECK(cudaMemcpyAsync(seg_a[0], s_start.data(), nact * sizeof(int),
+                                               cudaMemcpyHostToDevice, st));
+                FWN_CUDA_CHECK(cudaMemcpyAsync(seg_a[1], s_end.data(), nact * sizeof(int),
+                                               cudaMemcpyHostToDevice, st));
+                FWN_CUDA_CHECK(cudaMemcpyAsync(seg_a[2], s_node.data(), nact * sizeof(int),
+                                               cudaMemcpyHostToDevice, st));
+            }
+            k_split_init<<<grid_for(n, 256), 256, 0, st>>>(d_V, d_F, voff, foff, (int)nmeshes, nf,
+                                                           d_mesh_seg, A, final_perm, skeys, status);
+            FWN_CUDA_CHECK(cudaGetLastError());
+            check_input();
+            int node_base = nroots;
+            SplitSlots* cur = &A;
+            SplitSlots* nxt = &B;
+            int level = 0;
+            while (nact > 0) {
+                if (level > kSpatialLevels + 64)  // position splits halve every segment
+                    throw Error(FWN_INTERNAL, "split build did not converge");
+                if (node_base + 2 * nact > cap) throw Error(FWN_INTERNAL, "split build node overflow");
+                k_split_box_init<<<grid_for(6 * nact, 256), 256, 0, st>>>(nact, box);
+                k_split_box<<<grid_for(n, 256), 256, 0, st>>>(n, *cur, box);
+                k_split_decide<<<grid_for(nact, 128), 128, 0, st>>>(
+                    nact, level >= kSpatialLevels, box, axis_of, split_of, spatial_of);
+                k_split_flags<<<grid_for(n + 1, 256), 256, 0, st>>>(n, *cur, seg_a[0], seg_a[1],
+                                                                   axis_of, split_of, spatial_of,
+                                                                   lflags);
+                exclusive_scan_i32(lflags, n + 1, scan_tmp, st);
+                k_split_children<<<grid_for(nact + 1, 128), 128, 0, st>>>(
+                    nact, node_base, K, seg_a[0], seg_a[1], seg_a[2], lflags, first, last, parent,
+                    left, right, cact);
+                exclusive_scan_i32(cact, 2 * nact + 1, scan_tmp, st);
+                k_split_next<<<grid_for(nact, 128), 128, 0, st>>>(nact, node_base, seg_a[0],
+                                                                 seg_a[1], lflags, cact, seg_b[0],
+                                                                 seg_b[1], seg_b[2]);
+                FWN_CUDA_CHECK(cudaGetLastError());
+                // lflags now holds the exclusive scan of the left flags (a slot's flag is the
+                // step from its entry to the next)
+                k_split_scatter<<<grid_for(n, 256), 256, 0, st>>>(n, *cur, *nxt, lflags, seg_a[0],
+                                                                 seg_a[1], cact, final_perm);
+                FWN_CUDA_CHECK(cudaGetLastError());
+                node_base += 2 * nact;
+                int next = 0;
+                FWN_CUDA_CHECK(cudaMemcpyAsync(&next, cact + 2 * nact, sizeof(int),
+                                               cudaMemcpyDeviceToHost, st));
+                FWN_CUDA_CHECK(cudaStreamSynchronize(st));
+                nact = next;
+                ++level;
+                std::swap(cur, nxt);
+                for (int k = 0; k < 3; ++k) std::swap(seg_a[k], seg_b[k]);
+            }
+            num_nodes = node_base;
+            keys = skeys;
+            tri_of_slot = reinterpret_cast<const uint32_t*>(final_perm);
+            FWN_CUDA_CHECK(cudaMemsetAsync(cnt, 0, (n + 1) * sizeof(int), st));
+            FWN_CUDA_CHECK(cudaMemsetAsync(leaf_list_len, 0, sizeof(int), st));
+            k_split_emit<<<grid_for(num_nodes, 256), 256, 0, st>>>(num_nodes, first, left, flags, cnt,
+                                                                   leaf_list, leaf_list_len);
+            exclusive_scan_i32(cnt, n + 1, scan_tmp, st);
+            k_positions<<<grid_for(num_nodes, 256), 256, 0, st>>>(num_nodes, parent, first, last,
+                                                                  flags, cnt, pos, skip);
+            k_split_mesh_roots<<<grid_for(nmeshes, 128), 128, 0, st>>>((int)nmeshes, d_root_node,
+                                                                       pos, skip, e.meshes);
+            FWN_CUDA_CHECK(cudaGetLastError());
         }
-        FWN_CUDA_CHECK(cudaMemsetAsync(cnt, 0, (n + 1) * sizeof(int), st));
-        FWN_CUDA_CHECK(cudaMemsetAsync(leaf_list_len, 0, sizeof(int), st));
-        k_emit_count<<<grid_for(nn, 256), 256, 0, st>>>(n, K, keys, parent, first, last, cnt, flags,
-                                                        leaf_list, leaf_list_len);
-        exclusive_scan_i32(cnt, n + 1, scan_tmp, st);
-        k_positions<<<grid_for(nn, 256), 256, 0, st>>>(n, parent, first, last, flags, cnt, pos, skip);
-        k_mesh_roots<<<grid_for(nmeshes, 128), 128, 0, st>>>((int)nmeshes, foff, n, parent, first,
-                                                             last, pos, skip, e.meshes);
         int E = 0, NL = 0;
         FWN_CUDA_CHECK(cudaMemcpyAsync(&E, cnt + n, sizeof(int), cudaMemcpyDeviceToHost, st));
         FWN_CUDA_CHECK(cudaMemcpyAsync(&NL, leaf_list_len, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -855,12 +1233,12 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
         StageRec* stage = dalloc<StageRec>(E, st);
         if (!(e.cfg.records & FWN_RECORDS_MOMENTS)) track(stage);
         else e.stage = stage;
-        FWN_CUDA_CHECK(cudaMemsetAsync(visit, 0, std::max(n - 1, 1) * sizeof(int), st));
+        FWN_CUDA_CHECK(cudaMemsetAsync(visit, 0, (size_t)nint * sizeof(int), st));
         FWN_CUDA_CHECK(cudaMemsetAsync(leaf_count, 0, sizeof(int), st));
         if (NL > 0)
             k_refit<<<grid_for(NL, 128), 128, 0, st>>>(NL, leaf_list, keys, parent, first, last, left,
                                                        right, pos, tri_of_slot, d_V, d_F, voff,
-                                                       stage, visit, status);
+                                                       stage, visit, status, split);
         FWN_CUDA_CHECK(cudaGetLastError());
         FWN_CUDA_CHECK(cudaMalloc(&e.tris, (size_t)n * sizeof(TriF32)));
         FWN_CUDA_CHECK(cudaMalloc(&e.sorted_tri, (size_t)n * sizeof(int)));
@@ -868,23 +1246,25 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
                                                         e.tris, e.sorted_tri);
         // exact radii of the internal nodes from the triangle records (chunks of each node's
         // slot run; the scan's last entry is the chunk total)
-        int* rchunk = (int*)track(dalloc<int>(n, st));
+        int* rchunk = (int*)track(dalloc<int>(num_nodes + 1, st));
         unsigned long long* r2bits = (unsigned long long*)track(dalloc<unsigned long long>(E, st));
         FWN_CUDA_CHECK(cudaMemsetAsync(r2bits, 0, (size_t)E * sizeof(unsigned long long), st));
-        k_radius_chunks<<<grid_for(n, 256), 256, 0, st>>>(n, keys, first, last, flags, rchunk);
-        exclusive_scan_i32(rchunk, n, scan_tmp, st);
+        k_radius_chunks<<<grid_for(num_nodes + 1, 256), 256, 0, st>>>(num_nodes, keys, first, last,
+                                                                      flags, rchunk);
+        exclusive_scan_i32(rchunk, num_nodes + 1, scan_tmp, st);
         if (n > 1) {
             int dev = 0, sms = 0;
             FWN_CUDA_CHECK(cudaGetDevice(&dev));
             FWN_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-            k_node_radius<<<sms * 8, 256, 0, st>>>(n, rchunk, first, last, pos, stage, e.tris,
-                                                   r2bits);
+            k_node_radius<<<sms * 8, 256, 0, st>>>(num_nodes, rchunk, first, last, pos, stage,
+                                                   e.tris, r2bits);
         }
         FWN_CUDA_CHECK(cudaGetLastError());
         if (e.cfg.records & FWN_RECORDS_F32) FWN_CUDA_CHECK(cudaMalloc(&e.nodes32, E * sizeof(NodeF32)));
         if (e.cfg.records & FWN_RECORDS_F64) FWN_CUDA_CHECK(cudaMalloc(&e.nodes64, E * sizeof(NodeF64)));
-        k_convert<<<grid_for(nn, 128), 128, 0, st>>>(n, keys, first, last, flags, pos, skip, stage,
-                                                     r2bits, e.nodes32, e.nodes64, leaf_count);
+        k_convert<<<grid_for(num_nodes, 128), 128, 0, st>>>(num_nodes, keys, first, last, flags, pos,
+                                                            skip, stage, r2bits, e.nodes32,
+                                                            e.nodes64, leaf_count);
         FWN_CUDA_CHECK(cudaGetLastError());
         int lc = 0;
         FWN_CUDA_CHECK(cudaMemcpyAsync(&lc, leaf_count, sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -58,7 +58,7 @@ def lib():
         L.oracle_ref_num_nodes.restype = i64
         L.oracle_ref_query.argtypes = [P, P, i64, C.c_float, P, P, C.c_int]
         L.oracle_ref_query.restype = None
-        L.oracle_lbvh_build.argtypes = [P, P, P, P, i64, C.c_int, C.c_float]
+        L.oracle_lbvh_build.argtypes = [P, P, P, P, i64, C.c_int, C.c_float, C.c_int]
         L.oracle_lbvh_build.restype = P
         L.oracle_lbvh_free.argtypes = [P]
         L.oracle_lbvh_num_nodes.argtypes = [P]
@@ -132,9 +132,12 @@ class RefTree:
 
 
 class LbvhTree:
-    """O3: CPU restatement of the device LBVH build and of the plain FP64 traversal."""
+    """O3: CPU restatement of the device tree builds (builder 0: LBVH over Morton codes with a
+    Karras hierarchy; builder 1: top-down longest-axis midpoint splits) and of the plain FP64
+    traversal."""
 
-    def __init__(self, V, F, leaf_size: int = 8, near_scale: float = 1e-3, voff=None, foff=None):
+    def __init__(self, V, F, leaf_size: int = 8, near_scale: float = 1e-3, voff=None, foff=None,
+                 builder: int = 0):
         self._V, self._F = _f32(V), _i32(F)
         if voff is None:
             voff = [0, len(self._V)]
@@ -143,7 +146,8 @@ class LbvhTree:
         self.foff = np.ascontiguousarray(foff, dtype=np.int64)
         self.nmeshes = len(self.voff) - 1
         self.h = lib().oracle_lbvh_build(_ptr(self._V), _ptr(self.voff), _ptr(self._F),
-                                         _ptr(self.foff), self.nmeshes, leaf_size, near_scale)
+                                         _ptr(self.foff), self.nmeshes, leaf_size, near_scale,
+                                         builder)
         if not self.h:
             raise ValueError("invalid mesh (index out of range or non-finite vertex)")
 

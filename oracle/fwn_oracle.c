@@ -588,8 +588,136 @@ static void lb_combine(const lb_stage* a, const lb_stage* b, lb_stage* R) {
 
 /* Builds the forest; voff/foff are [nmeshes+1] prefix offsets, triangle indices local per mesh.
  * Returns NULL on invalid input (bad index / non-finite referenced vertex). */
+/* Top-down splitting build (builder 1), restating the device's level-synchronous build: a node
+ * of m > K triangles splits its centroids' bounding box at the midpoint of its longest axis
+ * (ties: the lowest axis), split = (lo + hi) * 0.5f, left = centroids below the split, both sides
+ * keeping their order (a stable partition); when every centroid coincides, or the midpoint rounds
+ * down to lo, it splits by position instead (the first m / 2 left), as every node at depth
+ * >= SP_SPATIAL_LEVELS does. Nodes are created here in DFS pre-order, which is the order the
+ * device reaches with its position formula. */
+#define SP_SPATIAL_LEVELS 96
+typedef struct {
+    lb_tree* T;
+    const float* cen;   /* [nf*3] centroids, input triangle order */
+    int32_t* perm;      /* triangle ids, partitioned in place */
+    int32_t* tmp;
+    int K;
+    int64_t E;          /* nodes created so far */
+    int32_t* nfirst;    /* per node (DFS position): slot range and children */
+    int32_t* nlast;
+    int32_t* nleft;
+    int32_t* nright;
+} sp_ctx;
+
+static int32_t sp_build_rec(sp_ctx* c, int64_t b, int64_t e, int depth) {
+    const int32_t id = (int32_t)c->E++;
+    c->nfirst[id] = (int32_t)b;
+    c->nlast[id] = (int32_t)(e - 1);
+    c->nleft[id] = c->nright[id] = -1;
+    const int64_t m = e - b;
+    if (m <= c->K) return id;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int64_t i = b; i < e; ++i)
+        for (int a = 0; a < 3; ++a) {
+            const float x = c->cen[3 * (int64_t)c->perm[i] + a];
+            lo[a] = fminf(lo[a], x);
+            hi[a] = fmaxf(hi[a], x);
+        }
+    int axis = 0;
+    float ext = hi[0] - lo[0];
+    for (int a = 1; a < 3; ++a)
+        if (hi[a] - lo[a] > ext) {
+            ext = hi[a] - lo[a];
+            axis = a;
+        }
+    const float split = (lo[axis] + hi[axis]) * 0.5f;
+    const int spatial = depth < SP_SPATIAL_LEVELS && ext > 0.f && split > lo[axis];
+    int64_t nl = 0;
+    if (spatial) {
+        int64_t k = b;
+        for (int64_t i = b; i < e; ++i)  /* stable partition: left run, then right run */
+            if (c->cen[3 * (int64_t)c->perm[i] + axis] < split) c->tmp[k++] = c->perm[i];
+        nl = k - b;
+        for (int64_t i = b; i < e; ++i)
+            if (!(c->cen[3 * (int64_t)c->perm[i] + axis] < split)) c->tmp[k++] = c->perm[i];
+        memcpy(c->perm + b, c->tmp + b, (size_t)m * sizeof(int32_t));
+    } else {
+        nl = m / 2;
+    }
+    c->nleft[id] = sp_build_rec(c, b, b + nl, depth + 1);
+    c->nright[id] = sp_build_rec(c, b + nl, e, depth + 1);
+    return id;
+}
+
+/* Builder 1 after validation: per-mesh trees side by side (no node spans two meshes), then the
+ * same refit and exact radii as the LBVH. */
+static void lb_split_finish(lb_tree* T, const float* V, const int64_t* voff, const int32_t* F,
+                            const int64_t* foff, int64_t nmeshes, int K, const float* cen) {
+    const int64_t n = T->nf;
+    sp_ctx c;
+    memset(&c, 0, sizeof(c));
+    c.T = T;
+    c.cen = cen;
+    c.K = K;
+    c.perm = (int32_t*)malloc(n * sizeof(int32_t));
+    c.tmp = (int32_t*)malloc(n * sizeof(int32_t));
+    const int64_t cap = 2 * n;
+    c.nfirst = (int32_t*)malloc(cap * sizeof(int32_t));
+    c.nlast = (int32_t*)malloc(cap * sizeof(int32_t));
+    c.nleft = (int32_t*)malloc(cap * sizeof(int32_t));
+    c.nright = (int32_t*)malloc(cap * sizeof(int32_t));
+    for (int64_t t = 0; t < n; ++t) c.perm[t] = (int32_t)t;
+    for (int64_t mm = 0; mm < nmeshes; ++mm) {
+        if (foff[mm + 1] <= foff[mm]) continue;
+        const int32_t r = sp_build_rec(&c, foff[mm], foff[mm + 1], 0);
+        T->root[mm] = r;
+        T->end[mm] = (int32_t)c.E;
+    }
+    const int64_t E = c.E;
+    T->E = E;
+    T->skip = (int32_t*)malloc(E * sizeof(int32_t));
+    T->tbeg = (int32_t*)malloc(E * sizeof(int32_t));
+    T->tcnt = (int32_t*)malloc(E * sizeof(int32_t));
+    T->st = (lb_stage*)calloc(E, sizeof(lb_stage));
+    T->keys = (uint64_t*)malloc(n * sizeof(uint64_t));
+    T->sorted_tri = (int32_t*)malloc(n * sizeof(int32_t));
+    T->tv = (float*)malloc(n * 9 * sizeof(float));
+    int64_t mesh = 0;
+    for (int64_t s = 0; s < n; ++s) {
+        while (foff[mesh + 1] <= s) ++mesh;
+        const int64_t t = c.perm[s];
+        T->keys[s] = (uint64_t)mesh << MORTON_BITS;
+        T->sorted_tri[s] = (int32_t)t;
+        for (int j = 0; j < 3; ++j)
+            for (int a = 0; a < 3; ++a) T->tv[9 * s + 3 * j + a] = V[3 * (voff[mesh] + F[3 * t + j]) + a];
+    }
+    /* skip links: a node's subtree is the run of positions [id, id + size); the next node after
+     * it is the first one starting after its last slot (DFS order) */
+    for (int64_t i = E - 1; i >= 0; --i) {
+        const int leaf = c.nleft[i] < 0;
+        T->tbeg[i] = c.nfirst[i];
+        T->tcnt[i] = leaf ? c.nlast[i] - c.nfirst[i] + 1 : 0;
+        T->skip[i] = leaf ? (int32_t)(i + 1) : T->skip[c.nright[i]];
+    }
+    /* refit in decreasing position (children after parents), then exact radii */
+    for (int64_t i = E - 1; i >= 0; --i) {
+        if (c.nleft[i] < 0) {
+            lb_leaf(T, c.nfirst[i], c.nlast[i], &T->st[i]);
+        } else {
+            lb_combine(&T->st[c.nleft[i]], &T->st[c.nright[i]], &T->st[i]);
+            T->st[i].r = round_up_float(sqrt(lb_node_r2(T, c.nfirst[i], c.nlast[i], T->st[i].P)));
+        }
+    }
+    free(c.perm);
+    free(c.tmp);
+    free(c.nfirst);
+    free(c.nlast);
+    free(c.nleft);
+    free(c.nright);
+}
+
 void* oracle_lbvh_build(const float* V, const int64_t* voff, const int32_t* F, const int64_t* foff,
-                        int64_t nmeshes, int leaf_size, float near_scale) {
+                        int64_t nmeshes, int leaf_size, float near_scale, int builder) {
     lb_tree* T = (lb_tree*)calloc(1, sizeof(lb_tree));
     const int K = leaf_size;
     T->nmeshes = nmeshes;
@@ -631,6 +759,7 @@ void* oracle_lbvh_build(const float* V, const int64_t* voff, const int32_t* F, c
     while ((1ll << mesh_bits) < nmeshes) ++mesh_bits;
     (void)mesh_bits;
     kv_t* kv = (kv_t*)malloc(n * sizeof(kv_t));
+    float* cen = (float*)malloc(n * 3 * sizeof(float));
     int64_t m = 0;
     for (int64_t t = 0; t < n; ++t) {
         while (foff[m + 1] <= t) ++m;
@@ -647,6 +776,7 @@ void* oracle_lbvh_build(const float* V, const int64_t* voff, const int32_t* F, c
                 if (!isfinite(x[j])) goto bad;
             }
             c[a] = ((x[0] + x[1]) + x[2]) / 3.0f;
+            cen[3 * t + a] = c[a];
         }
         {
             const unsigned code = (spread3(quantize10(c[0], T->mlo[3 * m], inv[3 * m])) << 2) |
@@ -656,6 +786,14 @@ void* oracle_lbvh_build(const float* V, const int64_t* voff, const int32_t* F, c
             kv[t].idx = (uint32_t)t;
         }
     }
+    if (builder == 1) {
+        free(kv);
+        lb_split_finish(T, V, voff, F, foff, nmeshes, K, cen);
+        free(cen);
+        free(inv);
+        return T;
+    }
+    free(cen);
     qsort(kv, (size_t)n, sizeof(kv_t), cmp_kv);
     T->keys = (uint64_t*)malloc(n * sizeof(uint64_t));
     T->sorted_tri = (int32_t*)malloc(n * sizeof(int32_t));
@@ -791,6 +929,7 @@ void* oracle_lbvh_build(const float* V, const int64_t* voff, const int32_t* F, c
     return T;
 bad:
     free(kv);
+    free(cen);
     free(inv);
     free(T->root);
     free(T->end);

@@ -45,12 +45,16 @@ def _engine(V, F, **kw):
     return fwn.FastWindingNumber(V, F, **kw)
 
 
-@pytest.mark.parametrize("leaf", [1, 4, 7, 16])
-def test_build_matches_cpu_restatement(torch_cuda, oracle_mod, leaf):
+@pytest.mark.parametrize("leaf,builder", [(1, 0), (4, 0), (7, 0), (16, 0), (1, 1), (4, 1),
+                                          (12, 1), (16, 1)])
+def test_build_matches_cpu_restatement(torch_cuda, oracle_mod, leaf, builder):
+    """Both builders (0: LBVH over Morton codes, 1: top-down longest-axis splits) against their
+    CPU restatements: topology, skip links, leaf ranges, triangle order, centres and radii bit for
+    bit; FP64 moments to 1e-12."""
     g = np.load(GOLDEN / "displaced.npz")
-    eng = _engine(g["V"], g["F"], leaf_size=leaf)
+    eng = _engine(g["V"], g["F"], leaf_size=leaf, builder=builder)
     got = eng.export_tree()
-    ref = oracle_mod.LbvhTree(g["V"], g["F"], leaf_size=leaf).export()
+    ref = oracle_mod.LbvhTree(g["V"], g["F"], leaf_size=leaf, builder=builder).export()
     for k in ("skip", "tri_begin", "tri_count", "sorted_tri", "mesh_root"):
         np.testing.assert_array_equal(got[k], ref[k], err_msg=k)
     np.testing.assert_array_equal(got["center_radius"], ref["center_radius"])
@@ -77,11 +81,12 @@ def test_golden_uv_sphere(torch_cuda, oracle_mod):
     assert np.max(np.abs(xm - g["omega_exact"])) / FOUR_PI <= 1e-5
 
 
-@pytest.mark.parametrize("leaf", [1, 4, 16])
-def test_displaced_near_surface(torch_cuda, oracle_mod, leaf):
+@pytest.mark.parametrize("leaf,builder", [(1, 0), (4, 0), (16, 0), (4, 1), (12, 1)])
+def test_displaced_near_surface(torch_cuda, oracle_mod, leaf, builder):
     g = np.load(GOLDEN / "displaced.npz")
-    eng = _engine(g["V"], g["F"], leaf_size=leaf)
-    ref = oracle_mod.LbvhTree(g["V"], g["F"], leaf_size=leaf).query_f64(g["Q"], beta=2.0)
+    eng = _engine(g["V"], g["F"], leaf_size=leaf, builder=builder)
+    ref = oracle_mod.LbvhTree(g["V"], g["F"], leaf_size=leaf, builder=builder).query_f64(
+        g["Q"], beta=2.0)
     _, _, w64 = _q(eng, torch_cuda, g["Q"], precision=fwn.PRECISION_FP64, omega_f64=True)
     np.testing.assert_allclose(w64, ref, rtol=0, atol=1e-10 * FOUR_PI)
     for trav in (fwn.TRAVERSAL_THREAD, fwn.TRAVERSAL_WARP):
@@ -272,15 +277,16 @@ def test_concurrent_queries_one_handle(torch_cuda):
         np.testing.assert_array_equal(o, ref)
 
 
-def test_forest_matches_cpu_restatement(torch_cuda, oracle_mod):
+@pytest.mark.parametrize("builder", [0, 1])
+def test_forest_matches_cpu_restatement(torch_cuda, oracle_mod, builder):
     fo = W.batched_forest_workload(n_meshes=9, seed=11, f_lo=100, f_hi=20000, q_lo=50, q_hi=3000)
     # add an empty mesh in the middle
     voff = np.insert(fo.voff, 4, fo.voff[4])
     foff = np.insert(fo.foff, 4, fo.foff[4])
     qoff = np.insert(fo.qoff, 4, fo.qoff[4])
-    forest = fwn.Forest(fo.V, voff, fo.F, foff, records=BOTH, leaf_size=8)
+    forest = fwn.Forest(fo.V, voff, fo.F, foff, records=BOTH, leaf_size=8, builder=builder)
     got = forest.export_tree()
-    lb = oracle_mod.LbvhTree(fo.V, fo.F, leaf_size=8, voff=voff, foff=foff)
+    lb = oracle_mod.LbvhTree(fo.V, fo.F, leaf_size=8, voff=voff, foff=foff, builder=builder)
     ref = lb.export()
     for k in ("skip", "tri_begin", "tri_count", "sorted_tri", "mesh_root"):
         np.testing.assert_array_equal(got[k], ref[k], err_msg=k)
@@ -513,3 +519,32 @@ def test_fp64_warp_schedule_matches_thread_form(torch_cuda, oracle_mod, leaf):
     _, _, wx = _q(eng, torch_cuda, Q, precision=fwn.PRECISION_FP64, traversal=fwn.TRAVERSAL_WARP,
                   beta=1e30, omega_f64=True)
     assert np.max(np.abs(wx - g["omega_exact"])) / FOUR_PI <= 1e-10
+
+
+def test_split_builder_degenerate_geometry(torch_cuda, oracle_mod):
+    """The top-down builder on inputs that defeat midpoint splits: 300 copies of one triangle
+    (every centroid equal), a flat grid (one axis of zero extent) and a cluster of nearly equal
+    centroids (the midpoint rounds onto the low end) fall back to splits by position, and the
+    device tree still equals its CPU restatement bit for bit."""
+    tri = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    V1 = np.tile(tri, (300, 1))
+    F1 = np.arange(900, dtype=np.int32).reshape(300, 3)
+    g = np.stack(np.meshgrid(np.arange(20), np.arange(20), indexing="ij"), -1).reshape(-1, 2)
+    V2 = np.concatenate([g, np.zeros((len(g), 1))], 1).astype(np.float32)
+    q = np.arange(19)
+    a = (q[:, None] * 20 + q[None, :]).ravel()
+    F2 = np.concatenate([np.stack([a, a + 20, a + 1], 1), np.stack([a + 1, a + 20, a + 21], 1)]).astype(np.int32)
+    eps = np.float32(1.0) + np.arange(40, dtype=np.float32) * np.finfo(np.float32).eps
+    V3 = np.concatenate([np.stack([eps, eps, eps], 1),
+                         np.stack([eps + 1, eps, eps], 1),
+                         np.stack([eps, eps + 1, eps], 1)]).astype(np.float32)
+    F3 = np.stack([np.arange(40), np.arange(40) + 40, np.arange(40) + 80], 1).astype(np.int32)
+    for V, F in ((V1, F1), (V2, F2), (V3, F3)):
+        for leaf in (1, 4):
+            eng = _engine(V, F, leaf_size=leaf, builder=1)
+            got = eng.export_tree()
+            ref = oracle_mod.LbvhTree(V, F, leaf_size=leaf, builder=1).export()
+            for k in ("skip", "tri_begin", "tri_count", "sorted_tri", "mesh_root"):
+                np.testing.assert_array_equal(got[k], ref[k], err_msg=k)
+            np.testing.assert_array_equal(got["center_radius"], ref["center_radius"])
+            assert got["tri_count"].max() <= leaf

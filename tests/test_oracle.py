@@ -194,3 +194,26 @@ def test_lbvh_rejects_bad_input(oracle_mod):
     Vb[F[0, 0], 1] = np.nan
     with pytest.raises(ValueError):
         oracle_mod.LbvhTree(Vb, F)
+
+
+@pytest.mark.parametrize("builder", [0, 1])
+def test_tree_builders_structure_and_exact_limit(oracle_mod, builder):
+    """Both restated builds give a DFS tree whose leaves hold every triangle once in <= leaf_size
+    runs, with consistent skip links, and whose beta -> infinity traversal is the brute force."""
+    d = W.displaced_icosphere_workload(nu=10, n_queries=300)
+    for leaf in (1, 5, 12):
+        t = oracle_mod.LbvhTree(d.V, d.F, leaf_size=leaf, builder=builder)
+        ex = t.export()
+        E = t.num_nodes
+        skip, tb, tc = ex["skip"], ex["tri_begin"], ex["tri_count"]
+        assert np.all(skip > np.arange(E)) and np.all(skip <= E)
+        leaves = tc > 0
+        assert tc.max() <= leaf and tc[leaves].sum() == len(d.F)
+        covered = np.concatenate([np.arange(b, b + c) for b, c in zip(tb[leaves], tc[leaves])])
+        np.testing.assert_array_equal(np.sort(covered), np.arange(len(d.F)))
+        assert sorted(ex["sorted_tri"]) == list(range(len(d.F)))
+        r = ex["center_radius"][:, 3]
+        assert np.all(r >= 0) and np.all(np.isfinite(r))
+    exact = oracle_mod.brute_f64(d.V, d.F, d.Q)
+    w = oracle_mod.LbvhTree(d.V, d.F, leaf_size=8, builder=builder).query_f64(d.Q, beta=1e30)
+    np.testing.assert_allclose(w, exact, rtol=0, atol=1e-10 * 4 * np.pi)
