@@ -278,6 +278,23 @@ def percentiles(x):
     return {"p50": v[0], "p90": v[1], "p99": v[2], "p99.9": v[3], "max": mx}
 
 
+def cpu_reference(V, F):
+    """The CPU implementation of the reference path for the timed CPU legs: the reference's own
+    FastWindingNumber when a built reference is present under baseline/_ref (kind "reference"),
+    else the speed build of the oracle's restatement O2 (kind "port"). Returns (tree, kind,
+    description)."""
+    import oracle
+    ok, why = oracle.reference_available()
+    if ok:
+        return (oracle.ReferenceEngine(V, F), "reference",
+                "adobe/lagrange lagrange::winding::FastWindingNumber (baseline/_ref), per-point "
+                "solid_angle calls over all host threads")
+    return (oracle.RefTree(V, F, leaf_size=CPU_LEAF, fast=True), "port",
+            "CPU restatement of the reference path (float order-2 Barill tree, beta 2, leaf "
+            f"{CPU_LEAF}, -O3), per-point queries over all host threads; the reference itself: "
+            + why)
+
+
 def cpu_sample(wl, size: int, seed: int = 7):
     """A bounded sample of the workload's queries: half far/box, half near-surface when the
     workload has both kinds, else uniform."""
@@ -307,7 +324,7 @@ def run_reference(args, rank, world):
     wl = make_workload(args)
     nthr = oracle.nthreads_default()
     t0 = time.perf_counter()
-    tree = oracle.RefTree(wl.V, wl.F, leaf_size=CPU_LEAF)
+    tree, kind, what = cpu_reference(wl.V, wl.F)
     build_s = time.perf_counter() - t0
     sample = cpu_sample(wl, args.cpu_sample)
     for _ in range(args.warmup):
@@ -324,16 +341,14 @@ def run_reference(args, rank, world):
         "data": "synthetic",
         "config": {"workload": wl.name, "triangles": int(len(wl.F)), "queries": int(len(wl.Q)),
                    "beta": wl.beta, "leaf_size": CPU_LEAF},
-        "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": nthr, "kind": "port",
+        "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": nthr, "kind": kind,
                          "sample": f"{len(sample)} queries per step (half far, half near-surface "
                                    f"where the workload has both) of the {len(wl.Q)}-query "
                                    f"workload; tree build "
                                    f"{build_s:.2f} s single-thread",
                          "build_s": build_s},
         "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "reference library (jdumas/WindingNumber via lagrange_winding) cannot be built in "
-                "this environment; this arm times the CPU restatement of its algorithm (float "
-                "order-2 Barill tree, beta=2, per-point queries over all host threads)",
+        "note": what,
     }
     print(json.dumps(line), flush=True)
     barrier(dist)
@@ -430,7 +445,7 @@ def measure_soup(dev, *, steps=5, warmup=3, cpu=True):
                                       "note": "includes the beta=2 far-field truncation error"}
         # is_inside against the CPU restatement of the reference tree on every point
         t0 = time.perf_counter()
-        ref = oracle.RefTree(wl.V, wl.F, leaf_size=CPU_LEAF)
+        ref, kind, _ = cpu_reference(wl.V, wl.F)
         om_ref, in_ref = ref.query(wl.Q, beta=wl.beta, nthreads=nthr)
         cpu_s = time.perf_counter() - t0
         band = np.abs(om_ref / FOUR_PI - 0.5) > 1e-3
@@ -440,7 +455,7 @@ def measure_soup(dev, *, steps=5, warmup=3, cpu=True):
             "disagree_outside_band": int(np.sum(ig[band] != in_ref[band])),
             "max_dw_vs_reference_restatement": float(dref.max()),
             "rms_dw_vs_reference_restatement": float(np.sqrt(np.mean(dref ** 2))),
-            "cpu_s": cpu_s}
+            "reference_kind": kind, "cpu_s": cpu_s}
     eng.close()
     del Vd, Fd, Qd, w, ins, w64, flush
     return out
@@ -742,7 +757,7 @@ def run_ours(args, rank, world, local):
         import oracle
         nthr = oracle.nthreads_default()
         t0 = time.perf_counter()
-        tree = oracle.RefTree(wl.V, wl.F, leaf_size=CPU_LEAF)
+        tree, kind, what = cpu_reference(wl.V, wl.F)
         build_s = time.perf_counter() - t0
         sample = cpu_sample(wl, args.cpu_sample)
         tree.query(sample[:1000], nthreads=nthr)
@@ -754,10 +769,9 @@ def run_ours(args, rank, world, local):
         tree.query(s1, beta=wl.beta, nthreads=1)
         dt1 = time.perf_counter() - t0
         result["cpu_baseline"] = {
-            "value": len(sample) / dt, "unit": "queries/s", "cores": nthr, "kind": "port",
+            "value": len(sample) / dt, "unit": "queries/s", "cores": nthr, "kind": kind,
             "sample": f"{len(sample)} queries (half far, half near-surface) of the workload; "
-                      f"float order-2 Barill tree restating the reference path; build "
-                      f"{build_s:.2f} s single-thread",
+                      f"{what}; build {build_s:.2f} s single-thread",
             "single_thread": {"value": len(s1) / dt1, "unit": "queries/s", "sample": len(s1)},
         }
         # is_inside agreement with the restated reference outside the +-1e-3 band, on every point
@@ -995,7 +1009,7 @@ def measure_forest(fo, dev, dist, rank, world, *, leaf=0, builder=0, steps=10, w
             q0, q1 = int(fo.qoff[m]), int(fo.qoff[m + 1])
             idx = np.arange(q0, q1)  # every query of the mesh
             t0 = time.perf_counter()
-            tree = oracle.RefTree(Vm, Fm, leaf_size=CPU_LEAF)
+            tree, kind, what = cpu_reference(Vm, Fm)
             build_s += time.perf_counter() - t0
             t0 = time.perf_counter()
             om, inn = tree.query(fo.Q[idx], beta=fo.beta, nthreads=nthr)
@@ -1005,10 +1019,9 @@ def measure_forest(fo, dev, dist, rank, world, *, leaf=0, builder=0, steps=10, w
             dis += int(np.sum(ih_all[idx][band] != inn[band]))
             maxdw = max(maxdw, float(np.max(np.abs(wh_all[idx] - om)) / FOUR_PI))
         result["cpu_baseline"] = {
-            "value": nq_cpu / t_cpu, "unit": "queries/s", "cores": nthr, "kind": "port",
-            "sample": f"all {nq_cpu} queries of meshes {picks} (float order-2 Barill tree "
-                      f"restating the reference path, one tree per mesh; builds {build_s:.2f} s "
-                      f"single-thread, not in the rate)"}
+            "value": nq_cpu / t_cpu, "unit": "queries/s", "cores": nthr, "kind": kind,
+            "sample": f"all {nq_cpu} queries of meshes {picks}, one tree per mesh ({what}); "
+                      f"builds {build_s:.2f} s single-thread, not in the rate"}
         result["inside_vs_reference"] = {"sample": nq_cpu, "disagree_outside_band": dis,
                                          "max_dw_vs_reference_restatement": maxdw}
     if grid:

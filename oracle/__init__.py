@@ -10,8 +10,11 @@ third-party library jdumas/WindingNumber @ a48b8f555b490afe7aab9159c7daaf83fa2cd
 known-answer tests (tests/test_oracle.py) and committed golden vectors (tests/golden/).
 
 The C sources are in ``fwn_oracle.c`` (O1 FP64 brute force, O2 float Barill tree restating the
-reference path, O3 restatement of the device LBVH build + FP64 traversal). ``build()`` compiles
-them with gcc (``-ffp-contract=off``) into ``oracle/liboracle_fwn.so``.
+reference path, O3 restatement of the device tree builds + FP64 traversal). ``build()`` compiles
+them with gcc (``-ffp-contract=off``) into ``oracle/liboracle_fwn.so`` (the checker) and with -O3
+into ``oracle/liboracle_fwn_fast.so`` (the timed CPU legs). When a built reference is present
+under ``baseline/_ref``, ``ReferenceEngine`` calls the reference's own FastWindingNumber through
+``ref_shim.cpp`` (compiled into ``oracle/_ref``).
 """
 from __future__ import annotations
 
@@ -25,21 +28,117 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 SRC = HERE / "fwn_oracle.c"
 LIB = HERE / "liboracle_fwn.so"
+# The same sources built for speed, for the timed CPU legs of the benchmark: -O3 with the
+# compiler's default floating-point contraction (the checker build keeps every operation
+# separately rounded, which the bit-exact replay of the device build needs; the timed tree
+# evaluation O2 does not).
+LIB_FAST = HERE / "liboracle_fwn_fast.so"
+REF_SHIM = HERE / "ref_shim.cpp"
+REF_DIR = HERE.parent / "baseline" / "_ref"
+REF_LIB = HERE / "_ref" / "libref_shim.so"
 
 _lib = None
+_lib_fast = None
+_ref = None
 
 
-def build(force: bool = False) -> Path:
-    if not force and LIB.exists() and LIB.stat().st_mtime >= SRC.stat().st_mtime:
-        return LIB
-    tmp = LIB.with_suffix(".so.tmp")
-    cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", "-pthread",
-           "-Wall", "-Wno-unused-function", str(SRC), "-o", str(tmp), "-lm"]
+def _compile(out: Path, flags: list[str], force: bool) -> Path:
+    if not force and out.exists() and out.stat().st_mtime >= SRC.stat().st_mtime:
+        return out
+    tmp = out.with_suffix(".so.tmp")
+    cmd = ["gcc", *flags, "-std=c11", "-fPIC", "-shared", "-pthread", "-Wall",
+           "-Wno-unused-function", str(SRC), "-o", str(tmp), "-lm"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, out)
+    return out
+
+
+def build(force: bool = False) -> Path:
+    _compile(LIB_FAST, ["-O3", "-funroll-loops"], force)
+    return _compile(LIB, ["-O2", "-ffp-contract=off"], force)
+
+
+def reference_available():
+    """(True, path) when a built reference is present under baseline/_ref (its headers and
+    liblagrange_winding), with the C shim over its FastWindingNumber compiled into oracle/_ref;
+    else (False, why)."""
+    inc = REF_DIR / "include" / "lagrange" / "winding" / "FastWindingNumber.h"
+    libs = sorted(REF_DIR.glob("**/liblagrange_winding*.so*")) if REF_DIR.exists() else []
+    if not inc.exists() or not libs:
+        return False, ("no built reference under baseline/_ref (lagrange_winding needs Eigen, "
+                       "TBB, spdlog, fmt and jdumas/WindingNumber fetched at configure time; "
+                       "the offline install fails)")
+    if REF_LIB.exists() and REF_LIB.stat().st_mtime >= REF_SHIM.stat().st_mtime:
+        return True, str(REF_LIB)
+    REF_LIB.parent.mkdir(exist_ok=True)
+    libdirs = sorted({str(p.parent) for p in REF_DIR.glob("**/liblagrange*.so*")})
+    cmd = ["g++", "-std=c++17", "-O3", "-fPIC", "-shared", "-pthread", f"-I{REF_DIR / 'include'}",
+           str(REF_SHIM), "-o", str(REF_LIB)]
+    for d in libdirs:
+        cmd += [f"-L{d}", f"-Wl,-rpath,{d}"]
+    cmd += ["-llagrange_winding", "-llagrange_core"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        return False, "the shim over the reference did not compile: " + r.stderr.strip()[-300:]
+    return True, str(REF_LIB)
+
+
+class ReferenceEngine:
+    """The reference's own FastWindingNumber through oracle/ref_shim.cpp (only when
+    reference_available() is true)."""
+
+    def __init__(self, V, F):
+        global _ref
+        ok, path = reference_available()
+        if not ok:
+            raise RuntimeError(path)
+        if _ref is None:
+            L = C.CDLL(path)
+            L.refshim_build.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64]
+            L.refshim_build.restype = C.c_void_p
+            L.refshim_free.argtypes = [C.c_void_p]
+            L.refshim_query.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                                        C.c_void_p, C.c_int]
+            _ref = L
+        self._V, self._F = _f32(V), _i32(F)
+        self.h = _ref.refshim_build(_ptr(self._V), len(self._V), _ptr(self._F), len(self._F))
+
+    def __del__(self):
+        if getattr(self, "h", None) and _ref is not None:
+            _ref.refshim_free(self.h)
+            self.h = None
+
+    def query(self, Q, beta: float = 2.0, nthreads: int | None = None):
+        Q = _f32(Q)
+        om = np.empty(len(Q), np.float32)
+        ins = np.empty(len(Q), np.uint8)
+        _ref.refshim_query(self.h, _ptr(Q), len(Q), _ptr(om), _ptr(ins),
+                           nthreads or nthreads_default())
+        return om, ins
+
+
+def _bind(L):
+    P = C.c_void_p
+    i64 = C.c_int64
+    L.oracle_ref_build.argtypes = [P, i64, P, i64, C.c_int]
+    L.oracle_ref_build.restype = P
+    L.oracle_ref_free.argtypes = [P]
+    L.oracle_ref_num_nodes.argtypes = [P]
+    L.oracle_ref_num_nodes.restype = i64
+    L.oracle_ref_query.argtypes = [P, P, i64, C.c_float, P, P, C.c_int]
+    L.oracle_ref_query.restype = None
+    return L
+
+
+def lib_fast():
+    """The speed build of the same sources (the timed CPU legs only)."""
+    global _lib_fast
+    if _lib_fast is None:
+        build()
+        _lib_fast = _bind(C.CDLL(str(LIB_FAST)))
+    return _lib_fast
 
 
 def lib():
@@ -105,29 +204,31 @@ def brute_f64(V, F, Q, nthreads: int | None = None) -> np.ndarray:
 
 
 class RefTree:
-    """O2: float order-2 Barill tree, the restatement of the reference FastWindingNumber."""
+    """O2: float order-2 Barill tree, the restatement of the reference FastWindingNumber.
+    fast=True uses the speed build (timed CPU legs); the default is the checker build."""
 
-    def __init__(self, V, F, leaf_size: int = 4):
+    def __init__(self, V, F, leaf_size: int = 4, fast: bool = False):
+        self._L = lib_fast() if fast else lib()
         self._V, self._F = _f32(V), _i32(F)
-        self.h = lib().oracle_ref_build(_ptr(self._V), len(self._V), _ptr(self._F), len(self._F),
-                                        leaf_size)
+        self.h = self._L.oracle_ref_build(_ptr(self._V), len(self._V), _ptr(self._F),
+                                          len(self._F), leaf_size)
 
     def __del__(self):
         h = getattr(self, "h", None)
         if h:
-            lib().oracle_ref_free(h)
+            self._L.oracle_ref_free(h)
             self.h = None
 
     @property
     def num_nodes(self) -> int:
-        return lib().oracle_ref_num_nodes(self.h)
+        return self._L.oracle_ref_num_nodes(self.h)
 
     def query(self, Q, beta: float = 2.0, nthreads: int | None = None):
         Q = _f32(Q)
         om = np.empty(len(Q), np.float32)
         ins = np.empty(len(Q), np.uint8)
-        lib().oracle_ref_query(self.h, _ptr(Q), len(Q), beta, _ptr(om), _ptr(ins),
-                               nthreads or nthreads_default())
+        self._L.oracle_ref_query(self.h, _ptr(Q), len(Q), beta, _ptr(om), _ptr(ins),
+                                 nthreads or nthreads_default())
         return om, ins
 
 

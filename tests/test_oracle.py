@@ -217,3 +217,29 @@ def test_tree_builders_structure_and_exact_limit(oracle_mod, builder):
     exact = oracle_mod.brute_f64(d.V, d.F, d.Q)
     w = oracle_mod.LbvhTree(d.V, d.F, leaf_size=8, builder=builder).query_f64(d.Q, beta=1e30)
     np.testing.assert_allclose(w, exact, rtol=0, atol=1e-10 * 4 * np.pi)
+
+
+def test_o2_speed_build_matches_checker(oracle_mod):
+    """The -O3 build of O2 that the timed CPU legs use gives the checker build's answers up to
+    float contraction."""
+    g = np.load(GOLDEN / "uv_sphere.npz")
+    a, ia = oracle_mod.RefTree(g["V"], g["F"], 8).query(g["Q"][:2000], nthreads=2)
+    b, ib = oracle_mod.RefTree(g["V"], g["F"], 8, fast=True).query(g["Q"][:2000], nthreads=2)
+    assert np.max(np.abs(a.astype(np.float64) - b)) / (4 * np.pi) <= 1e-5
+    band = np.abs(a / (4 * np.pi) - 0.5) > 1e-3
+    np.testing.assert_array_equal(ia[band], ib[band])
+
+
+def test_reference_engine_when_present(oracle_mod):
+    """When a built reference is present under baseline/_ref, its own FastWindingNumber (through
+    oracle/ref_shim.cpp) answers like the FP64 brute force on a closed sphere: is_inside equal
+    outside the +-1e-3 band, |dw| within the beta = 2 truncation. Skipped otherwise, with why."""
+    ok, why = oracle_mod.reference_available()
+    if not ok:
+        pytest.skip(why)
+    g = np.load(GOLDEN / "uv_sphere.npz")
+    om, ins = oracle_mod.ReferenceEngine(g["V"], g["F"]).query(g["Q"])
+    exact = g["omega_exact"] / (4 * np.pi)
+    assert np.max(np.abs(om / (4 * np.pi) - exact)) <= 1e-2
+    band = np.abs(exact - 0.5) > 1e-3
+    np.testing.assert_array_equal(ins[band].astype(bool), exact[band] > 0.5)
