@@ -86,6 +86,9 @@ def parse():
     p.add_argument("--no-clocks", action="store_true")
     p.add_argument("--no-graph", action="store_true")  # time plain launches instead of a graph
     p.add_argument("--no-batched", action="store_true")  # default line without forest/soup parts
+    # strong scaling: one query set split over the ranks (contiguous ranges of the query order,
+    # results all-gathered) instead of a full set per rank
+    p.add_argument("--split-queries", action="store_true")
     return p.parse_args()
 
 
@@ -493,7 +496,8 @@ def run_ours(args, rank, world, local):
     wl = make_workload(args)
     if wl.near_mask is None:
         wl.near_mask = np.zeros(len(wl.Q), bool)
-    wl.Q, wl.near_mask = rank_queries(wl.Q, wl.near_mask, rank)
+    if not args.split_queries:  # weak scaling: every rank answers its own full-size set
+        wl.Q, wl.near_mask = rank_queries(wl.Q, wl.near_mask, rank)
     n = len(wl.Q)
     trav = fwn.TRAVERSAL_WARP if args.traversal == "warp" else fwn.TRAVERSAL_THREAD
     Vd = torch.from_numpy(wl.V).to(dev)
@@ -550,6 +554,27 @@ def run_ours(args, rank, world, local):
         graph.replay()
         torch.cuda.synchronize()
         step = graph.replay
+    split_check = None
+    if args.split_queries:
+        # strong scaling: every rank computes the query order of the whole set, answers its
+        # contiguous range of it and all-gathers the results (lagrange_gb300.shard)
+        from lagrange_gb300 import shard
+        gather = shard.torch_all_gather(dist) if dist is not None else (lambda x: [x])
+        r_, w_ = (dist.get_rank(), dist.get_world_size()) if dist is not None else (0, 1)
+
+        def step():
+            order = eng.query_order(Qd)
+            return shard.query_sharded(
+                Qd, order, r_, w_,
+                lambda sub: eng.query(sub.contiguous(), traversal=trav, sort_queries=False),
+                gather)
+        for _ in range(max(1, args.warmup)):
+            step()
+        query_mixed()
+        ws, is_ = step()
+        torch.cuda.synchronize()
+        # each query's result depends on its own walk only, so the split set is bit-identical
+        split_check = bool(torch.equal(ws, w_out) and torch.equal(is_, i_out))
     # work counters (untimed)
     _, _, stats = eng.query(Qd, traversal=trav, block_size=args.block, stats=True)
     torch.cuda.synchronize()
@@ -571,26 +596,33 @@ def run_ours(args, rank, world, local):
     step_ms = [a.elapsed_time(b) for a, b in ev]
     ms = sum(step_ms) / args.steps
     ms = max_over_ranks(dist, ms, dev)
-    value = job_value(n, world, ms / 1e3)
+    # strong scaling: the ranks share one set of n queries; weak: each rank answers n
+    value = n / (ms / 1e3) if args.split_queries else job_value(n, world, ms / 1e3)
     clocks = clk.summary()
 
     result = {
         "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 near field/refit)",
+        "scaling": "strong" if args.split_queries else "weak", "vs_baseline": None,
+        "dtype": "f32 (FP64 near field/refit)",
         "data": "synthetic",
-        "config": {"workload": wl.name, "triangles": int(len(wl.F)), "queries_per_gpu": n,
+        "config": {"workload": wl.name, "triangles": int(len(wl.F)),
+                   "queries_per_gpu": n // world if args.split_queries else n,
                    "beta": wl.beta, "leaf_size": args.leaf,
                    "builder": "split" if builder == fwn.BUILDER_SPLIT else "lbvh",
                    "traversal": "warp" if trav == fwn.TRAVERSAL_WARP else "thread",
                    "block": args.block, "tuning": tuning, "autotuned": tuned,
                    "step": "plain launches" if args.no_graph else "CUDA graph of one query call",
                    "l2": "flushed before every step (256 MB write)",
-                   "parallelism": f"replicas x{world} (query shards, no collective)"},
+                   "parallelism": (f"tree replicas x{world}, one query set split in contiguous "
+                                   f"ranges of the query order, results all-gathered"
+                                   if args.split_queries else
+                                   f"replicas x{world} (query shards, no collective)")},
         "build_ms": min(build_ms), "tree": {"nodes": info["num_nodes"], "leaves": info["num_leaves"],
                                             "device_bytes": info["device_bytes"]},
         "step_ms_min": min(step_ms), "step_ms_median": statistics.median(step_ms),
         "wall_s_timed": t_wall,
+        "split_queries_bit_identical": split_check,
         # per step: keys + 4 sort passes x 3 kernels + traversal + result scatter
         "gpu_launches": (1 + 4 * 3 + 1 + 1) * args.steps,
         "clocks": clocks,
@@ -731,12 +763,19 @@ def run_ours(args, rank, world, local):
 
     # ---- e2e through the C ABI with host buffers ---------------------------------------------
     if not args.no_e2e:
-        Qh = torch.from_numpy(wl.Q).pin_memory()
-        wh = torch.empty(n, dtype=torch.float32).pin_memory()
-        ih = torch.empty(n, dtype=torch.uint8).pin_memory()
+        # strong scaling: each rank's host call takes its contiguous slice of the caller's array
+        if args.split_queries:
+            from lagrange_gb300 import shard
+            q0, q1 = shard.shard_ranges(n, world)[rank]
+        else:
+            q0, q1 = 0, n
+        ne = q1 - q0
+        Qh = torch.from_numpy(wl.Q[q0:q1]).pin_memory()
+        wh = torch.empty(ne, dtype=torch.float32).pin_memory()
+        ih = torch.empty(ne, dtype=torch.uint8).pin_memory()
 
         def e2e_call():
-            fwn._check(L.fwn_query_host(eng.handle, C.c_void_p(Qh.data_ptr()), n,
+            fwn._check(L.fwn_query_host(eng.handle, C.c_void_p(Qh.data_ptr()), ne,
                                         C.c_void_p(wh.data_ptr()), C.c_void_p(ih.data_ptr())))
         e2e_call()
         ts = []
@@ -748,8 +787,9 @@ def run_ours(args, rank, world, local):
             e2e_call()
             ts.append(time.perf_counter() - t0)
         e2e_s = max_over_ranks(dist, sum(ts) / len(ts), dev)
-        result["e2e"] = {"value": job_value(n, world, e2e_s), "unit": "queries/s",
-                         "h2d_bytes_per_step": n * 12, "d2h_bytes_per_step": n * 5,
+        result["e2e"] = {"value": (n / e2e_s) if args.split_queries else job_value(n, world, e2e_s),
+                         "unit": "queries/s",
+                         "h2d_bytes_per_step": ne * 12, "d2h_bytes_per_step": ne * 5,
                          "ms_per_step": e2e_s * 1e3, "api": "fwn_query_host (pinned host buffers)"}
 
     # ---- CPU baseline (rank 0, N=1 only) -----------------------------------------------------
