@@ -42,10 +42,14 @@ struct QCounters {
     unsigned nodes = 0, far = 0, tri = 0, tri64 = 0, steps = 0;
 };
 
+// The mixed form's arithmetic is written with explicit roundings (_rn intrinsics, and fmaf where
+// a fused operation is wanted): the compiler may not contract a product into a neighbouring add
+// on its own, because its choice could differ between the kernels that inline these functions
+// (point walk, grid walk, forest walk, thread walk), and a query must get the same bits from all.
 __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
-    const float y = x - c;
-    const float t = s + y;
-    c = (t - s) - y;
+    const float y = __fsub_rn(x, c);
+    const float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(t, s), y);
     s = t;
 }
 
@@ -67,12 +71,12 @@ __device__ __forceinline__ float taylor_f32(const float4 m0, const float4 m1, co
                                             const float4 m3, const float4 m4, const float4 m5,
                                             float dx, float dy, float dz, float d2, float trM1) {
     const float rinv = rsqrtf(d2);
-    const float rinv2 = rinv * rinv;
-    const float rinv3 = rinv * rinv2;
-    const float xx = dx * dx, yy = dy * dy, zz = dz * dz;
-    const float xy = dx * dy, xz = dx * dz, yz = dy * dz;
+    const float rinv2 = __fmul_rn(rinv, rinv);
+    const float rinv3 = __fmul_rn(rinv, rinv2);
+    const float xx = __fmul_rn(dx, dx), yy = __fmul_rn(dy, dy), zz = __fmul_rn(dz, dz);
+    const float xy = __fmul_rn(dx, dy), xz = __fmul_rn(dx, dz), yz = __fmul_rn(dy, dz);
     const float t0 = fmaf(dx, m0.x, fmaf(dy, m0.y, fmaf(dz, m0.z, trM1)));
-    float t1 = m0.w * dx;
+    float t1 = __fmul_rn(m0.w, dx);
     t1 = fmaf(m1.x, dy, t1);
     t1 = fmaf(m1.y, dz, t1);
     t1 = fmaf(m1.z, xx, t1);
@@ -81,11 +85,11 @@ __device__ __forceinline__ float taylor_f32(const float4 m0, const float4 m1, co
     t1 = fmaf(m2.y, xy, t1);
     t1 = fmaf(m2.z, xz, t1);
     t1 = fmaf(m2.w, yz, t1);
-    const float gx = fmaf(m3.x, dx, fmaf(m3.w, dy, m4.x * dz));  // xxx xxy xxz
-    const float gy = fmaf(m4.y, dx, fmaf(m3.y, dy, m4.z * dz));  // xyy yyy yyz
-    const float gz = fmaf(m4.w, dx, fmaf(m5.x, dy, m3.z * dz));  // xzz yzz zzz
-    const float t2 = fmaf(xx, gx, fmaf(yy, gy, fmaf(zz, gz, m5.y * xy * dz)));
-    return rinv3 * fmaf(rinv2, fmaf(rinv2, t2, t1), t0);
+    const float gx = fmaf(m3.x, dx, fmaf(m3.w, dy, __fmul_rn(m4.x, dz)));  // xxx xxy xxz
+    const float gy = fmaf(m4.y, dx, fmaf(m3.y, dy, __fmul_rn(m4.z, dz)));  // xyy yyy yyz
+    const float gz = fmaf(m4.w, dx, fmaf(m5.x, dy, __fmul_rn(m3.z, dz)));  // xzz yzz zzz
+    const float t2 = fmaf(xx, gx, fmaf(yy, gy, fmaf(zz, gz, __fmul_rn(__fmul_rn(m5.y, xy), dz))));
+    return __fmul_rn(rinv3, fmaf(rinv2, fmaf(rinv2, t2, t1), t0));
 }
 
 __device__ __forceinline__ double taylor_f64(const NodeF64* __restrict__ nd, double dx, double dy,
@@ -134,25 +138,29 @@ __device__ __noinline__ float tri_omega_near64(float v0x, float v0y, float v0z, 
                  bz = (double)v1z - (double)qz;
     const double cx = (double)v2x - (double)qx, cy = (double)v2y - (double)qy,
                  cz = (double)v2z - (double)qz;
-    const double la = sqrt(ax * ax + ay * ay + az * az);
-    const double lb = sqrt(bx * bx + by * by + bz * bz);
-    const double lc = sqrt(cx * cx + cy * cy + cz * cz);
+    const double la = sqrt(fma(ax, ax, fma(ay, ay, __dmul_rn(az, az))));
+    const double lb = sqrt(fma(bx, bx, fma(by, by, __dmul_rn(bz, bz))));
+    const double lc = sqrt(fma(cx, cx, fma(cy, cy, __dmul_rn(cz, cz))));
     if (la == 0.0 || lb == 0.0 || lc == 0.0) return 0.f;
-    const double det = ax * (by * cz - bz * cy) + ay * (bz * cx - bx * cz) + az * (bx * cy - by * cx);
+    const double crx = fma(by, cz, -__dmul_rn(bz, cy)), cry = fma(bz, cx, -__dmul_rn(bx, cz)),
+                 crz = fma(bx, cy, -__dmul_rn(by, cx));
+    const double det = fma(ax, crx, fma(ay, cry, __dmul_rn(az, crz)));
     if (det == 0.0) return 0.f;
-    const double D = la * lb * lc + (ax * bx + ay * by + az * bz) * lc +
-                     (bx * cx + by * cy + bz * cz) * la + (cx * ax + cy * ay + cz * az) * lb;
+    const double ab = fma(ax, bx, fma(ay, by, __dmul_rn(az, bz)));
+    const double bc = fma(bx, cx, fma(by, cy, __dmul_rn(bz, cz)));
+    const double ca = fma(cx, ax, fma(cy, ay, __dmul_rn(cz, az)));
+    const double D = fma(ab, lc, fma(bc, la, fma(ca, lb, __dmul_rn(__dmul_rn(la, lb), lc))));
     const double m = fmax(fabs(det), fabs(D));
     const int ex = max(-1000, min(1000, ((__double2hiint(m) >> 20) & 0x7ff) - 1023));
     const double sc = __hiloint2double((1023 - ex) << 20, 0);  // 2^-ex, exact scaling
-    return 2.0f * atan2f((float)(det * sc), (float)(D * sc));
+    return __fmul_rn(2.0f, atan2f((float)__dmul_rn(det, sc), (float)__dmul_rn(D, sc)));
 }
 
 // sqrt(x) for x >= 0 as x * rsqrt(x): two instructions instead of the correctly rounded square
 // root, a few ulp of error (well inside the mixed form's budget; the ill-conditioned triangles
 // where it could matter are re-evaluated in FP64). Exactly 0 for x = 0.
 __device__ __forceinline__ float sqrt_fast(float x) {
-    return x * rsqrtf(fmaxf(x, 1e-37f));
+    return __fmul_rn(x, rsqrtf(fmaxf(x, 1e-37f)));
 }
 
 template <bool STATS>
@@ -161,28 +169,34 @@ __device__ __forceinline__ float tri_omega_mixed(float v0x, float v0y, float v0z
                                                  float v2z, float rt, float inv_nlen, float qx,
                                                  float qy, float qz, float tau, float cond,
                                                  QCounters& qc) {
-    const float ax = v0x - qx, ay = v0y - qy, az = v0z - qz;
-    const float bx = v1x - qx, by = v1y - qy, bz = v1z - qz;
-    const float cx = v2x - qx, cy = v2y - qy, cz = v2z - qz;
-    const float det = ax * (by * cz - bz * cy) + ay * (bz * cx - bx * cz) + az * (bx * cy - by * cx);
-    const float la = sqrt_fast(ax * ax + ay * ay + az * az);
-    const float lb = sqrt_fast(bx * bx + by * by + bz * bz);
-    const float lc = sqrt_fast(cx * cx + cy * cy + cz * cz);
-    const float D = la * lb * lc + (ax * bx + ay * by + az * bz) * lc +
-                    (bx * cx + by * cy + bz * cz) * la + (cx * ax + cy * ay + cz * az) * lb;
+    const float ax = __fsub_rn(v0x, qx), ay = __fsub_rn(v0y, qy), az = __fsub_rn(v0z, qz);
+    const float bx = __fsub_rn(v1x, qx), by = __fsub_rn(v1y, qy), bz = __fsub_rn(v1z, qz);
+    const float cx = __fsub_rn(v2x, qx), cy = __fsub_rn(v2y, qy), cz = __fsub_rn(v2z, qz);
+    const float crx = fmaf(by, cz, -__fmul_rn(bz, cy)), cry = fmaf(bz, cx, -__fmul_rn(bx, cz)),
+                crz = fmaf(bx, cy, -__fmul_rn(by, cx));
+    const float det = fmaf(ax, crx, fmaf(ay, cry, __fmul_rn(az, crz)));
+    const float la = sqrt_fast(fmaf(ax, ax, fmaf(ay, ay, __fmul_rn(az, az))));
+    const float lb = sqrt_fast(fmaf(bx, bx, fmaf(by, by, __fmul_rn(bz, bz))));
+    const float lc = sqrt_fast(fmaf(cx, cx, fmaf(cy, cy, __fmul_rn(cz, cz))));
+    const float ab = fmaf(ax, bx, fmaf(ay, by, __fmul_rn(az, bz)));
+    const float bc = fmaf(bx, cx, fmaf(by, cy, __fmul_rn(bz, cz)));
+    const float ca = fmaf(cx, ax, fmaf(cy, ay, __fmul_rn(cz, az)));
+    const float prod = __fmul_rn(__fmul_rn(la, lb), lc);
+    const float D = fmaf(ab, lc, fmaf(bc, la, fmaf(ca, lb, prod)));
     // FP64 near field: the triangle is within tau of q (lower bound of the distance:
     // max(plane distance, centroid distance - Rt)) AND its FP32 evaluation is ill-conditioned.
     // The FP32 rounding errors of det and D are ~eps*|a||b||c| each, so the angle error is
     // ~eps*kappa with kappa = |a||b||c| / |(det, D)|; and when D <= 0, a det within its rounding
     // error may carry the wrong sign, i.e. the wrong side of atan2's branch cut (+-pi).
-    const float h = fabsf(det) * inv_nlen;
+    const float h = __fmul_rn(fabsf(det), inv_nlen);
     if (h < tau) {
-        const float sx = ax + bx + cx, sy = ay + by + cy, sz = az + bz + cz;
-        const float dc = sqrt_fast(sx * sx + sy * sy + sz * sz) * (1.0f / 3.0f);
-        if (dc - rt < tau) {
-            const float prod = la * lb * lc;
-            const bool ill = prod > cond * sqrt_fast(fmaf(det, det, D * D)) ||
-                             (D <= 0.f && fabsf(det) <= 1e-6f * prod);
+        const float sx = __fadd_rn(__fadd_rn(ax, bx), cx), sy = __fadd_rn(__fadd_rn(ay, by), cy),
+                    sz = __fadd_rn(__fadd_rn(az, bz), cz);
+        const float dc = __fmul_rn(sqrt_fast(fmaf(sx, sx, fmaf(sy, sy, __fmul_rn(sz, sz)))),
+                                   1.0f / 3.0f);
+        if (__fsub_rn(dc, rt) < tau) {
+            const bool ill = prod > __fmul_rn(cond, sqrt_fast(fmaf(det, det, __fmul_rn(D, D)))) ||
+                             (D <= 0.f && fabsf(det) <= __fmul_rn(1e-6f, prod));
             if (ill) {
                 if (STATS) ++qc.tri64;
                 return tri_omega_near64(v0x, v0y, v0z, v1x, v1y, v1z, v2x, v2y, v2z, qx, qy, qz);
@@ -190,7 +204,7 @@ __device__ __forceinline__ float tri_omega_mixed(float v0x, float v0y, float v0z
         }
     }
     if (la == 0.f || lb == 0.f || lc == 0.f || det == 0.f) return 0.f;
-    return 2.0f * atan2f(det, D);
+    return __fmul_rn(2.0f, atan2f(det, D));
 }
 
 __device__ __forceinline__ void flush_stats(const QCounters& c, unsigned long long* stats) {
