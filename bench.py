@@ -54,11 +54,9 @@ BYTES_TRI = 48
 BYTES_QUERY_IO = 12 + 4 + 1 + 4  # point in, Omega + inside out, sort index
 CPU_LEAF = 8  # leaf size of the CPU restatement of the reference tree, in every CPU timing
 # DRAM bytes (read + write) of one traversal launch, keyed by (workload, leaf size, warp-schedule
-# variant), from one-pass ncu captures (gpu__time_duration, dram__bytes_read/write) of the same
-# bench command lines; other workloads and leaf sizes: not captured (traffic null)
-NCU_TRAFFIC = {("displaced_icosphere_nu316_q10000000", 8, 4): 1.44e9 + 351.02e6,
-               ("displaced_icosphere_nu316_q10000000", 12, 4): 1.37e9 + 334.33e6,
-               ("displaced_icosphere_nu316_q10000000", 16, 4): 1.35e9 + 330.50e6}
+# variant, builder), from one-pass ncu captures (gpu__time_duration, dram__bytes_read/write) of
+# the same bench command lines; other configurations: not captured (traffic null)
+NCU_TRAFFIC = {("displaced_icosphere_nu316_q10000000", 12, 4, 0): 952.36e6 + 57.72e6}
 
 
 def parse():
@@ -670,7 +668,7 @@ def run_ours(args, rank, world, local):
     # the warp-schedule variant the traversal ran (tuning 0 resolves by batch size, as in the
     # library: two queries per lane once the batch fills every SM's warp slots four times)
     variant = tuning or (4 if n >= 4 * props.multi_processor_count * 32 * 64 else 3)
-    traffic = NCU_TRAFFIC.get((wl.name, args.leaf, variant)) if world == 1 else None
+    traffic = NCU_TRAFFIC.get((wl.name, args.leaf, variant, builder)) if world == 1 else None
     hbm_peak = measured_peaks().get("hbm_gbs")
     result["roofline"] = {
         "bound": "fp32", "achieved": achieved, "peak": peak_fp32, "unit": "TFLOP/s",
@@ -684,7 +682,7 @@ def run_ours(args, rank, world, local):
         "peak_nominal": peak_nominal,
         "traffic_source": (f"one-pass ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) "
                            f"of the traversal launch of this workload at leaf {args.leaf}, "
-                           f"variant {variant}" if traffic else
+                           f"variant {variant}, builder {builder}" if traffic else
                            "null: no capture for this workload / leaf / variant"),
         "hbm": ({"achieved_gbs": traffic / (kernel_ms / 1e3) / 1e9, "peak_gbs": hbm_peak,
                  "frac": traffic / (kernel_ms / 1e3) / 1e9 / hbm_peak,
