@@ -100,7 +100,9 @@ typedef struct fwn_config {
                               0 = every triangle within the distance. Default 4 */
     int32_t tuning;        /* warp-schedule variant (set by fwn_autotune): queries per lane and
                               register cap. 1: 1 query per lane, 72 registers; 2: 1, no cap;
-                              3: 1, 64 registers; 4: 2 queries per lane, 64 registers; 5: 2, 80.
+                              3: 1, 64 registers; 4: 2 queries per lane, 64 registers; 5: 2, 80;
+                              6: as 4 with both query slots' Taylor terms in paired f32x2
+                              arithmetic (same results bit for bit).
                               0 (default): 4 for batches that fill the GPU, else 3 */
     int32_t builder;       /* FWN_BUILDER_*. Default FWN_BUILDER_LBVH */
     int32_t reserved[5];
@@ -241,7 +243,7 @@ FWN_API fwn_status fwn_export_moments(fwn_handle h, double* moments);
 
 /* Autotuner (no reference counterpart: the reference has no tunable parameters). For one mesh
  * (DEVICE arrays) and a representative DEVICE sample of query points, builds the tree with both
- * builders for leaf sizes 4, 8, 12 and 16 and times every query schedule (the warp cursor's variants 1-5; thread per
+ * builders for leaf sizes 4, 8, 12 and 16 and times every query schedule (the warp cursor's variants 1-6; thread per
  * query with blocks of 64/128/256) with CUDA events; returns the fastest. Apply it
  * with cfg.builder, cfg.leaf_size, cfg.traversal, cfg.block_size, cfg.tuning. `base` gives beta and the
  * precision knobs (NULL = defaults). cache_path (may be NULL) names a text file keyed by GPU name
@@ -256,7 +258,7 @@ FWN_API fwn_status fwn_autotune(const float* d_vertices, int64_t num_vertices,
  * so its knobs are the builder, the leaf size and the register cap: builds the forest (DEVICE
  * vertex/triangle arrays, HOST offset arrays as in fwn_forest_build_device) with both builders
  * for leaf sizes 4, 8, 12 and 16 and
- * times the forest query with tuning 3, 1, 4 and 5 on the DEVICE points with HOST query_offsets
+ * times the forest query with tuning 3, 1, 4, 5 and 6 on the DEVICE points with HOST query_offsets
  * [num_meshes + 1]. Returns the fastest (builder, leaf size, tuning; traversal WARP, block 128). Cache as
  * in fwn_autotune, keyed also by log2 of the mesh count. Synchronous on `stream`. */
 FWN_API fwn_status fwn_forest_autotune(const float* d_vertices, const int64_t* vertex_offsets,

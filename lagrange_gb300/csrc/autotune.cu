@@ -32,6 +32,7 @@ const Candidate kCandidates[] = {
     {FWN_TRAVERSAL_WARP, 128, 2},    // 1 query per lane, no register cap
     {FWN_TRAVERSAL_WARP, 128, 4},    // 2 queries per lane, 64-register cap
     {FWN_TRAVERSAL_WARP, 128, 5},    // 2 queries per lane, 80-register cap
+    {FWN_TRAVERSAL_WARP, 128, 6},    // 2 queries per lane, 64-register cap, paired Taylor terms
     {FWN_TRAVERSAL_THREAD, 64, 0},   // thread per query
     {FWN_TRAVERSAL_THREAD, 128, 0},
     {FWN_TRAVERSAL_THREAD, 256, 0},
@@ -235,7 +236,7 @@ extern "C" FWN_API fwn_status fwn_forest_autotune(const float* d_V, const int64_
             e.cfg.builder = builder;
             FWN_CUDA_CHECK(cudaGetDevice(&e.device));
             build_forest(e, d_V, vertex_offsets, d_F, triangle_offsets, num_meshes, st);
-            for (int tuning : {3, 1, 4, 5}) {  // warp-schedule variants (queries per lane, cap)
+            for (int tuning : {3, 1, 4, 5, 6}) {  // warp-schedule variants (queries per lane, cap)
                 QueryArgs a = resolve_query_args(e, nullptr);
                 a.precision = FWN_PRECISION_MIXED;
                 a.tuning = tuning;

@@ -92,6 +92,60 @@ __device__ __forceinline__ float taylor_f32(const float4 m0, const float4 m1, co
     return __fmul_rn(rinv3, fmaf(rinv2, fmaf(rinv2, t2, t1), t0));
 }
 
+// ---- paired f32x2 arithmetic (sm_100+): two FP32 lanes per instruction on a 64-bit register
+// pair. Each half rounds exactly like the scalar instruction, so a paired evaluation gives the
+// scalar results bit for bit while issuing half as many FP32 instructions.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 pk2(float lo, float hi) {
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void upk2(f32x2 v, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+    f32x2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 bc2(float x) { return pk2(x, x); }
+
+// taylor_f32 for two query slots at once (halves: slot 0, slot 1), the same operations in the
+// same order, so each half equals the scalar taylor_f32 of its slot.
+__device__ __forceinline__ void taylor_f32x2(const float4 m0, const float4 m1, const float4 m2,
+                                             const float4 m3, const float4 m4, const float4 m5,
+                                             float trM1, float dx0, float dy0, float dz0,
+                                             float d20, float dx1, float dy1, float dz1,
+                                             float d21, float& out0, float& out1) {
+    const f32x2 rinv = pk2(rsqrtf(d20), rsqrtf(d21));
+    const f32x2 rinv2 = mul2(rinv, rinv);
+    const f32x2 rinv3 = mul2(rinv, rinv2);
+    const f32x2 DX = pk2(dx0, dx1), DY = pk2(dy0, dy1), DZ = pk2(dz0, dz1);
+    const f32x2 XX = mul2(DX, DX), YY = mul2(DY, DY), ZZ = mul2(DZ, DZ);
+    const f32x2 XY = mul2(DX, DY), XZ = mul2(DX, DZ), YZ = mul2(DY, DZ);
+    const f32x2 t0 = fma2(DX, bc2(m0.x), fma2(DY, bc2(m0.y), fma2(DZ, bc2(m0.z), bc2(trM1))));
+    f32x2 t1 = mul2(bc2(m0.w), DX);
+    t1 = fma2(bc2(m1.x), DY, t1);
+    t1 = fma2(bc2(m1.y), DZ, t1);
+    t1 = fma2(bc2(m1.z), XX, t1);
+    t1 = fma2(bc2(m1.w), YY, t1);
+    t1 = fma2(bc2(m2.x), ZZ, t1);
+    t1 = fma2(bc2(m2.y), XY, t1);
+    t1 = fma2(bc2(m2.z), XZ, t1);
+    t1 = fma2(bc2(m2.w), YZ, t1);
+    const f32x2 gx = fma2(bc2(m3.x), DX, fma2(bc2(m3.w), DY, mul2(bc2(m4.x), DZ)));
+    const f32x2 gy = fma2(bc2(m4.y), DX, fma2(bc2(m3.y), DY, mul2(bc2(m4.z), DZ)));
+    const f32x2 gz = fma2(bc2(m4.w), DX, fma2(bc2(m5.x), DY, mul2(bc2(m3.z), DZ)));
+    const f32x2 t2 = fma2(XX, gx, fma2(YY, gy, fma2(ZZ, gz, mul2(mul2(bc2(m5.y), XY), DZ))));
+    upk2(mul2(rinv3, fma2(rinv2, fma2(rinv2, t2, t1), t0)), out0, out1);
+}
+
 __device__ __forceinline__ double taylor_f64(const NodeF64* __restrict__ nd, double dx, double dy,
                                              double dz, double d2) {
     const double rinv = 1.0 / sqrt(d2);
@@ -417,7 +471,7 @@ struct WarpSmem {
     float res[32 * QPL * WARP_LEAF_MAX];
 };
 
-template <bool STATS, int QPL>
+template <bool STATS, int QPL, bool PAIRED = false>
 __device__ __forceinline__ void warp_walk(const NodeF32* __restrict__ nodes,
                                           const TriF32* __restrict__ tris, Slot (&sl)[QPL],
                                           float cond, float beta, WarpSmem<QPL>& sm,
@@ -463,14 +517,29 @@ __device__ __forceinline__ void warp_walk(const NodeF32* __restrict__ nodes,
         float4 an = a;
         int4 bn = b;
         if (nc != DONE) load_sector0(nodes + nc, an, bn);  // next step's test sector, in flight
+        if constexpr (PAIRED && QPL == 2) {
+            // both slots' Taylor terms in one paired evaluation when any lane of either is far
+            if (__any_sync(0xffffffffu, do_far[0] || do_far[1])) {
+                float t[2];
+                taylor_f32x2(m0, m1, m2, m3, m4, m5, __int_as_float(b.w), dx[0], dy[0], dz[0],
+                             d2[0], dx[QPL - 1], dy[QPL - 1], dz[QPL - 1], d2[QPL - 1], t[0], t[1]);
 #pragma unroll
-        for (int j = 0; j < QPL; ++j) {
-            if (__any_sync(0xffffffffu, do_far[j])) {  // warp-uniform: all lanes evaluate
-                const float t = taylor_f32(m0, m1, m2, m3, m4, m5, dx[j], dy[j], dz[j], d2[j],
-                                           __int_as_float(b.w));
-                if (do_far[j]) {
-                    kahan_add(sl[j].s, sl[j].c, t);
-                    if (STATS) ++qc.far;
+                for (int j = 0; j < QPL; ++j)
+                    if (do_far[j]) {
+                        kahan_add(sl[j].s, sl[j].c, t[j]);
+                        if (STATS) ++qc.far;
+                    }
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < QPL; ++j) {
+                if (__any_sync(0xffffffffu, do_far[j])) {  // warp-uniform: all lanes evaluate
+                    const float t = taylor_f32(m0, m1, m2, m3, m4, m5, dx[j], dy[j], dz[j], d2[j],
+                                               __int_as_float(b.w));
+                    if (do_far[j]) {
+                        kahan_add(sl[j].s, sl[j].c, t);
+                        if (STATS) ++qc.far;
+                    }
                 }
             }
         }
@@ -538,7 +607,7 @@ __device__ __forceinline__ void write_result(const Slot& s, int64_t qi, float* _
 // One mesh: each warp takes the next 32 * QPL queries of the (sorted) order. With sorted_omega
 // the results go, coalesced, to position k of the sorted order (k_scatter_results then writes
 // them to the callers' indices in one pass); otherwise to the callers' indices directly.
-template <bool STATS, int MINB, int QPL>
+template <bool STATS, int MINB, int QPL, bool PAIRED = false>
 __global__ void __launch_bounds__(WARP_BLOCK, MINB)
 k_query_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
              const MeshInfo mi, const float* __restrict__ Q, const uint32_t* __restrict__ order,
@@ -565,7 +634,7 @@ k_query_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
         sl[j].resume = valid ? mi.root : DONE;
         sl[j].end = mi.end;
     }
-    warp_walk<STATS, QPL>(nodes, tris, sl, mi.cond, beta, smem[w], qc, status);
+    warp_walk<STATS, QPL, PAIRED>(nodes, tris, sl, mi.cond, beta, smem[w], qc, status);
 #pragma unroll
     for (int j = 0; j < QPL; ++j) {
         if (qi[j] < 0) continue;
@@ -594,7 +663,7 @@ __global__ void k_scatter_results(const float* __restrict__ sorted_omega,
 // index i + nx (j + ny k). Each warp takes one 4 x 4 x (2 QPL) brick of voxels (bricks in raster
 // order; slot q of a lane holds layer pair q), so a warp's queries are spatially compact without
 // a sort; no point array is read.
-template <int MINB, int QPL>
+template <int MINB, int QPL, bool PAIRED = false>
 __global__ void __launch_bounds__(WARP_BLOCK, MINB)
 k_query_grid(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
              const MeshInfo mi, float ox, float oy, float oz, float sx, float sy, float sz,
@@ -623,7 +692,7 @@ k_query_grid(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
         sl[q].end = mi.end;
     }
     QCounters qc;
-    warp_walk<false, QPL>(nodes, tris, sl, mi.cond, beta, smem[w], qc, status);
+    warp_walk<false, QPL, PAIRED>(nodes, tris, sl, mi.cond, beta, smem[w], qc, status);
 #pragma unroll
     for (int q = 0; q < QPL; ++q)
         if (out[q] >= 0) write_result(sl[q], out[q], omega, inside);
@@ -632,7 +701,7 @@ k_query_grid(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
 // Forest: one persistent launch over all meshes. Queries are sorted by (mesh, Hilbert index); each
 // warp takes the next 32 * QPL sorted queries from a global work counter until none are left. A
 // slot's walk ends at its own mesh's subtree end, so a warp may serve queries of two meshes.
-template <int MINB, int QPL>
+template <int MINB, int QPL, bool PAIRED = false>
 __global__ void __launch_bounds__(WARP_BLOCK, MINB)
 k_forest_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
               const MeshInfo* __restrict__ meshes, const float* __restrict__ Q,
@@ -670,7 +739,7 @@ k_forest_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris
                 sl[j].resume = sl[j].end = DONE;
             }
         }
-        warp_walk<false, QPL>(nodes, tris, sl, cond, beta, smem[w], qc, status);
+        warp_walk<false, QPL, PAIRED>(nodes, tris, sl, cond, beta, smem[w], qc, status);
 #pragma unroll
         for (int j = 0; j < QPL; ++j) {
             if (qi[j] < 0) continue;
@@ -918,6 +987,7 @@ inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 
 // Warp-schedule variants (fwn_config::tuning): queries per lane and register cap.
 //   1: 1 query per lane, 72 registers      2: 1 per lane, no cap     3: 1 per lane, 64 registers
 //   4: 2 queries per lane, 64 registers    5: 2 per lane, 80 registers
+//   6: 2 queries per lane, 64 registers, both slots' Taylor terms in paired f32x2 arithmetic
 //   0 (default): 4 when the batch fills every SM's warp slots four times over at two queries per
 //   lane, else 3 (with fewer queries, two per lane would leave SMs idle)
 int warp_variant(int tuning, int64_t n) {
@@ -929,12 +999,12 @@ int warp_variant(int tuning, int64_t n) {
     return n >= 4 * wave ? 4 : 3;
 }
 
-template <int MINB, int QPL>
+template <int MINB, int QPL, bool PAIRED = false>
 void launch_query_warp(const Engine& e, const MeshInfo& mi, const float* d_points,
                        const uint32_t* order, int64_t n, float beta, float* d_omega,
                        uint8_t* d_inside, float* sorted_omega, unsigned* d_status,
                        cudaStream_t st) {
-    k_query_warp<false, MINB, QPL><<<grid_for(n, WARP_BLOCK * QPL), WARP_BLOCK, 0, st>>>(
+    k_query_warp<false, MINB, QPL, PAIRED><<<grid_for(n, WARP_BLOCK * QPL), WARP_BLOCK, 0, st>>>(
         e.nodes32, e.tris, mi, d_points, order, n, beta, d_omega, d_inside, sorted_omega,
         d_status, nullptr);
 }
@@ -952,6 +1022,7 @@ void launch_query_warp_variant(int variant, const Engine& e, const MeshInfo& mi,
         case 2: launch_query_warp<1, 1>(e, mi, d_points, order, n, beta, d_omega, d_inside, so, d_status, st); break;
         case 4: launch_query_warp<8, 2>(e, mi, d_points, order, n, beta, d_omega, d_inside, so, d_status, st); break;
         case 5: launch_query_warp<6, 2>(e, mi, d_points, order, n, beta, d_omega, d_inside, so, d_status, st); break;
+        case 6: launch_query_warp<8, 2, true>(e, mi, d_points, order, n, beta, d_omega, d_inside, so, d_status, st); break;
         default: launch_query_warp<8, 1>(e, mi, d_points, order, n, beta, d_omega, d_inside, so, d_status, st); break;
     }
     if (so) k_scatter_results<<<grid_for(n, 256), 256, 0, st>>>(so, order, n, d_omega, d_inside);
@@ -975,7 +1046,7 @@ QueryArgs resolve_query_args(const Engine& e, const fwn_query_opts* o) {
         if (o->beta > 0.f) a.beta = o->beta;
         if (o->tuning > 0) a.tuning = o->tuning;
     }
-    if (a.tuning < 0 || a.tuning > 5) throw Error(FWN_INVALID_ARG, "tuning must be in [0, 5]");
+    if (a.tuning < 0 || a.tuning > 6) throw Error(FWN_INVALID_ARG, "tuning must be in [0, 6]");
     if (a.precision != FWN_PRECISION_MIXED && a.precision != FWN_PRECISION_FP64)
         throw Error(FWN_INVALID_ARG, "unknown precision");
     // AUTO: the warp walk for the mixed form; for the FP64 form the plain thread-per-query walk
@@ -1110,7 +1181,7 @@ void query_grid(const Engine& e, int mesh, const QueryArgs& a, const float origi
     FWN_CUDA_CHECK(cudaMemsetAsync(status.p, 0, sizeof(unsigned), st));
     const int64_t threads = nbricks * 32;
     auto kern = v == 1 ? k_query_grid<7, 1> : v == 2 ? k_query_grid<1, 1> : v == 4 ? k_query_grid<8, 2>
-              : v == 5 ? k_query_grid<6, 2> : k_query_grid<8, 1>;
+              : v == 5 ? k_query_grid<6, 2> : v == 6 ? k_query_grid<8, 2, true> : k_query_grid<8, 1>;
     kern<<<grid_for(threads, WARP_BLOCK), WARP_BLOCK, 0, st>>>(
         e.nodes32, e.tris, mi, origin[0], origin[1], origin[2], spacing[0], spacing[1], spacing[2],
         nx, ny, nz, bx, by, nbricks, a.beta, d_omega, d_inside, status.as<unsigned>());
@@ -1190,7 +1261,7 @@ void query_forest(const Engine& e, const QueryArgs& a, const float* d_points,
     const int v = warp_variant(a.tuning, n);
     const int qpl = v >= 4 ? 2 : 1;
     auto kern = v == 1 ? k_forest_warp<7, 1> : v == 2 ? k_forest_warp<1, 1> : v == 4 ? k_forest_warp<8, 2>
-              : v == 5 ? k_forest_warp<6, 2> : k_forest_warp<8, 1>;
+              : v == 5 ? k_forest_warp<6, 2> : v == 6 ? k_forest_warp<8, 2, true> : k_forest_warp<8, 1>;
     FWN_CUDA_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, WARP_BLOCK, 0));
     const int64_t chunks = (n + 32 * qpl - 1) / (32 * qpl);
     const int64_t want = (chunks + WARP_BLOCK / 32 - 1) / (WARP_BLOCK / 32);
