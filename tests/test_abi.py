@@ -56,7 +56,8 @@ def test_invalid_arguments_rejected_on_host(engine_lib):
                              ("leaf_size", 0, "leaf_size"), ("records", 4, "records"),
                              ("block_size", 48, "block_size"), ("precision", 7, "precision"),
                              ("fp64_near_scale", -1.0, "fp64_near_scale"), ("tuning", 7, "tuning"),
-                             ("tuning", -1, "tuning"), ("fp64_cond", -1.0, "fp64_cond")):
+                             ("tuning", -1, "tuning"), ("fp64_cond", -1.0, "fp64_cond"),
+                             ("builder", 2, "builder")):
         cfg = fwn.config_default(**{field: val})
         st, msg, _ = _build_status(V.ctypes.data_as(C.c_void_p), 3, None, 0, cfg)
         assert st == 1 and frag in msg, (field, msg)
