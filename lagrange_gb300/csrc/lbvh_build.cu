@@ -321,73 +321,87 @@ struct SplitSlots {
     int* seg;   // active segment of the slot at this level (-1: in a leaf)
 };
 
-__global__ void k_split_init(const float* __restrict__ V, const int32_t* __restrict__ F,
-                             const int64_t* __restrict__ voff, const int64_t* __restrict__ foff,
-                             int nmeshes, int64_t nf, const int* __restrict__ mesh_seg,
-                             SplitSlots out, int* __restrict__ final_perm,
-                             uint64_t* __restrict__ keys, unsigned* __restrict__ status) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nf) return;
-    const int m = find_mesh(foff, nmeshes, t);
-    const int64_t nvm = voff[m + 1] - voff[m];
-    float c[3] = {0.f, 0.f, 0.f};
-    bool ok = true;
-    int32_t idx[3];
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-        idx[j] = F[3 * t + j];
-        if (idx[j] < 0 || (int64_t)idx[j] >= nvm) ok = false;
-    }
-    if (!ok) {
-        atomicOr(status, ST_BAD_INDEX);
-    } else {
-        float v[3][3];
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            const float* p = V + 3 * (voff[m] + idx[j]);
-            v[j][0] = p[0];
-            v[j][1] = p[1];
-            v[j][2] = p[2];
-            if (!isfinite(v[j][0]) || !isfinite(v[j][1]) || !isfinite(v[j][2])) ok = false;
-        }
-        if (!ok) atomicOr(status, ST_NONFINITE);
-#pragma unroll
-        for (int a = 0; a < 3; ++a) c[a] = ((v[0][a] + v[1][a]) + v[2][a]) / 3.0f;
-    }
-    const int sg = mesh_seg[m];
-    out.perm[t] = (int)t;
-    out.cx[t] = c[0];
-    out.cy[t] = c[1];
-    out.cz[t] = c[2];
-    out.seg[t] = sg;
-    if (sg < 0) final_perm[t] = (int)t;  // the whole mesh is one leaf
-    keys[t] = (uint64_t)m << MORTON_BITS;
-}
-
-__global__ void k_split_box_init(int nact, unsigned* __restrict__ box) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < 6 * nact) box[i] = (i % 6) < 3 ? 0xffffffffu : 0u;
-}
-
-// Centroid box per active segment: lanes of a warp that hold the same segment reduce together
-// (ordered-int encodings, so min / max are integer reductions), one atomic per group and axis.
-__global__ void k_split_box(int64_t n, SplitSlots cur, unsigned* __restrict__ box) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int sg = i < n ? cur.seg[i] : -1;
-    const unsigned act = __ballot_sync(0xffffffffu, sg >= 0);
-    if (sg < 0) return;
-    const unsigned peers = __match_any_sync(act, sg);
+// Centroid boxes: lanes of a warp that add to the same box reduce together first (ordered-int
+// encodings, so min / max are integer reductions), then one atomic per group and axis. Every
+// lane of the warp must call it; lanes with key < 0 add nothing.
+__device__ __forceinline__ void box_add(int key, float cx, float cy, float cz,
+                                        unsigned* __restrict__ box) {
+    const unsigned act = __ballot_sync(0xffffffffu, key >= 0);
+    if (key < 0) return;
+    const unsigned peers = __match_any_sync(act, key);
     const bool leader = (threadIdx.x & 31) == (unsigned)(__ffs(peers) - 1);
-    const float c[3] = {cur.cx[i], cur.cy[i], cur.cz[i]};
+    const float c[3] = {cx, cy, cz};
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         const unsigned e = enc_float(c[a]);
         const unsigned lo = __reduce_min_sync(peers, e), hi = __reduce_max_sync(peers, e);
         if (leader) {
-            atomicMin(&box[6 * sg + a], lo);
-            atomicMax(&box[6 * sg + 3 + a], hi);
+            atomicMin(&box[6 * key + a], lo);
+            atomicMax(&box[6 * key + 3 + a], hi);
         }
     }
+}
+
+__device__ __forceinline__ void box_clear(unsigned* __restrict__ b) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        b[a] = 0xffffffffu;  // min of nothing
+        b[3 + a] = 0u;       // max of nothing
+    }
+}
+
+__global__ void k_split_box_init(int nact, unsigned* __restrict__ box) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nact) box_clear(box + 6 * i);
+}
+
+// Validation, centroids and the first level's slots; the boxes of the first level's segments
+// (the meshes of > leaf_size triangles) accumulate here too.
+__global__ void k_split_init(const float* __restrict__ V, const int32_t* __restrict__ F,
+                             const int64_t* __restrict__ voff, const int64_t* __restrict__ foff,
+                             int nmeshes, int64_t nf, const int* __restrict__ mesh_seg,
+                             SplitSlots out, int* __restrict__ final_perm,
+                             uint64_t* __restrict__ keys, unsigned* __restrict__ box,
+                             unsigned* __restrict__ status) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int key = -1;
+    float c[3] = {0.f, 0.f, 0.f};
+    if (t < nf) {
+        const int m = find_mesh(foff, nmeshes, t);
+        const int64_t nvm = voff[m + 1] - voff[m];
+        bool ok = true;
+        int32_t idx[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            idx[j] = F[3 * t + j];
+            if (idx[j] < 0 || (int64_t)idx[j] >= nvm) ok = false;
+        }
+        if (!ok) {
+            atomicOr(status, ST_BAD_INDEX);
+        } else {
+            float v[3][3];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const float* p = V + 3 * (voff[m] + idx[j]);
+                v[j][0] = p[0];
+                v[j][1] = p[1];
+                v[j][2] = p[2];
+                if (!isfinite(v[j][0]) || !isfinite(v[j][1]) || !isfinite(v[j][2])) ok = false;
+            }
+            if (!ok) atomicOr(status, ST_NONFINITE);
+#pragma unroll
+            for (int a = 0; a < 3; ++a) c[a] = ((v[0][a] + v[1][a]) + v[2][a]) / 3.0f;
+        }
+        key = mesh_seg[m];
+        out.perm[t] = (int)t;
+        out.cx[t] = c[0];
+        out.cy[t] = c[1];
+        out.cz[t] = c[2];
+        out.seg[t] = key;
+        if (key < 0) final_perm[t] = (int)t;  // the whole mesh is one leaf
+        keys[t] = (uint64_t)m << MORTON_BITS;
+    }
+    box_add(key, c[0], c[1], c[2], box);
 }
 
 __global__ void k_split_decide(int nact, bool by_position, const unsigned* __restrict__ box,
@@ -439,82 +453,83 @@ __global__ void k_split_flags(int64_t n, SplitSlots cur, const int* __restrict__
     flags[i] = f;  // flags[n] = 0: the scan's total entry
 }
 
-// Children of every active segment (lf = exclusive scan of the left flags); cact[c] = 1 when
-// child c (2s left, 2s + 1 right) stays active; cact[2 nact] = 0 for the scan's total.
+// Children of every active segment (lf = exclusive scan of the left flags): the two nodes, and
+// for each child of > K triangles a slot of the next level (allocated with an atomic counter,
+// its box cleared); child_next[2s + c] = that slot or -1 for a leaf. The next level's order of
+// segments is immaterial: positions come from the node ranges alone.
 __global__ void k_split_children(int nact, int node_base, int K, const int* __restrict__ s_start,
                                  const int* __restrict__ s_end, const int* __restrict__ s_node,
                                  const int* __restrict__ lf, int* __restrict__ nfirst,
                                  int* __restrict__ nlast, int* __restrict__ nparent,
                                  int* __restrict__ nleft, int* __restrict__ nright,
-                                 int* __restrict__ cact) {
+                                 int* __restrict__ next_count, int* __restrict__ n_start,
+                                 int* __restrict__ n_end, int* __restrict__ n_node,
+                                 unsigned* __restrict__ n_box, int* __restrict__ child_next) {
     const int sg = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sg > nact) return;
-    if (sg == nact) {
-        cact[2 * nact] = 0;
-        return;
-    }
-    const int b = s_start[sg], e = s_end[sg], nl = lf[e] - lf[b];
+    if (sg >= nact) return;
+    const int b = s_start[sg], e = s_end[sg], mid = b + (lf[e] - lf[b]);
     const int l = node_base + 2 * sg, r = l + 1, p = s_node[sg];
     nfirst[l] = b;
-    nlast[l] = b + nl - 1;
-    nfirst[r] = b + nl;
+    nlast[l] = mid - 1;
+    nfirst[r] = mid;
     nlast[r] = e - 1;
     nparent[l] = p;
     nparent[r] = p;
     nleft[l] = nright[l] = nleft[r] = nright[r] = -1;
     nleft[p] = l;
     nright[p] = r;
-    cact[2 * sg] = nl > K ? 1 : 0;
-    cact[2 * sg + 1] = (e - b - nl) > K ? 1 : 0;
-}
-
-// The next level's active segments (cs = exclusive scan of cact).
-__global__ void k_split_next(int nact, int node_base, const int* __restrict__ s_start,
-                             const int* __restrict__ s_end, const int* __restrict__ lf,
-                             const int* __restrict__ cs, int* __restrict__ n_start,
-                             int* __restrict__ n_end, int* __restrict__ n_node) {
-    const int sg = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sg >= nact) return;
-    const int b = s_start[sg], e = s_end[sg], mid = b + (lf[e] - lf[b]);
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
-        const int ch = 2 * sg + c;
-        if (cs[ch + 1] == cs[ch]) continue;
-        const int k = cs[ch];
-        n_start[k] = c == 0 ? b : mid;
-        n_end[k] = c == 0 ? mid : e;
-        n_node[k] = node_base + ch;
+        const int cb = c == 0 ? b : mid, ce = c == 0 ? mid : e;
+        int k = -1;
+        if (ce - cb > K) {
+            k = atomicAdd(next_count, 1);
+            n_start[k] = cb;
+            n_end[k] = ce;
+            n_node[k] = node_base + 2 * sg + c;
+            box_clear(n_box + 6 * k);
+        }
+        child_next[2 * sg + c] = k;
     }
 }
 
 // Stable partition of every active segment: left-flagged slots first, each side in its order.
-// Slots of children that stay active go to the next level's buffers; those of leaves are final.
+// Slots of children that stay active go to the next level's buffers (and into their child's
+// box); those of leaves are final.
 __global__ void k_split_scatter(int64_t n, SplitSlots cur, SplitSlots nxt,
                                 const int* __restrict__ lf, const int* __restrict__ s_start,
-                                const int* __restrict__ s_end, const int* __restrict__ cs,
-                                int* __restrict__ final_perm) {
+                                const int* __restrict__ s_end, const int* __restrict__ child_next,
+                                int* __restrict__ final_perm, unsigned* __restrict__ n_box) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int sg = cur.seg[i];
-    if (sg < 0) {
-        nxt.seg[i] = -1;
-        return;
+    int key = -1;
+    float cx = 0.f, cy = 0.f, cz = 0.f;
+    if (i < n) {
+        const int sg = cur.seg[i];
+        if (sg < 0) {
+            nxt.seg[i] = -1;
+        } else {
+            const int b = s_start[sg], e = s_end[sg];
+            const int fb = lf[b], nl = lf[e] - fb, left_before = lf[i] - fb;
+            const bool left = lf[i + 1] != lf[i];  // the exclusive scan steps where the flag is set
+            const int64_t dest = left ? b + left_before : b + nl + ((int)(i - b) - left_before);
+            const int k = child_next[2 * sg + (left ? 0 : 1)];
+            if (k >= 0) {
+                cx = cur.cx[i];
+                cy = cur.cy[i];
+                cz = cur.cz[i];
+                nxt.perm[dest] = cur.perm[i];
+                nxt.cx[dest] = cx;
+                nxt.cy[dest] = cy;
+                nxt.cz[dest] = cz;
+                nxt.seg[dest] = k;
+                key = k;
+            } else {
+                final_perm[dest] = cur.perm[i];
+                nxt.seg[dest] = -1;
+            }
+        }
     }
-    const int b = s_start[sg], e = s_end[sg];
-    const int fb = lf[b], nl = lf[e] - fb, left_before = lf[i] - fb;
-    const bool left = lf[i + 1] != lf[i];  // the exclusive scan steps where the flag is set
-    const int64_t dest = left ? b + left_before : b + nl + ((int)(i - b) - left_before);
-    const int ch = 2 * sg + (left ? 0 : 1);
-    if (cs[ch + 1] != cs[ch]) {
-        nxt.perm[dest] = cur.perm[i];
-        nxt.cx[dest] = cur.cx[i];
-        nxt.cy[dest] = cur.cy[i];
-        nxt.cz[dest] = cur.cz[i];
-        nxt.seg[dest] = cs[ch];
-    } else {
-        final_perm[dest] = cur.perm[i];
-        nxt.seg[dest] = -1;
-    }
+    box_add(key, cx, cy, cz, n_box);
 }
 
 // Node flags of the split tree (every node emitted; leaves = no children), the per-first-slot
@@ -1134,13 +1149,15 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
                 X->seg = (int*)track(dalloc<int>(n, st));
             }
             int* lflags = (int*)track(dalloc<int>(n + 1, st));
-            int* cact = (int*)track(dalloc<int>(2 * smax + 1, st));
+            int* child_next = (int*)track(dalloc<int>(2 * (size_t)smax, st));
+            int* next_count = (int*)track(dalloc<int>(1, st));
             int* seg_a[3], *seg_b[3];  // start, end, node of this level / the next
             for (int k = 0; k < 3; ++k) {
                 seg_a[k] = (int*)track(dalloc<int>(smax, st));
                 seg_b[k] = (int*)track(dalloc<int>(smax, st));
             }
-            unsigned* box = (unsigned*)track(dalloc<unsigned>(6 * (size_t)smax, st));
+            unsigned* box_a = (unsigned*)track(dalloc<unsigned>(6 * (size_t)smax, st));
+            unsigned* box_b = (unsigned*)track(dalloc<unsigned>(6 * (size_t)smax, st));
             int* axis_of = (int*)track(dalloc<int>(smax, st));
             float* split_of = (float*)track(dalloc<float>(smax, st));
             int* spatial_of = (int*)track(dalloc<int>(smax, st));
@@ -1165,9 +1182,11 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
                                                cudaMemcpyHostToDevice, st));
                 FWN_CUDA_CHECK(cudaMemcpyAsync(seg_a[2], s_node.data(), nact * sizeof(int),
                                                cudaMemcpyHostToDevice, st));
+                k_split_box_init<<<grid_for(nact, 256), 256, 0, st>>>(nact, box_a);
             }
             k_split_init<<<grid_for(n, 256), 256, 0, st>>>(d_V, d_F, voff, foff, (int)nmeshes, nf,
-                                                           d_mesh_seg, A, final_perm, skeys, status);
+                                                           d_mesh_seg, A, final_perm, skeys, box_a,
+                                                           status);
             FWN_CUDA_CHECK(cudaGetLastError());
             check_input();
             int node_base = nroots;
@@ -1178,35 +1197,31 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
                 if (level > kSpatialLevels + 64)  // position splits halve every segment
                     throw Error(FWN_INTERNAL, "split build did not converge");
                 if (node_base + 2 * nact > cap) throw Error(FWN_INTERNAL, "split build node overflow");
-                k_split_box_init<<<grid_for(6 * nact, 256), 256, 0, st>>>(nact, box);
-                k_split_box<<<grid_for(n, 256), 256, 0, st>>>(n, *cur, box);
                 k_split_decide<<<grid_for(nact, 128), 128, 0, st>>>(
-                    nact, level >= kSpatialLevels, box, axis_of, split_of, spatial_of);
+                    nact, level >= kSpatialLevels, box_a, axis_of, split_of, spatial_of);
                 k_split_flags<<<grid_for(n + 1, 256), 256, 0, st>>>(n, *cur, seg_a[0], seg_a[1],
                                                                    axis_of, split_of, spatial_of,
                                                                    lflags);
                 exclusive_scan_i32(lflags, n + 1, scan_tmp, st);
-                k_split_children<<<grid_for(nact + 1, 128), 128, 0, st>>>(
+                FWN_CUDA_CHECK(cudaMemsetAsync(next_count, 0, sizeof(int), st));
+                k_split_children<<<grid_for(nact, 128), 128, 0, st>>>(
                     nact, node_base, K, seg_a[0], seg_a[1], seg_a[2], lflags, first, last, parent,
-                    left, right, cact);
-                exclusive_scan_i32(cact, 2 * nact + 1, scan_tmp, st);
-                k_split_next<<<grid_for(nact, 128), 128, 0, st>>>(nact, node_base, seg_a[0],
-                                                                 seg_a[1], lflags, cact, seg_b[0],
-                                                                 seg_b[1], seg_b[2]);
-                FWN_CUDA_CHECK(cudaGetLastError());
+                    left, right, next_count, seg_b[0], seg_b[1], seg_b[2], box_b, child_next);
                 // lflags now holds the exclusive scan of the left flags (a slot's flag is the
                 // step from its entry to the next)
                 k_split_scatter<<<grid_for(n, 256), 256, 0, st>>>(n, *cur, *nxt, lflags, seg_a[0],
-                                                                 seg_a[1], cact, final_perm);
+                                                                 seg_a[1], child_next, final_perm,
+                                                                 box_b);
                 FWN_CUDA_CHECK(cudaGetLastError());
                 node_base += 2 * nact;
                 int next = 0;
-                FWN_CUDA_CHECK(cudaMemcpyAsync(&next, cact + 2 * nact, sizeof(int),
+                FWN_CUDA_CHECK(cudaMemcpyAsync(&next, next_count, sizeof(int),
                                                cudaMemcpyDeviceToHost, st));
                 FWN_CUDA_CHECK(cudaStreamSynchronize(st));
                 nact = next;
                 ++level;
                 std::swap(cur, nxt);
+                std::swap(box_a, box_b);
                 for (int k = 0; k < 3; ++k) std::swap(seg_a[k], seg_b[k]);
             }
             num_nodes = node_base;
