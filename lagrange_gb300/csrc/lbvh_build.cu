@@ -321,11 +321,41 @@ struct SplitSlots {
     int* seg;   // active segment of the slot at this level (-1: in a leaf)
 };
 
-// Centroid boxes: lanes of a warp that add to the same box reduce together first (ordered-int
-// encodings, so min / max are integer reductions), then one atomic per group and axis. Every
-// lane of the warp must call it; lanes with key < 0 add nothing.
+// Centroid boxes: lanes that add to the same box reduce together first (ordered-int encodings,
+// so min / max are integer reductions), then one atomic per group and axis. When the whole
+// block adds to one box (the top levels, where a segment spans many blocks) the block reduces
+// in shared memory and issues six atomics; otherwise each warp groups its lanes by box. Every
+// thread of the block must call it; threads with key < 0 add nothing.
 __device__ __forceinline__ void box_add(int key, float cx, float cy, float cz,
                                         unsigned* __restrict__ box) {
+    __shared__ int s_key;
+    __shared__ unsigned s_box[6];
+    if (threadIdx.x == 0) {
+        s_key = key;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            s_box[a] = 0xffffffffu;
+            s_box[3 + a] = 0u;
+        }
+    }
+    __syncthreads();
+    if (__syncthreads_and(key >= 0 && key == s_key)) {  // uniform over the block
+        const float c[3] = {cx, cy, cz};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const unsigned e = enc_float(c[a]);
+            const unsigned lo = __reduce_min_sync(0xffffffffu, e);
+            const unsigned hi = __reduce_max_sync(0xffffffffu, e);
+            if ((threadIdx.x & 31) == 0) {
+                atomicMin(&s_box[a], lo);
+                atomicMax(&s_box[3 + a], hi);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x < 3) atomicMin(&box[6 * key + threadIdx.x], s_box[threadIdx.x]);
+        else if (threadIdx.x < 6) atomicMax(&box[6 * key + threadIdx.x], s_box[threadIdx.x]);
+        return;
+    }
     const unsigned act = __ballot_sync(0xffffffffu, key >= 0);
     if (key < 0) return;
     const unsigned peers = __match_any_sync(act, key);
@@ -777,11 +807,26 @@ __global__ void k_refit(int num_leaves, const int* __restrict__ leaf_list,
 // The far test of a node compares |q - P| with beta * r, so r must bound the distance from P to
 // every point of the node's triangles; the tightest such bound is the distance to the farthest
 // vertex (triangles are convex hulls of their vertices). Leaves compute it in leaf_moments. An
-// internal node's triangles are the contiguous run of sorted slots [first, last]: it is split into
-// chunks of kRadiusChunk slots, one warp per chunk, whose maxima meet in an atomicMax on the bit
-// pattern (non-negative doubles order like their bits). The result does not depend on the order,
-// so it equals the serial maximum bit for bit.
+// internal node's triangles are the contiguous run of sorted slots [first, last]. Nodes of at
+// most kRadiusChunk triangles (all but the top few levels) take one warp each
+// (k_node_radius_small); larger ones are split into chunks of kRadiusChunk slots, one warp per
+// chunk, whose maxima meet in an atomicMax on the bit pattern (non-negative doubles order like
+// their bits). A maximum does not depend on the order, so it equals the serial one bit for bit.
 constexpr int kRadiusChunk = 2048;
+
+__device__ __forceinline__ double slots_r2(const TriF32* __restrict__ tris, int s0, int s1,
+                                           const double* P, int lane) {
+    double r2 = 0.0;
+    for (int s = s0 + lane; s < s1; s += 32) {
+        const float4 t0 = tris[s].t0, t1 = tris[s].t1, t2 = tris[s].t2;
+        r2 = fmax(r2, vertex_r2(t0.x, t0.y, t0.z, P));
+        r2 = fmax(r2, vertex_r2(t0.w, t1.x, t1.y, P));
+        r2 = fmax(r2, vertex_r2(t1.z, t1.w, t2.x, P));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r2 = fmax(r2, __shfl_xor_sync(0xffffffffu, r2, o));
+    return r2;
+}
 
 __device__ __forceinline__ bool internal_emitted(const uint64_t* __restrict__ keys,
                                                  const int* __restrict__ first,
@@ -791,16 +836,41 @@ __device__ __forceinline__ bool internal_emitted(const uint64_t* __restrict__ ke
     return (fl & 1) && !(fl & 2) && !is_cross(keys, first, last, u);
 }
 
-// chunks[u] for the nodes u < num_nodes (0 unless an emitted single-mesh internal node);
-// chunks[num_nodes] = 0 becomes the total after the exclusive scan.
+// chunks[u] for the nodes u < num_nodes (0 unless an emitted single-mesh internal node of more than
+// kRadiusChunk triangles); chunks[num_nodes] = 0 becomes the total after the exclusive scan.
 __global__ void k_radius_chunks(int num_nodes, const uint64_t* __restrict__ keys,
                                 const int* __restrict__ first, const int* __restrict__ last,
                                 const uint8_t* __restrict__ flags, int* __restrict__ chunks) {
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u > num_nodes) return;
-    chunks[u] = (u < num_nodes && internal_emitted(keys, first, last, flags, u))
+    chunks[u] = (u < num_nodes && internal_emitted(keys, first, last, flags, u) &&
+                 last[u] - first[u] + 1 > kRadiusChunk)
                     ? (last[u] - first[u] + kRadiusChunk) / kRadiusChunk
                     : 0;
+}
+
+// Nodes of at most kRadiusChunk triangles: each warp scans 32 consecutive node ids and takes the
+// internal ones among them in turn, all lanes on one node.
+__global__ void k_node_radius_small(int num_nodes, const uint64_t* __restrict__ keys,
+                                    const int* __restrict__ first, const int* __restrict__ last,
+                                    const uint8_t* __restrict__ flags, const int* __restrict__ pos,
+                                    const StageRec* __restrict__ stage,
+                                    const TriF32* __restrict__ tris,
+                                    unsigned long long* __restrict__ r2bits) {
+    const int lane = threadIdx.x & 31;
+    const int u0 = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
+    const int u = u0 + lane;
+    const bool mine = u < num_nodes && internal_emitted(keys, first, last, flags, u) &&
+                      last[u] - first[u] + 1 <= kRadiusChunk;
+    unsigned todo = __ballot_sync(0xffffffffu, mine);
+    while (todo) {
+        const int v = u0 + __ffs(todo) - 1;
+        todo &= todo - 1;
+        const int i = pos[v];
+        const double P[3] = {stage[i].P[0], stage[i].P[1], stage[i].P[2]};
+        const double r2 = slots_r2(tris, first[v], last[v] + 1, P, lane);
+        if (lane == 0) r2bits[i] = (unsigned long long)__double_as_longlong(r2);
+    }
 }
 
 // Grid-stride over the chunks: chunk c belongs to the last node u with off[u] <= c.
@@ -823,15 +893,7 @@ __global__ void k_node_radius(int num_nodes, const int* __restrict__ off,
         const int s1 = min(last[u] + 1, s0 + kRadiusChunk);
         const int i = pos[u];
         const double P[3] = {stage[i].P[0], stage[i].P[1], stage[i].P[2]};
-        double r2 = 0.0;
-        for (int s = s0 + lane; s < s1; s += 32) {
-            const float4 t0 = tris[s].t0, t1 = tris[s].t1, t2 = tris[s].t2;
-            r2 = fmax(r2, vertex_r2(t0.x, t0.y, t0.z, P));
-            r2 = fmax(r2, vertex_r2(t0.w, t1.x, t1.y, P));
-            r2 = fmax(r2, vertex_r2(t1.z, t1.w, t2.x, P));
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) r2 = fmax(r2, __shfl_xor_sync(0xffffffffu, r2, o));
+        const double r2 = slots_r2(tris, s0, s1, P, lane);
         if (lane == 0) atomicMax(&r2bits[i], (unsigned long long)__double_as_longlong(r2));
     }
 }
@@ -1259,8 +1321,9 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
         FWN_CUDA_CHECK(cudaMalloc(&e.sorted_tri, (size_t)n * sizeof(int)));
         k_tri_records<<<grid_for(n, 256), 256, 0, st>>>(n, tri_of_slot, keys, d_V, d_F, voff,
                                                         e.tris, e.sorted_tri);
-        // exact radii of the internal nodes from the triangle records (chunks of each node's
-        // slot run; the scan's last entry is the chunk total)
+        // exact radii of the internal nodes from the triangle records: one warp per node of at
+        // most kRadiusChunk triangles, chunks of the larger nodes' slot runs (the scan's last
+        // entry is the chunk total)
         int* rchunk = (int*)track(dalloc<int>(num_nodes + 1, st));
         unsigned long long* r2bits = (unsigned long long*)track(dalloc<unsigned long long>(E, st));
         FWN_CUDA_CHECK(cudaMemsetAsync(r2bits, 0, (size_t)E * sizeof(unsigned long long), st));
@@ -1271,7 +1334,9 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
             int dev = 0, sms = 0;
             FWN_CUDA_CHECK(cudaGetDevice(&dev));
             FWN_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-            k_node_radius<<<sms * 8, 256, 0, st>>>(num_nodes, rchunk, first, last, pos, stage,
+            k_node_radius_small<<<grid_for((int64_t)((num_nodes + 31) / 32) * 32, 256), 256, 0, st>>>(
+                num_nodes, keys, first, last, flags, pos, stage, e.tris, r2bits);
+            k_node_radius<<<sms * 4, 256, 0, st>>>(num_nodes, rchunk, first, last, pos, stage,
                                                    e.tris, r2bits);
         }
         FWN_CUDA_CHECK(cudaGetLastError());
