@@ -629,6 +629,26 @@ __device__ __forceinline__ double vertex_r2(double x, double y, double z, const 
     return fmad(dx, dx, fmad(dy, dy, dz * dz));
 }
 
+// Running maximum of vertex_r2 over a stream of vertices, with FP64 only where it can matter:
+// GB300's FP64 rate is a small fraction of FP32, so each vertex first gets a float estimate
+// e = |v - P|^2 (P is a float value; every step rounded once: relative error below 6e-7 while no
+// step underflows) and its exact FP64 term is taken only when e comes within 1e-5 of the
+// largest estimate seen so far (or the estimates are near float's underflow or overflow). The
+// vertex with the largest exact term always passes (its estimate is within 1.2e-6 of every
+// other vertex's or above), so the maximum equals the plain FP64 maximum bit for bit.
+struct ScreenedMax {
+    float m = 0.f;     // largest estimate so far
+    double r2 = 0.0;   // largest exact term among the vertices that passed
+    __device__ __forceinline__ void add(float x, float y, float z, const float* Pf, const double* P) {
+        const float dx = x - Pf[0], dy = y - Pf[1], dz = z - Pf[2];
+        const float e = (dx * dx + dy * dy) + dz * dz;
+        if (!(m < INFINITY) || e >= m * 0.99999f - 1e-37f) {
+            r2 = fmax(r2, vertex_r2(x, y, z, P));
+            m = fmaxf(m, e);
+        }
+    }
+};
+
 __device__ void leaf_moments(const float* __restrict__ V, const int32_t* __restrict__ F,
                              const int64_t* __restrict__ voff, const uint64_t* __restrict__ keys,
                              const uint32_t* __restrict__ tri_of_slot, int f, int l,
@@ -693,14 +713,19 @@ __device__ void leaf_moments(const float* __restrict__ V, const int32_t* __restr
         }
         for (int j = 0; j < 3; ++j) R.M1[3 * i + j] = fmad(N[i], e[j], M1[3 * i + j]);
     }
-    double r2 = 0.0;
+    ScreenedMax sm;
+    const float Pf[3] = {(float)P[0], (float)P[1], (float)P[2]};
     for (int s = f; s <= l; ++s) {
         const int64_t t = tri_of_slot[s];
         const int m = (int)(keys[s] >> MORTON_BITS);
-        double v[3][3];
-        load_tri_d(V, F, voff[m], t, v);
-        for (int j = 0; j < 3; ++j) r2 = fmax(r2, vertex_r2(v[j][0], v[j][1], v[j][2], P));
+        const int64_t vb = voff[m];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const float* vp = V + 3 * (vb + F[3 * t + j]);
+            sm.add(vp[0], vp[1], vp[2], Pf, P);
+        }
     }
+    const double r2 = sm.r2;
     for (int a = 0; a < 3; ++a) {
         R.P[a] = P[a];
         R.N[a] = N[a];
@@ -816,13 +841,15 @@ constexpr int kRadiusChunk = 2048;
 
 __device__ __forceinline__ double slots_r2(const TriF32* __restrict__ tris, int s0, int s1,
                                            const double* P, int lane) {
-    double r2 = 0.0;
+    ScreenedMax sm;
+    const float Pf[3] = {(float)P[0], (float)P[1], (float)P[2]};
     for (int s = s0 + lane; s < s1; s += 32) {
         const float4 t0 = tris[s].t0, t1 = tris[s].t1, t2 = tris[s].t2;
-        r2 = fmax(r2, vertex_r2(t0.x, t0.y, t0.z, P));
-        r2 = fmax(r2, vertex_r2(t0.w, t1.x, t1.y, P));
-        r2 = fmax(r2, vertex_r2(t1.z, t1.w, t2.x, P));
+        sm.add(t0.x, t0.y, t0.z, Pf, P);
+        sm.add(t0.w, t1.x, t1.y, Pf, P);
+        sm.add(t1.z, t1.w, t2.x, Pf, P);
     }
+    double r2 = sm.r2;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) r2 = fmax(r2, __shfl_xor_sync(0xffffffffu, r2, o));
     return r2;
