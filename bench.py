@@ -11,16 +11,28 @@ A step = one winding-number query pass over the 10M points against the built tre
              buffers; H2D of the points and D2H of Omega + inside inside the timed region)
   plain_fp64 the plain FP64 form (FP64 everywhere, same tree), its queries/s and the max / RMS
              |dw| between the two forms over all queries (gate: <= 1e-4)
-  roofline   FP32-issue roofline of the traversal kernel from device work counters
-  cpu_baseline  the CPU restatement of the reference path (oracle O2) on the host cores
+  roofline   FP32 roofline of the traversal kernel: algorithmic flops from device work
+             counters over its CUDA-event time, against the FP32 FMA peak measured in the same
+             process (fwn_probe_fp32_peak)
+  cpu_baseline  the CPU implementation of the reference path on the host cores (the reference
+             itself when a built one is present under baseline/_ref, else the oracle's
+             restatement O2)
+  batched    the 512-mesh forest (one persistent CUDA-graph launch; build ms, meshes/s, the
+             per-mesh FP64 launches with max |dw| over every query, is_inside against the
+             reference restatement on sampled meshes)
+  soup       the defective 1M-triangle soup (|dw| split near / far against the FP64 form on
+             every point and against the FP64 brute force on a sample; is_inside against the
+             reference restatement on every point)
 
-``--impl reference`` times the reference path's CPU implementation (the oracle restatement,
-since the reference library cannot be built here) on the same workload and prints the same
-line with ``"impl": "reference"``.
+``--impl reference`` times the reference path's CPU implementation on the same workload (the
+reference itself when a built one is present under baseline/_ref, else the oracle restatement)
+and prints the same line with ``"impl": "reference"``.
 
-Multi-GPU (torchrun): every rank builds its own replica of the tree and answers its own 10M
-queries (rank r > 0: a seeded shuffle of the set) — no collective on the data path; value = all ranks' queries /
-the slowest rank's time (weak scaling).
+Multi-GPU (torchrun): every rank builds its own replica of the tree. By default every rank
+answers its own 10M queries (rank r > 0: a seeded shuffle of the set), with no collective on the
+data path; value = all ranks' queries / the slowest rank's time (weak scaling). With
+``--split-queries`` the ranks share one set: each answers its contiguous range of the query order
+and the results are all-gathered (strong scaling).
 """
 from __future__ import annotations
 
