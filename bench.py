@@ -23,6 +23,9 @@ A step = one winding-number query pass over the 10M points against the built tre
   soup       the defective 1M-triangle soup (|dw| split near / far against the FP64 form on
              every point and against the FP64 brute force on a sample; is_inside against the
              reference restatement on every point)
+  voxel      4 x 5M-triangle meshes on 256^3 voxel-centre grids (67M queries; explicit points in
+             one persistent launch and the device-generated grid path; is_inside against the
+             reference restatement on mesh 0's 16.7M voxels)
 
 ``--impl reference`` times the reference path's CPU implementation on the same workload (the
 reference itself when a built one is present under baseline/_ref, else the oracle restatement)
@@ -475,19 +478,21 @@ def measure_soup(dev, *, steps=5, warmup=3, cpu=True):
     return out
 
 
-def batched_summary(dev, *, steps=5, warmup=3, cpu=True):
-    """The 512-mesh forest (seed 3) inside the default line: its persistent CUDA-graph query,
-    build, meshes/s, per-mesh FP64 launches with max |dw| over every query, and is_inside against
-    the CPU restatement of the reference on sampled meshes."""
+def batched_summary(dev, *, steps=5, warmup=3, cpu=True, voxel=False):
+    """A batched workload inside the default line. The 512-mesh forest (seed 3): its persistent
+    CUDA-graph query, build, meshes/s, per-mesh FP64 launches with max |dw| over every query, and
+    is_inside against the CPU restatement of the reference on sampled meshes. voxel=True: the 4
+    displaced 5M-triangle meshes on 256^3 voxel-centre grids (the volume sign pass), the same
+    figures plus the grid path that generates the centres on the device."""
     from lagrange_gb300 import workloads as W
     t0 = time.perf_counter()
-    fo = W.batched_forest_workload()
+    fo = W.voxel_workload() if voxel else W.batched_forest_workload()
     gen_s = time.perf_counter() - t0
     r = measure_forest(fo, dev, None, 0, 1, leaf=0, steps=steps, warmup=warmup, e2e=True, cpu=cpu,
-                       fp64=True, clocks=False, grid=False)
+                       fp64=True, clocks=False, grid=voxel)
     keep = ("value", "unit", "ms_per_step", "build_ms", "meshes_per_s_build_plus_query",
             "gpu_launches", "sort_key_bits", "plain_fp64_per_mesh_launches", "cpu_baseline",
-            "inside_vs_reference")
+            "inside_vs_reference", "grid_path")
     out = {"metric": r["metric"], **{k: r[k] for k in keep if k in r}}
     out["config"] = {**r["config"], "generation_s": gen_s}
     if "e2e" in r:
@@ -899,6 +904,10 @@ def run_ours(args, rank, world, local):
         torch.cuda.empty_cache()
         result["soup"] = measure_soup(dev, steps=min(args.steps, 5),
                                       warmup=max(3, min(args.warmup, 5)), cpu=not args.no_cpu)
+        torch.cuda.empty_cache()
+        result["voxel"] = batched_summary(dev, steps=min(args.steps, 5),
+                                          warmup=max(3, min(args.warmup, 5)),
+                                          cpu=not args.no_cpu, voxel=True)
     if rank == 0:
         print(json.dumps(result), flush=True)
     barrier(dist)
