@@ -832,24 +832,43 @@ __global__ void k_refit(int num_leaves, const int* __restrict__ leaf_list,
 // The far test of a node compares |q - P| with beta * r, so r must bound the distance from P to
 // every point of the node's triangles; the tightest such bound is the distance to the farthest
 // vertex (triangles are convex hulls of their vertices). Leaves compute it in leaf_moments. An
-// internal node's triangles are the contiguous run of sorted slots [first, last]. Nodes of at
-// most kRadiusChunk triangles (all but the top few levels) take one warp each
-// (k_node_radius_small); larger ones are split into chunks of kRadiusChunk slots, one warp per
-// chunk, whose maxima meet in an atomicMax on the bit pattern (non-negative doubles order like
-// their bits). A maximum does not depend on the order, so it equals the serial one bit for bit.
+// internal node's triangles are the contiguous run of sorted slots [first, last]. Every internal
+// node of at most kRadiusChunk triangles (all but the top few levels) takes one warp of its own
+// (a compacted list, so large and small nodes spread evenly over the warps); larger ones are
+// split into chunks of kRadiusChunk slots, one warp per chunk, whose maxima meet in an atomicMax
+// on the bit pattern (non-negative doubles order like their bits). A maximum does not depend on
+// the order, so it equals the serial one bit for bit.
 constexpr int kRadiusChunk = 2048;
 
+// Largest vertex_r2 over slots [s0, s1), one warp: a first pass takes the largest float estimate
+// M of |v - P|^2 over the run (the ScreenedMax bound: an estimate is within 6e-7 of its exact
+// value while no step underflows), a second pass takes the exact FP64 term of the vertices whose
+// estimate reaches M (1 - 1e-5) only (or all of them near float's underflow or overflow). The
+// vertex with the largest exact term always qualifies, so the result is the plain FP64 maximum
+// bit for bit, at a few FP64 terms per run instead of three per triangle.
 __device__ __forceinline__ double slots_r2(const TriF32* __restrict__ tris, int s0, int s1,
                                            const double* P, int lane) {
-    ScreenedMax sm;
     const float Pf[3] = {(float)P[0], (float)P[1], (float)P[2]};
+    auto est = [&](float x, float y, float z) {
+        const float dx = x - Pf[0], dy = y - Pf[1], dz = z - Pf[2];
+        return (dx * dx + dy * dy) + dz * dz;
+    };
+    float m = 0.f;
     for (int s = s0 + lane; s < s1; s += 32) {
         const float4 t0 = tris[s].t0, t1 = tris[s].t1, t2 = tris[s].t2;
-        sm.add(t0.x, t0.y, t0.z, Pf, P);
-        sm.add(t0.w, t1.x, t1.y, Pf, P);
-        sm.add(t1.z, t1.w, t2.x, Pf, P);
+        m = fmaxf(m, fmaxf(est(t0.x, t0.y, t0.z), fmaxf(est(t0.w, t1.x, t1.y), est(t1.z, t1.w, t2.x))));
     }
-    double r2 = sm.r2;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    const bool all = !(m < INFINITY);
+    const float thr = m * 0.99999f - 1e-37f;
+    double r2 = 0.0;
+    for (int s = s0 + lane; s < s1; s += 32) {
+        const float4 t0 = tris[s].t0, t1 = tris[s].t1, t2 = tris[s].t2;
+        if (all || est(t0.x, t0.y, t0.z) >= thr) r2 = fmax(r2, vertex_r2(t0.x, t0.y, t0.z, P));
+        if (all || est(t0.w, t1.x, t1.y) >= thr) r2 = fmax(r2, vertex_r2(t0.w, t1.x, t1.y, P));
+        if (all || est(t1.z, t1.w, t2.x) >= thr) r2 = fmax(r2, vertex_r2(t1.z, t1.w, t2.x, P));
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) r2 = fmax(r2, __shfl_xor_sync(0xffffffffu, r2, o));
     return r2;
@@ -876,23 +895,28 @@ __global__ void k_radius_chunks(int num_nodes, const uint64_t* __restrict__ keys
                     : 0;
 }
 
-// Nodes of at most kRadiusChunk triangles: each warp scans 32 consecutive node ids and takes the
-// internal ones among them in turn, all lanes on one node.
-__global__ void k_node_radius_small(int num_nodes, const uint64_t* __restrict__ keys,
+// The internal nodes of at most kRadiusChunk triangles, in any order (list[0 .. *count)).
+__global__ void k_radius_list(int num_nodes, const uint64_t* __restrict__ keys,
+                              const int* __restrict__ first, const int* __restrict__ last,
+                              const uint8_t* __restrict__ flags, int* __restrict__ list,
+                              int* __restrict__ count) {
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= num_nodes) return;
+    if (internal_emitted(keys, first, last, flags, u) && last[u] - first[u] + 1 <= kRadiusChunk)
+        list[atomicAdd(count, 1)] = u;
+}
+
+// One warp per listed node (grid-stride), all lanes on its slot run.
+__global__ void k_node_radius_small(const int* __restrict__ list, const int* __restrict__ count,
                                     const int* __restrict__ first, const int* __restrict__ last,
-                                    const uint8_t* __restrict__ flags, const int* __restrict__ pos,
-                                    const StageRec* __restrict__ stage,
+                                    const int* __restrict__ pos, const StageRec* __restrict__ stage,
                                     const TriF32* __restrict__ tris,
                                     unsigned long long* __restrict__ r2bits) {
     const int lane = threadIdx.x & 31;
-    const int u0 = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
-    const int u = u0 + lane;
-    const bool mine = u < num_nodes && internal_emitted(keys, first, last, flags, u) &&
-                      last[u] - first[u] + 1 <= kRadiusChunk;
-    unsigned todo = __ballot_sync(0xffffffffu, mine);
-    while (todo) {
-        const int v = u0 + __ffs(todo) - 1;
-        todo &= todo - 1;
+    const int total = *count;
+    const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+    for (int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); w < total; w += nwarps) {
+        const int v = list[w];
         const int i = pos[v];
         const double P[3] = {stage[i].P[0], stage[i].P[1], stage[i].P[2]};
         const double r2 = slots_r2(tris, first[v], last[v] + 1, P, lane);
@@ -1361,8 +1385,12 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
             int dev = 0, sms = 0;
             FWN_CUDA_CHECK(cudaGetDevice(&dev));
             FWN_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-            k_node_radius_small<<<grid_for((int64_t)((num_nodes + 31) / 32) * 32, 256), 256, 0, st>>>(
-                num_nodes, keys, first, last, flags, pos, stage, e.tris, r2bits);
+            int* rlist = (int*)track(dalloc<int>(num_nodes + 1, st));  // [count | list]
+            FWN_CUDA_CHECK(cudaMemsetAsync(rlist, 0, sizeof(int), st));
+            k_radius_list<<<grid_for(num_nodes, 256), 256, 0, st>>>(num_nodes, keys, first, last,
+                                                                    flags, rlist + 1, rlist);
+            k_node_radius_small<<<sms * 16, 256, 0, st>>>(rlist + 1, rlist, first, last, pos,
+                                                          stage, e.tris, r2bits);
             k_node_radius<<<sms * 4, 256, 0, st>>>(num_nodes, rchunk, first, last, pos, stage,
                                                    e.tris, r2bits);
         }
