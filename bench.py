@@ -23,6 +23,8 @@ A step = one winding-number query pass over the 10M points against the built tre
   soup       the defective 1M-triangle soup (|dw| split near / far against the FP64 form on
              every point and against the FP64 brute force on a sample; is_inside against the
              reference restatement on every point)
+  uvsphere   the 64x32 UV sphere with 100k queries, checked on every point against the FP64
+             brute force
   voxel      4 x 5M-triangle meshes on 256^3 voxel-centre grids (67M queries; explicit points in
              one persistent launch and the device-generated grid path; is_inside against the
              reference restatement on mesh 0's 16.7M voxels)
@@ -479,6 +481,80 @@ def measure_soup(dev, *, steps=5, warmup=3, cpu=True):
     return out
 
 
+def measure_uvsphere(dev, *, steps=10, warmup=3, cpu=True):
+    """The CPU-runnable configuration: the 64x32 UV sphere (3,968 triangles) with 100k queries
+    uniform in [-1.5, 1.5]^3. Its oracle is the FP64 brute force over all triangles, evaluated on
+    every point: |dw| of the mixed and FP64 forms against it (beta = 2 truncation included) and
+    is_inside against it outside +-1e-3; plus the reference path's CPU rate on all points."""
+    import torch
+    import lagrange_gb300 as fwn
+    from lagrange_gb300 import workloads as W
+    wl = W.uv_sphere_workload()
+    n = len(wl.Q)
+    Vd, Fd, Qd = (torch.from_numpy(a).to(dev) for a in (wl.V, wl.F, wl.Q))
+    leaf, trav, block, tuning, builder, tuned = autotune_choice(fwn, Vd, Fd, Qd)
+    eng = fwn.FastWindingNumber(Vd, Fd, leaf_size=leaf, traversal=trav, block_size=block,
+                                tuning=tuning, builder=builder,
+                                records=fwn.RECORDS_F32 | fwn.RECORDS_F64)
+    L = fwn.library()
+    stream = torch.cuda.current_stream(dev)
+    sptr = C.c_void_p(stream.cuda_stream)
+    w = torch.empty(n, dtype=torch.float32, device=dev)
+    ins = torch.empty(n, dtype=torch.uint8, device=dev)
+    om = fwn._opts(precision=fwn.PRECISION_MIXED, traversal=trav, block_size=block, tuning=tuning)
+
+    def q_mixed():
+        fwn._check(L.fwn_query_ex(eng.handle, C.byref(om), C.c_void_p(Qd.data_ptr()), n,
+                                  C.c_void_p(w.data_ptr()), C.c_void_p(ins.data_ptr()), None, None,
+                                  sptr))
+    for _ in range(warmup):
+        q_mixed()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        q_mixed()
+        b.record(stream)
+        torch.cuda.synchronize()
+        ts.append(a.elapsed_time(b))
+    ms = statistics.median(ts)
+    _, _, w64 = eng.query(Qd, precision=fwn.PRECISION_FP64, traversal=fwn.TRAVERSAL_THREAD,
+                          omega_f64=True)
+    torch.cuda.synchronize()
+    out = {"workload": wl.name, "triangles": int(len(wl.F)), "queries": n, "leaf_size": leaf,
+           "tuning": tuning, "builder": builder, "value": n / (ms / 1e3), "unit": "queries/s",
+           "ms_per_step": ms, "steps": steps, "build_ms": eng.info()["build_ms"],
+           "step": "one query call (keys, sort, walk, scatter), CUDA events, median"}
+    if cpu:
+        import oracle
+        nthr = oracle.nthreads_default()
+        exact = oracle.brute_f64(wl.V, wl.F, wl.Q, nthreads=nthr)
+        wm = w.cpu().numpy().astype(np.float64)
+        w6 = w64.cpu().numpy()
+        im = ins.cpu().numpy()
+        dm, d6 = np.abs(wm - exact) / FOUR_PI, np.abs(w6 - exact) / FOUR_PI
+        band = np.abs(exact / FOUR_PI - 0.5) > 1e-3
+        out["vs_brute_force_fp64"] = {
+            "points": n, "max_dw": float(dm.max()), "rms_dw": float(np.sqrt(np.mean(dm ** 2))),
+            "fp64_form_max_dw": float(d6.max()), "mixed_vs_fp64_form_max_dw":
+                float(np.max(np.abs(wm - w6)) / FOUR_PI),
+            "inside_disagree_outside_band": int(np.sum(im[band] != (exact[band] / FOUR_PI > 0.5))),
+            "note": "every point; includes the beta=2 far-field truncation error"}
+        tree, kind, what = cpu_reference(wl.V, wl.F)
+        tree.query(wl.Q[:1000], beta=wl.beta, nthreads=nthr)
+        t0 = time.perf_counter()
+        om_ref, in_ref = tree.query(wl.Q, beta=wl.beta, nthreads=nthr)
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": n / dt, "unit": "queries/s", "cores": nthr, "kind": kind,
+                               "sample": f"all {n} queries; {what}"}
+        out["inside_vs_reference"] = {
+            "disagree_outside_band": int(np.sum(im[band] != in_ref[band])),
+            "max_dw_vs_reference_restatement": float(np.max(np.abs(wm - om_ref)) / FOUR_PI)}
+    eng.close()
+    return out
+
+
 def batched_summary(dev, *, steps=5, warmup=3, cpu=True, voxel=False):
     """A batched workload inside the default line. The 512-mesh forest (seed 3): its persistent
     CUDA-graph query, build, meshes/s, per-mesh FP64 launches with max |dw| over every query, and
@@ -905,6 +981,10 @@ def run_ours(args, rank, world, local):
         torch.cuda.empty_cache()
         result["soup"] = measure_soup(dev, steps=min(args.steps, 5),
                                       warmup=max(3, min(args.warmup, 5)), cpu=not args.no_cpu)
+        torch.cuda.empty_cache()
+        result["uvsphere"] = measure_uvsphere(dev, steps=max(args.steps, 10),
+                                              warmup=max(3, min(args.warmup, 5)),
+                                              cpu=not args.no_cpu)
         torch.cuda.empty_cache()
         result["voxel"] = batched_summary(dev, steps=min(args.steps, 5),
                                           warmup=max(3, min(args.warmup, 5)),
