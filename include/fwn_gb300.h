@@ -317,6 +317,19 @@ FWN_API fwn_status fwn_forest_query(fwn_handle h, const float* d_points,
                                     uint8_t* d_inside, const fwn_query_opts* opts,
                                     void* stream);
 
+/* No counterpart in the reference (lagrange serializes meshes, not the winding engine). Writes a
+ * built engine, single mesh or forest, to a file: a header with its sizes and configuration, its
+ * per-mesh data, node records (FP32 and/or FP64, as built) and triangle records, and a checksum.
+ * Reading it back with fwn_load skips the build. Synchronous. */
+FWN_API fwn_status fwn_save(fwn_handle h, const char* path);
+
+/* Reads an engine written by fwn_save onto the current device (the FP64 staging moments kept for
+ * fwn_export_moments are not saved). The header, the sizes, the checksum and every node's skip
+ * link and triangle range are checked before any device work: a foreign, truncated or corrupt
+ * file returns FWN_INVALID_ARG. Queries on the loaded engine equal those on the saved one.
+ * Synchronous. */
+FWN_API fwn_status fwn_load(const char* path, fwn_handle* out);
+
 /* No counterpart in the reference (a diagnostic). Usage of the library's per-device pool of
  * stream-ordered query scratch (zeros if no call has used the pool on `device` yet): bytes the
  * pool holds from the driver, bytes handed out, and the high-water mark of handed-out bytes since

@@ -90,7 +90,7 @@ EXPORTS = ["fwn_config_default", "fwn_last_error", "fwn_version", "fwn_build", "
            "fwn_forest_build_device", "fwn_forest_query", "fwn_query_noalloc", "fwn_autotune",
            "fwn_query_grid", "fwn_orientation_criterion", "fwn_query_order",
            "fwn_forest_autotune", "fwn_forest_sort_key_bits", "fwn_probe_fp32_peak",
-           "fwn_scratch_pool_stats"]
+           "fwn_scratch_pool_stats", "fwn_save", "fwn_load"]
 
 
 def library():
@@ -136,12 +136,15 @@ def library():
     L.fwn_probe_fp32_peak.argtypes = [C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double), P]
     u64p = C.POINTER(C.c_uint64)
     L.fwn_scratch_pool_stats.argtypes = [C.c_int32, C.c_int32, u64p, u64p, u64p]
+    L.fwn_save.argtypes = [P, C.c_char_p]
+    L.fwn_load.argtypes = [C.c_char_p, C.POINTER(P)]
     for name in ("fwn_build", "fwn_build_device", "fwn_destroy", "fwn_get_info", "fwn_query",
                  "fwn_query_ex", "fwn_query_host", "fwn_export_tree", "fwn_export_moments",
                  "fwn_forest_build", "fwn_forest_build_device", "fwn_forest_query",
                  "fwn_query_noalloc", "fwn_autotune", "fwn_query_grid",
                  "fwn_orientation_criterion", "fwn_query_order", "fwn_forest_autotune",
-                 "fwn_forest_sort_key_bits", "fwn_probe_fp32_peak", "fwn_scratch_pool_stats"):
+                 "fwn_forest_sort_key_bits", "fwn_probe_fp32_peak", "fwn_scratch_pool_stats",
+                 "fwn_save", "fwn_load"):
         getattr(L, name).restype = st
     _lib = L
     return L
@@ -267,6 +270,18 @@ class FastWindingNumber:
             _check(L.fwn_build(V.ctypes.data_as(C.c_void_p), len(V),
                                F.ctypes.data_as(C.c_void_p), len(F), C.byref(cfg),
                                C.byref(self._h)))
+
+    def save(self, path) -> None:
+        """Writes the built engine to a file (fwn_save); `load` reads it back without a build."""
+        _check(library().fwn_save(self._h, str(path).encode()))
+
+    @classmethod
+    def load(cls, path):
+        """An engine read from a file written by `save`, on the current device (fwn_load)."""
+        obj = cls.__new__(cls)
+        obj._h = C.c_void_p(None)
+        _check(library().fwn_load(str(path).encode(), C.byref(obj._h)))
+        return obj
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:

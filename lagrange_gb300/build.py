@@ -36,6 +36,7 @@ SOURCES = [
     ("autotune.cu", []),
     ("callers.cu", []),
     ("probe.cu", []),
+    ("persist.cu", []),
 ]
 
 

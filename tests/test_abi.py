@@ -106,3 +106,27 @@ def test_forest_sort_key_bits(engine_lib):
     kb = C.c_int32(0)
     assert L.fwn_forest_sort_key_bits(2, bad.ctypes.data_as(C.c_void_p), C.byref(kb)) == 1
     assert L.fwn_forest_sort_key_bits(0, bad.ctypes.data_as(C.c_void_p), C.byref(kb)) == 1
+
+
+def test_load_refuses_bad_files_before_device_work(engine_lib, tmp_path):
+    """fwn_load checks a file before it touches the device: a missing file, a foreign file and a
+    truncated header all return FWN_INVALID_ARG with a message (no GPU is needed to see it)."""
+    L = fwn.library()
+    h = C.c_void_p()
+
+    def status(path):
+        st = L.fwn_load(str(path).encode(), C.byref(h))
+        buf = C.create_string_buffer(256)
+        L.fwn_last_error(buf, 256)
+        return st, buf.value.decode()
+
+    st, msg = status(tmp_path / "missing.fwn")
+    assert st == 1 and "cannot open" in msg and not h.value
+    (tmp_path / "foreign.fwn").write_bytes(b"NOTANFWN" + bytes(300))
+    st, msg = status(tmp_path / "foreign.fwn")
+    assert st == 1 and "magic" in msg
+    (tmp_path / "short.fwn").write_bytes(b"FWNGB300" + bytes(4))
+    st, msg = status(tmp_path / "short.fwn")
+    assert st == 1 and "truncated" in msg
+    assert L.fwn_load(None, C.byref(h)) == 1
+    assert L.fwn_save(None, b"x") == 6

@@ -548,3 +548,40 @@ def test_split_builder_degenerate_geometry(torch_cuda, oracle_mod):
                 np.testing.assert_array_equal(got[k], ref[k], err_msg=k)
             np.testing.assert_array_equal(got["center_radius"], ref["center_radius"])
             assert got["tri_count"].max() <= leaf
+
+
+@pytest.mark.parametrize("builder", [0, 1])
+def test_save_load_round_trip(torch_cuda, tmp_path, builder):
+    """An engine written with fwn_save and read back with fwn_load has the same tree and answers
+    every query with the same bits (mixed and FP64 forms); a forest with an empty mesh too. A
+    file with one payload byte flipped is refused by its checksum."""
+    g = np.load(GOLDEN / "displaced.npz")
+    eng = _engine(g["V"], g["F"], leaf_size=8, builder=builder, records=BOTH)
+    path = tmp_path / "eng.fwn"
+    eng.save(path)
+    back = fwn.FastWindingNumber.load(path)
+    a, b = eng.export_tree(), back.export_tree()
+    for k in a:
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+    for kw in ({}, {"precision": fwn.PRECISION_FP64, "omega_f64": True}):
+        ra, rb = _q(eng, torch_cuda, g["Q"], **kw), _q(back, torch_cuda, g["Q"], **kw)
+        for x, y in zip(ra, rb):
+            np.testing.assert_array_equal(x, y)
+    raw = bytearray(path.read_bytes())
+    raw[len(raw) // 2] ^= 0x40
+    bad = tmp_path / "bad.fwn"
+    bad.write_bytes(bytes(raw))
+    with pytest.raises(fwn.WindingError, match="corrupt"):
+        fwn.FastWindingNumber.load(bad)
+    fo = W.batched_forest_workload(n_meshes=5, seed=13, f_lo=200, f_hi=3000, q_lo=50, q_hi=500)
+    voff = np.insert(fo.voff, 2, fo.voff[2])
+    foff = np.insert(fo.foff, 2, fo.foff[2])
+    qoff = np.insert(fo.qoff, 2, fo.qoff[2])
+    forest = fwn.Forest(fo.V, voff, fo.F, foff, leaf_size=8, builder=builder)
+    forest.save(tmp_path / "forest.fwn")
+    f2 = fwn.Forest.load(tmp_path / "forest.fwn")
+    Qd = torch_cuda.from_numpy(fo.Q).cuda()
+    w1, i1 = forest.query_forest(Qd, qoff)
+    w2, i2 = f2.query_forest(Qd, qoff)
+    torch_cuda.cuda.synchronize()
+    assert torch_cuda.equal(w1, w2) and torch_cuda.equal(i1, i2)
