@@ -130,3 +130,48 @@ def test_load_refuses_bad_files_before_device_work(engine_lib, tmp_path):
     assert st == 1 and "truncated" in msg
     assert L.fwn_load(None, C.byref(h)) == 1
     assert L.fwn_save(None, b"x") == 6
+
+
+def _engine_file(path, *, skip=1, tri_count=1, root=0, end=1, tri_id=0, flip=False):
+    """A one-mesh, one-leaf engine file laid out as fwn_save writes it (header, MeshInfo,
+    NodeF32, TriF32, triangle id), with a correct FNV-1a 64 checksum unless `flip`."""
+    import struct
+    mesh = struct.pack("<2i12f", root, end, *([0.0] * 12))
+    node = struct.pack("<4f3if", 0, 0, 0, 1, skip, 0, tri_count, 0) + bytes(96)
+    tri = bytes(48)
+    payload = bytearray(mesh + node + tri + struct.pack("<i", tri_id))
+    h = 1469598103934665603
+    for b in payload:
+        h = ((h ^ b) * 1099511628211) & 0xFFFFFFFFFFFFFFFF
+    if flip:
+        payload[70] ^= 1
+    cfg = bytes(fwn.config_default())
+    assert len(cfg) == 64
+    header = (b"FWNGB300" + struct.pack("<II", 1, 144) + cfg +
+              struct.pack("<5q2i2Q", 3, 1, 1, 1, 1, 1, 0, len(payload), h))
+    assert len(header) == 144
+    path.write_bytes(header + bytes(payload))
+    return path
+
+
+def test_load_checks_payload_before_device_work(engine_lib, tmp_path):
+    """A file whose checksum does not match its payload, or whose node links, triangle ranges,
+    mesh roots or triangle ids would send the walk out of bounds, is refused on the host."""
+    L = fwn.library()
+    h = C.c_void_p()
+
+    def status(path):
+        st = L.fwn_load(str(path).encode(), C.byref(h))
+        buf = C.create_string_buffer(256)
+        L.fwn_last_error(buf, 256)
+        return st, buf.value.decode()
+
+    cases = [({"flip": True}, "checksum"), ({"skip": 0}, "inconsistent node"),
+             ({"skip": 2}, "inconsistent node"), ({"tri_count": 2}, "inconsistent node"),
+             ({"tri_count": 17}, "inconsistent node"), ({"root": 1}, "mesh root"),
+             ({"end": 2}, "mesh root"), ({"tri_id": 1}, "triangle id"),
+             ({"tri_id": -1}, "triangle id")]
+    for i, (kw, what) in enumerate(cases):
+        st, msg = status(_engine_file(tmp_path / f"c{i}.fwn", **kw))
+        assert st == 1 and what in msg and not h.value, (kw, msg)
+
