@@ -763,6 +763,7 @@ def run_ours(args, rank, world, local):
     # the warp-schedule variant the traversal ran (tuning 0 resolves by batch size, as in the
     # library: two queries per lane once the batch fills every SM's warp slots four times)
     variant = tuning or (4 if n >= 4 * props.multi_processor_count * 32 * 64 else 3)
+    qpl = 2 if variant >= 4 else 1  # queries per lane of the variant
     traffic = NCU_TRAFFIC.get((wl.name, args.leaf, variant, builder)) if world == 1 else None
     hbm_peak = measured_peaks().get("hbm_gbs")
     result["roofline"] = {
@@ -785,6 +786,8 @@ def run_ours(args, rank, world, local):
                 if traffic and hbm_peak else None),
         "per_query": {"far_evals": far / n, "tri_evals": tri / n, "nodes_tested": nodes / n,
                       "tri_fp64": stats["tri_evals_fp64"] / n,
+                      "warp_steps_per_warp": stats["warp_steps"] / math.ceil(n / (32 * qpl)),
+                      "slot_utilisation": nodes / (stats["warp_steps"] * 32 * qpl),
                       "flops": flops / n, "l2_bytes": l2_bytes / n},
         "l2_gbs_algorithmic": l2_bytes / (kernel_ms / 1e3) / 1e9,
     }

@@ -126,7 +126,9 @@ typedef struct fwn_query_stats {
     uint64_t tri_evals;        /* exact triangle solid angles (all precisions) */
     uint64_t tri_evals_fp64;   /* of which evaluated in FP64 (mixed form only) */
     uint64_t warp_steps;       /* node steps summed over warps (max over the warp's lanes);
-                                  nodes_tested / (32 * warp_steps) = lane utilisation */
+                                  the warp schedule counts with the variant's queries per lane
+                                  (qpl = 2 for tunings >= 4): nodes_tested / (32 * qpl *
+                                  warp_steps) = slot utilisation */
 } fwn_query_stats;
 
 /* Result of fwn_autotune: the fastest (builder, leaf_size, traversal, block_size, tuning) on the

@@ -32,6 +32,14 @@ namespace {
 
 constexpr double TWO_PI_D = 6.283185307179586476925286766559;  // Omega/(4 pi) > 0.5 <=> Omega > 2 pi
 
+// is_inside of a float Omega: (double)Omega > 2 pi (the reference compares in double, since its pi
+// is a double). 2 pi lies strictly between the floats 0x40C90FDA and 0x40C90FDB, so for every float
+// x, (double)x > 2 pi <=> x > 0x40C90FDA (NaN: false on both sides). The float comparison keeps
+// the test off the FP64 pipe, which on GB300 issues 2 operations per SM per cycle.
+__device__ __forceinline__ uint8_t inside_of(float res) {
+    return res > __int_as_float(0x40C90FDA) ? 1 : 0;
+}
+
 __device__ __forceinline__ unsigned lanemask_lt() {
     unsigned m;
     asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
@@ -418,7 +426,7 @@ k_query_thread(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tri
     if (valid) {
         const float res = s - c;
         if (omega) omega[qi] = res;
-        if (inside) inside[qi] = (double)res > TWO_PI_D ? 1 : 0;
+        if (inside) inside[qi] = inside_of(res);
     }
     if (STATS) flush_stats(qc, stats);
 }
@@ -451,6 +459,10 @@ __device__ __forceinline__ int mesh_of_query(const int64_t* __restrict__ qoff, i
 // lanes (triangles staged in shared memory, each query with its mesh's FP64 near-field radius)
 // and each owning slot adds its results in triangle order.
 constexpr int WARP_LEAF_MAX = 16;
+// ceil(2^16 / c) for c = 0..WARP_LEAF_MAX (entry 0 unused): the leaf pair loop's divisor table
+__constant__ unsigned kPairMagic[WARP_LEAF_MAX + 1] = {
+    0u, 65536u, 32768u, 21846u, 16384u, 13108u, 10923u, 9363u, 8192u,
+    7282u, 6554u, 5958u, 5462u, 5042u, 4682u, 4370u, 4096u};
 constexpr int WARP_BLOCK = 128;
 constexpr int DONE = INT_MAX;
 
@@ -562,11 +574,14 @@ __device__ __forceinline__ void warp_walk(const NodeF32* __restrict__ nodes,
                     sm.q[off[j] + __popc(lm[j] & lt)] = make_float4(sl[j].qx, sl[j].qy, sl[j].qz, sl[j].tau);
             __syncwarp();
             const int np = nl * cnt;
-            const float inv = 1.0f / (float)cnt;
+            // p = r * cnt + t by a multiply-shift: floor(p * ceil(2^16 / cnt) / 2^16) = p / cnt
+            // for every p < 4096 and cnt <= 16 (p < 64 * 16 here); integer ALU only, where a
+            // float reciprocal would put two conversions per pair on GB300's narrow FP64 pipe
+            const unsigned mcnt = kPairMagic[cnt];
             for (int base = 0; base < np; base += 32) {
                 const int p = base + lane;
                 if (p < np) {
-                    const int r = (int)(((float)p + 0.5f) * inv);  // p = r * cnt + t
+                    const int r = (int)(((unsigned)p * mcnt) >> 16);
                     const int t = p - r * cnt;
                     const float4 qq = sm.q[r];
                     const float4 t0 = sm.leaf[3 * t], t1 = sm.leaf[3 * t + 1], t2 = sm.leaf[3 * t + 2];
@@ -601,7 +616,7 @@ __device__ __forceinline__ void write_result(const Slot& s, int64_t qi, float* _
                                              uint8_t* __restrict__ inside) {
     const float res = s.s - s.c;
     if (omega) omega[qi] = res;
-    if (inside) inside[qi] = (double)res > TWO_PI_D ? 1 : 0;
+    if (inside) inside[qi] = inside_of(res);
 }
 
 // One mesh: each warp takes the next 32 * QPL queries of the (sorted) order. With sorted_omega
@@ -656,7 +671,7 @@ __global__ void k_scatter_results(const float* __restrict__ sorted_omega,
     const float res = sorted_omega[k];
     const int64_t qi = order[k];
     if (omega) omega[qi] = res;
-    if (inside) inside[qi] = (double)res > TWO_PI_D ? 1 : 0;
+    if (inside) inside[qi] = inside_of(res);
 }
 
 // Regular grid: voxel (i, j, k) has centre fmaf(i + 0.5, spacing, origin) per axis and output
@@ -803,7 +818,7 @@ k_query_f64(const NodeF64* __restrict__ nodes, const TriF32* __restrict__ tris, 
         const float res = (float)s;
         if (omega) omega[qi] = res;
         if (omega64) omega64[qi] = s;
-        if (inside) inside[qi] = (double)res > TWO_PI_D ? 1 : 0;
+        if (inside) inside[qi] = inside_of(res);
     }
     if (STATS) flush_stats(qc, stats);
 }
@@ -892,7 +907,7 @@ k_query_warp_f64(const NodeF64* __restrict__ nodes, const TriF32* __restrict__ t
         const float res = (float)s;
         if (omega) omega[qi] = res;
         if (omega64) omega64[qi] = s;
-        if (inside) inside[qi] = (double)res > TWO_PI_D ? 1 : 0;
+        if (inside) inside[qi] = inside_of(res);
     }
 }
 
@@ -947,7 +962,10 @@ __device__ __forceinline__ unsigned query_key(const MeshInfo& mi, const float* q
         const float lo = mi.lo[a] - 0.25f * ext;
         const float inv = ext > 0.f ? 1.0f / (1.5f * ext) : 0.f;
         const float u = (q[a] - lo) * inv * 1024.0f;
-        c[a] = (unsigned)(u >= 0.f ? (int)fminf(u, 1023.0f) : 0);
+        // floor of u clamped to [0, 1023] (NaN -> 0): adding 2^23 rounded down leaves floor(v)
+        // in the low mantissa bits for 0 <= v < 2^23, the same value as the truncating (int)
+        // conversion, without a conversion instruction (GB300 runs those on its narrow FP64 pipe)
+        c[a] = u >= 0.f ? __float_as_uint(__fadd_rd(fminf(u, 1023.0f), 8388608.0f)) - 0x4B000000u : 0u;
     }
     return hilbert3(c[0], c[1], c[2]);
 }
@@ -1128,9 +1146,12 @@ void query_mesh(const Engine& e, int mesh, const QueryArgs& a, const float* d_po
         else
             k_query_f64<false><<<grid_for(n, 128), 128, 0, st>>>(e.nodes64, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, d_omega64, d_status, d_stats);
     } else if (a.traversal == FWN_TRAVERSAL_WARP) {
-        if (want_stats)  // counters: one query per lane, no register cap
-            k_query_warp<true, 1, 1><<<grid_for(n, WARP_BLOCK), WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, nullptr, d_status, d_stats);
-        else
+        if (want_stats) {  // counters: no register cap, the variant's queries per lane
+            if (warp_variant(a.tuning, n) >= 4)
+                k_query_warp<true, 1, 2><<<grid_for(n, WARP_BLOCK * 2), WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, nullptr, d_status, d_stats);
+            else
+                k_query_warp<true, 1, 1><<<grid_for(n, WARP_BLOCK), WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, nullptr, d_status, d_stats);
+        } else
             launch_query_warp_variant(warp_variant(a.tuning, n), e, mi, d_points, order, n, a.beta,
                                       d_omega, d_inside, d_status, st, sorted_omega);
     } else {
