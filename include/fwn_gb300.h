@@ -243,6 +243,14 @@ FWN_API fwn_status fwn_export_tree(fwn_handle h, int32_t* skip, int32_t* tri_beg
  * a build that kept the staging records (tests). */
 FWN_API fwn_status fwn_export_moments(fwn_handle h, double* moments);
 
+/* Copies the node records as they are on the device into HOST buffers (either may be NULL):
+ * nodes32 [num_nodes x 128 B] (float4 P.xyz r; int32 skip, tri_begin, tri_count; float trM1;
+ * float N.xyz, W.xyz, C[6], D[10], 2 zero floats), nodes64 [num_nodes x 256 B] (double P.xyz r;
+ * int32 skip, tri_begin, tri_count, 0; double trM1, N.xyz, W.xyz, C[6], D[10], 3 zero doubles).
+ * FWN_INVALID_ARG when a requested record set is not kept. Inspection and tests: every FP32
+ * coefficient is the FP64 one rounded to nearest. */
+FWN_API fwn_status fwn_export_nodes(fwn_handle h, void* nodes32, void* nodes64);
+
 /* Autotuner (no reference counterpart: the reference has no tunable parameters). For one mesh
  * (DEVICE arrays) and a representative DEVICE sample of query points, builds the tree with both
  * builders for leaf sizes 4, 8, 12 and 16 and times every query schedule (the warp cursor's variants 1-6; thread per

@@ -86,7 +86,7 @@ _lib = None
 # every entry point declared in include/fwn_gb300.h
 EXPORTS = ["fwn_config_default", "fwn_last_error", "fwn_version", "fwn_build", "fwn_build_device",
            "fwn_destroy", "fwn_get_info", "fwn_query", "fwn_query_ex", "fwn_query_host",
-           "fwn_export_tree", "fwn_export_moments", "fwn_forest_build",
+           "fwn_export_tree", "fwn_export_moments", "fwn_export_nodes", "fwn_forest_build",
            "fwn_forest_build_device", "fwn_forest_query", "fwn_query_noalloc", "fwn_autotune",
            "fwn_query_grid", "fwn_orientation_criterion", "fwn_query_order",
            "fwn_forest_autotune", "fwn_forest_sort_key_bits", "fwn_probe_fp32_peak",
@@ -121,6 +121,7 @@ def library():
     L.fwn_query_order.argtypes = [P, P, i64, P, P]
     L.fwn_export_tree.argtypes = [P, P, P, P, P, P, P]
     L.fwn_export_moments.argtypes = [P, P]
+    L.fwn_export_nodes.argtypes = [P, P, P]
     L.fwn_forest_build.argtypes = [P, P, P, P, i64, C.POINTER(fwn_config), C.POINTER(P)]
     L.fwn_forest_build_device.argtypes = [P, P, P, P, i64, C.POINTER(fwn_config), P,
                                           C.POINTER(P)]
@@ -139,7 +140,7 @@ def library():
     L.fwn_save.argtypes = [P, C.c_char_p]
     L.fwn_load.argtypes = [C.c_char_p, C.POINTER(P)]
     for name in ("fwn_build", "fwn_build_device", "fwn_destroy", "fwn_get_info", "fwn_query",
-                 "fwn_query_ex", "fwn_query_host", "fwn_export_tree", "fwn_export_moments",
+                 "fwn_query_ex", "fwn_query_host", "fwn_export_tree", "fwn_export_moments", "fwn_export_nodes",
                  "fwn_forest_build", "fwn_forest_build_device", "fwn_forest_query",
                  "fwn_query_noalloc", "fwn_autotune", "fwn_query_grid",
                  "fwn_orientation_criterion", "fwn_query_order", "fwn_forest_autotune",
@@ -447,6 +448,24 @@ class FastWindingNumber:
         _check(library().fwn_export_tree(self._h, p(out["skip"]), p(out["tri_begin"]),
                                          p(out["tri_count"]), p(out["center_radius"]),
                                          p(out["sorted_tri"]), p(out["mesh_root"])))
+        return out
+
+    def export_nodes(self) -> dict:
+        """The device node records as arrays: "f32" [E, 32] float32 and "f64" [E, 32] float64
+        (the raw 128 B / 256 B records; the integer fields read as their bit patterns), each
+        present when the engine keeps that record set."""
+        inf = self.info()
+        E = inf["num_nodes"]
+        out = {}
+        rec = inf.get("records", RECORDS_F32)
+        n32 = np.zeros((E, 32), np.float32) if rec & RECORDS_F32 else None
+        n64 = np.zeros((E, 32), np.float64) if rec & RECORDS_F64 else None
+        p = lambda a: a.ctypes.data_as(C.c_void_p) if a is not None else None  # noqa: E731
+        _check(library().fwn_export_nodes(self._h, p(n32), p(n64)))
+        if n32 is not None:
+            out["f32"] = n32
+        if n64 is not None:
+            out["f64"] = n64
         return out
 
     def export_moments(self) -> np.ndarray:

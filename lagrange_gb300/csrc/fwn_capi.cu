@@ -409,6 +409,19 @@ FWN_API fwn_status fwn_export_moments(fwn_handle h, double* moments) {
     });
 }
 
+FWN_API fwn_status fwn_export_nodes(fwn_handle h, void* nodes32, void* nodes64) {
+    return guarded([&] {
+        Engine* e = engine_of(h);
+        const int64_t E = e->num_nodes;
+        if (nodes32 && !e->nodes32) throw Error(FWN_INVALID_ARG, "engine keeps no FP32 records");
+        if (nodes64 && !e->nodes64) throw Error(FWN_INVALID_ARG, "engine keeps no FP64 records");
+        if (E && nodes32)
+            FWN_CUDA_CHECK(cudaMemcpy(nodes32, e->nodes32, E * sizeof(NodeF32), cudaMemcpyDeviceToHost));
+        if (E && nodes64)
+            FWN_CUDA_CHECK(cudaMemcpy(nodes64, e->nodes64, E * sizeof(NodeF64), cudaMemcpyDeviceToHost));
+    });
+}
+
 FWN_API fwn_status fwn_forest_build(const float* V, const int64_t* voff, const int32_t* F,
                                     const int64_t* foff, int64_t nmeshes, const fwn_config* cfg,
                                     fwn_handle* out) {

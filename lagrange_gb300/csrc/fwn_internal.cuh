@@ -88,7 +88,7 @@ struct MeshInfo {
 };
 
 // FP64 staging record written by the refit (one per emitted node, indexed by DFS position).
-struct StageRec {
+struct __align__(32) StageRec {
     double P[3];     // expansion centre (a float value, see refit)
     double area;
     double N[3];
@@ -96,7 +96,9 @@ struct StageRec {
     double M2[18];   // [i*6+s], s: xx yy zz xy xz yz
     double r;        // radius about P: farthest vertex of the node's triangles (a float value,
                      // rounded up); internal nodes get it after the refit (k_node_radius)
+    double pad;      // 288 B: records start on 32 B sectors, so reads of one record share them
 };
+static_assert(sizeof(StageRec) == 288, "StageRec must be 9 sectors");
 
 // ---------------------------------------------------------------------------------------------
 // Errors

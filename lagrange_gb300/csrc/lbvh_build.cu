@@ -18,6 +18,7 @@
 // (oracle/fwn_oracle.c, compiled with -ffp-contract=off) reproduces keys, topology, centres and
 // radii bit for bit.
 #include <cmath>
+#include <utility>
 #include <vector>
 
 #include "fwn_internal.cuh"
@@ -587,10 +588,37 @@ __global__ void k_split_mesh_roots(int nmeshes, const int* __restrict__ root_nod
 }
 
 // ---- K4: FP64 refit ---------------------------------------------------------------------------
+// Exact float <-> double conversions on the integer pipes. GB300 runs conversions on its FP64 pipe
+// (2 operations per SM per cycle), which the refit's FP64 arithmetic already saturates; these give
+// the hardware's results bit for bit (IEEE: float -> double is exact, double -> float rounds to
+// nearest even) and fall back to the hardware conversion for the rare operands outside the
+// normal range (subnormal results, infinities, NaN).
+__device__ __forceinline__ double f2d(float x) {
+    const unsigned b = __float_as_uint(x);
+    const unsigned e = (b >> 23) & 0xffu;
+    if ((b & 0x7fffffffu) == 0u) return __hiloint2double((int)b, 0);  // +-0
+    if (e == 0u || e == 0xffu) return (double)x;
+    const unsigned hi = (b & 0x80000000u) | ((e + 896u) << 20) | ((b & 0x7fffffu) >> 3);
+    return __hiloint2double((int)hi, (int)(b << 29));
+}
+
+__device__ __forceinline__ float d2f(double x) {
+    const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+    const unsigned e = (hi >> 20) & 0x7ffu;
+    if ((hi & 0x7fffffffu) == 0u && lo == 0u) return __uint_as_float(hi);  // +-0
+    if (e < 897u || e > 1150u) return (float)x;  // float subnormal / overflow, inf, NaN
+    // 52-bit fraction = (hi & 0xfffff) : lo; keep its top 23 bits, round the 29 below to even
+    const unsigned f = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned rem = lo & 0x1fffffffu;
+    const unsigned up = (rem > 0x10000000u || (rem == 0x10000000u && (f & 1u))) ? 1u : 0u;
+    // a carry out of the fraction steps the exponent (to infinity past the largest float)
+    return __uint_as_float((hi & 0x80000000u) + (((e - 896u) << 23) | f) + up);
+}
+
 __device__ __forceinline__ double round_up_float(double x) {
-    float f = (float)x;
-    if ((double)f < x) f = nextafterf(f, INFINITY);
-    return (double)f;
+    float f = d2f(x);
+    if (f2d(f) < x) f = nextafterf(f, INFINITY);
+    return f2d(f);
 }
 
 __device__ __forceinline__ void load_tri_d(const float* __restrict__ V, const int32_t* __restrict__ F,
@@ -598,9 +626,9 @@ __device__ __forceinline__ void load_tri_d(const float* __restrict__ V, const in
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
         const int64_t vi = vbase + F[3 * t + j];
-        v[j][0] = (double)V[3 * vi + 0];
-        v[j][1] = (double)V[3 * vi + 1];
-        v[j][2] = (double)V[3 * vi + 2];
+        v[j][0] = f2d(V[3 * vi + 0]);
+        v[j][1] = f2d(V[3 * vi + 1]);
+        v[j][2] = f2d(V[3 * vi + 2]);
     }
 }
 
@@ -624,8 +652,8 @@ __device__ __forceinline__ double fmad(double a, double b, double c) { return __
 // Squared distance of a vertex from P in FP64, fused at fixed places: the term whose maximum over
 // a node's vertices gives the node radius (leaves in leaf_moments, internal nodes in
 // k_node_radius; a maximum does not depend on the order of its terms).
-__device__ __forceinline__ double vertex_r2(double x, double y, double z, const double* P) {
-    const double dx = x - P[0], dy = y - P[1], dz = z - P[2];
+__device__ __forceinline__ double vertex_r2(float x, float y, float z, const double* P) {
+    const double dx = f2d(x) - P[0], dy = f2d(y) - P[1], dz = f2d(z) - P[2];
     return fmad(dx, dx, fmad(dy, dy, dz * dz));
 }
 
@@ -701,7 +729,7 @@ __device__ void leaf_moments(const float* __restrict__ V, const int32_t* __restr
     double P[3], e[3];
     for (int a = 0; a < 3; ++a) {
         const double pe = A > 0.0 ? S[a] / A : Cs[a] / cnt;
-        P[a] = (double)(float)pe;
+        P[a] = f2d(d2f(pe));
         e[a] = c0[a] - P[a];
     }
     for (int i = 0; i < 3; ++i) {
@@ -714,7 +742,7 @@ __device__ void leaf_moments(const float* __restrict__ V, const int32_t* __restr
         for (int j = 0; j < 3; ++j) R.M1[3 * i + j] = fmad(N[i], e[j], M1[3 * i + j]);
     }
     ScreenedMax sm;
-    const float Pf[3] = {(float)P[0], (float)P[1], (float)P[2]};
+    const float Pf[3] = {d2f(P[0]), d2f(P[1]), d2f(P[2])};
     for (int s = f; s <= l; ++s) {
         const int64_t t = tri_of_slot[s];
         const int m = (int)(keys[s] >> MORTON_BITS);
@@ -732,13 +760,22 @@ __device__ void leaf_moments(const float* __restrict__ V, const int32_t* __restr
     }
     R.area = A;
     R.r = round_up_float(sqrt(r2));
+    R.pad = 0.0;
 }
 
-__device__ __forceinline__ double ldcg_d(const double* p) { return __ldcg(p); }
+// Children's records: CG = read through L2 (ld.global.cg), for the atomic ascent, where other
+// threads of the same launch wrote them; otherwise plain cached loads (an earlier launch wrote
+// them), so the fields of one record share its L1 sectors.
+template <bool CG>
+__device__ __forceinline__ double ld_rec(const double* p) {
+    if constexpr (CG) return __ldcg(p);
+    else return *p;
+}
 
+template <bool CG>
 __device__ void combine_moments(const StageRec* __restrict__ a_, const StageRec* __restrict__ b_,
                                 StageRec& R) {
-    // children were written by other threads: read through L2 (ld.global.cg)
+    auto ldcg_d = [](const double* p) { return ld_rec<CG>(p); };
     double Pa[3], Pb[3], Na[3], Nb[3], M1a[9], M1b[9];
     const double Aa = ldcg_d(&a_->area), Ab = ldcg_d(&b_->area);
     for (int i = 0; i < 3; ++i) {
@@ -755,7 +792,7 @@ __device__ void combine_moments(const StageRec* __restrict__ a_, const StageRec*
     double P[3], ea[3], eb[3];
     for (int i = 0; i < 3; ++i) {
         const double pe = A > 0.0 ? fmad(Aa, Pa[i], Ab * Pb[i]) / A : (Pa[i] + Pb[i]) * 0.5;
-        P[i] = (double)(float)pe;
+        P[i] = f2d(d2f(pe));
         ea[i] = Pa[i] - P[i];
         eb[i] = Pb[i] - P[i];
     }
@@ -779,6 +816,7 @@ __device__ void combine_moments(const StageRec* __restrict__ a_, const StageRec*
         }
     R.area = A;
     R.r = 0.0;  // exact radius about P from the node's vertices: k_node_radius, after the refit
+    R.pad = 0.0;
 }
 
 __device__ __forceinline__ void store_rec(StageRec* dst, const StageRec& R) {
@@ -794,13 +832,14 @@ __global__ void k_refit(int num_leaves, const int* __restrict__ leaf_list,
                         const uint32_t* __restrict__ tri_of_slot, const float* __restrict__ V,
                         const int32_t* __restrict__ F, const int64_t* __restrict__ voff,
                         StageRec* __restrict__ stage, int* __restrict__ visit,
-                        unsigned* __restrict__ status, bool multi_root) {
+                        unsigned* __restrict__ status, bool multi_root, bool ascend) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= num_leaves) return;
     const int e = leaf_list[k];  // one emitted leaf per thread
     StageRec R;
     leaf_moments(V, F, voff, keys, tri_of_slot, first[e], last[e], R);
     store_rec(&stage[pos[e]], R);
+    if (!ascend) return;  // the internal nodes follow level by level (k_refit_level)
     int v = e;
     int guard = 0;
     while (v != 0) {
@@ -818,7 +857,7 @@ __global__ void k_refit(int num_leaves, const int* __restrict__ leaf_list,
             atomicOr(status, ST_REFIT_ORPHAN);
             return;
         }
-        combine_moments(&stage[pl], &stage[pr], R);
+        combine_moments<true>(&stage[pl], &stage[pr], R);
         store_rec(&stage[pos[p]], R);
         v = p;
         if (++guard > 4 * 64 + 64) {  // depth is bounded by key bits + index bits
@@ -826,6 +865,25 @@ __global__ void k_refit(int num_leaves, const int* __restrict__ leaf_list,
             return;
         }
     }
+}
+
+// The internal nodes of one level of a split tree (nodes[0 .. count)): each combines its two
+// children, whose records the leaf pass or the previous (deeper) level wrote.
+__global__ void k_refit_level(int count, const int* __restrict__ nodes,
+                              const int* __restrict__ left, const int* __restrict__ right,
+                              const int* __restrict__ pos, StageRec* __restrict__ stage,
+                              unsigned* __restrict__ status) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const int p = nodes[k];
+    const int l = left[p], r = right[p];
+    if (l < 0 || r < 0 || pos[l] < 0 || pos[r] < 0) {
+        atomicOr(status, ST_REFIT_ORPHAN);
+        return;
+    }
+    StageRec R;
+    combine_moments<false>(&stage[pos[l]], &stage[pos[r]], R);
+    store_rec(&stage[pos[p]], R);
 }
 
 // ---- K4a: exact node radii ------------------------------------------------------------------------
@@ -848,7 +906,7 @@ constexpr int kRadiusChunk = 2048;
 // bit for bit, at a few FP64 terms per run instead of three per triangle.
 __device__ __forceinline__ double slots_r2(const TriF32* __restrict__ tris, int s0, int s1,
                                            const double* P, int lane) {
-    const float Pf[3] = {(float)P[0], (float)P[1], (float)P[2]};
+    const float Pf[3] = {d2f(P[0]), d2f(P[1]), d2f(P[2])};
     auto est = [&](float x, float y, float z) {
         const float dx = x - Pf[0], dy = y - Pf[1], dz = z - Pf[2];
         return (dx * dx + dy * dy) + dz * dz;
@@ -906,22 +964,98 @@ __global__ void k_radius_list(int num_nodes, const uint64_t* __restrict__ keys,
         list[atomicAdd(count, 1)] = u;
 }
 
-// One warp per listed node (grid-stride), all lanes on its slot run.
-__global__ void k_node_radius_small(const int* __restrict__ list, const int* __restrict__ count,
-                                    const int* __restrict__ first, const int* __restrict__ last,
-                                    const int* __restrict__ pos, const StageRec* __restrict__ stage,
-                                    const TriF32* __restrict__ tris,
-                                    unsigned long long* __restrict__ r2bits) {
+// One warp per listed node (grid-stride), all lanes on its slot run. The float screen runs per
+// node; the vertices that pass it (a few per node) queue in the warp's shared buffer across the
+// warp's nodes and get their exact FP64 terms 32 at a time, one per lane, so the FP64 pipe (2
+// operations per SM per cycle on GB300, whatever the number of active lanes) sees full warps;
+// each term goes to its node's maximum by atomicMax on the bit pattern (r2bits starts at 0).
+constexpr int kRadiusWarps = 8;      // warps per block of k_node_radius_small
+constexpr int kRadiusQueue = 128;    // queued vertices per warp (one flush of 32 + 3 x 32 added)
+
+struct RadiusQueue {
+    float x[kRadiusQueue], y[kRadiusQueue], z[kRadiusQueue];
+    int node[kRadiusQueue];
+};
+
+__device__ __forceinline__ void radius_flush(RadiusQueue& q, int count,
+                                             const StageRec* __restrict__ stage,
+                                             unsigned long long* __restrict__ r2bits, int lane) {
+    __syncwarp();
+    if (lane < count) {
+        const int i = q.node[lane];
+        const double P[3] = {stage[i].P[0], stage[i].P[1], stage[i].P[2]};
+        const double r2 = vertex_r2(q.x[lane], q.y[lane], q.z[lane], P);
+        atomicMax(&r2bits[i], (unsigned long long)__double_as_longlong(r2));
+    }
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(32 * kRadiusWarps)
+k_node_radius_small(const int* __restrict__ list, const int* __restrict__ count,
+                    const int* __restrict__ first, const int* __restrict__ last,
+                    const int* __restrict__ pos, const StageRec* __restrict__ stage,
+                    const TriF32* __restrict__ tris, unsigned long long* __restrict__ r2bits) {
+    __shared__ RadiusQueue queues[kRadiusWarps];
+    RadiusQueue& q = queues[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
+    const unsigned lt = (1u << lane) - 1u;
     const int total = *count;
     const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
+    int queued = 0;  // warp-uniform
     for (int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); w < total; w += nwarps) {
         const int v = list[w];
         const int i = pos[v];
-        const double P[3] = {stage[i].P[0], stage[i].P[1], stage[i].P[2]};
-        const double r2 = slots_r2(tris, first[v], last[v] + 1, P, lane);
-        if (lane == 0) r2bits[i] = (unsigned long long)__double_as_longlong(r2);
+        const int s0 = first[v], s1 = last[v] + 1;
+        const float Pf[3] = {d2f(stage[i].P[0]), d2f(stage[i].P[1]), d2f(stage[i].P[2])};
+        auto est = [&](float x, float y, float z) {
+            const float dx = x - Pf[0], dy = y - Pf[1], dz = z - Pf[2];
+            return (dx * dx + dy * dy) + dz * dz;
+        };
+        float m = 0.f;
+        for (int s = s0 + lane; s < s1; s += 32) {
+            const float4 t0 = tris[s].t0, t1 = tris[s].t1, t2 = tris[s].t2;
+            m = fmaxf(m, fmaxf(est(t0.x, t0.y, t0.z), fmaxf(est(t0.w, t1.x, t1.y), est(t1.z, t1.w, t2.x))));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        const bool all = !(m < INFINITY);
+        const float thr = m * 0.99999f - 1e-37f;
+        for (int base = s0; base < s1; base += 32) {  // warp-uniform trip count
+            const int s = base + lane;
+            float vx[3] = {0.f, 0.f, 0.f}, vy[3] = {0.f, 0.f, 0.f}, vz[3] = {0.f, 0.f, 0.f};
+            if (s < s1) {
+                const float4 t0 = tris[s].t0, t1 = tris[s].t1, t2 = tris[s].t2;
+                vx[0] = t0.x; vy[0] = t0.y; vz[0] = t0.z;
+                vx[1] = t0.w; vy[1] = t1.x; vz[1] = t1.y;
+                vx[2] = t1.z; vy[2] = t1.w; vz[2] = t2.x;
+            }
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const bool c = s < s1 && (all || est(vx[j], vy[j], vz[j]) >= thr);
+                const unsigned bal = __ballot_sync(0xffffffffu, c);
+                if (c) {
+                    const int k = queued + __popc(bal & lt);
+                    q.x[k] = vx[j];
+                    q.y[k] = vy[j];
+                    q.z[k] = vz[j];
+                    q.node[k] = i;
+                }
+                queued += __popc(bal);
+            }
+            while (queued >= 32) {  // evaluate 32, move the rest down (each lane its own column)
+                radius_flush(q, 32, stage, r2bits, lane);
+                for (int k = 32 + lane; k < queued; k += 32) {
+                    q.x[k - 32] = q.x[k];
+                    q.y[k - 32] = q.y[k];
+                    q.z[k - 32] = q.z[k];
+                    q.node[k - 32] = q.node[k];
+                }
+                __syncwarp();
+                queued -= 32;
+            }  // queued < 32 here, so the next slot block adds at most 96: < kRadiusQueue
+        }
     }
+    if (queued > 0) radius_flush(q, queued, stage, r2bits, lane);
 }
 
 // Grid-stride over the chunks: chunk c belongs to the last node u with off[u] <= c.
@@ -1022,17 +1156,17 @@ __global__ void k_convert(int num_nodes, const uint64_t* __restrict__ keys, cons
     }
     if (n32) {
         NodeF32 o;
-        o.s0 = make_float4((float)R.P[0], (float)R.P[1], (float)R.P[2], (float)R.r);
+        o.s0 = make_float4(d2f(R.P[0]), d2f(R.P[1]), d2f(R.P[2]), d2f(R.r));
         o.skip = skip[u];
         o.tri_begin = tb;
         o.tri_count = tc;
-        o.trM1 = (float)c.trM1;
-        o.m0 = make_float4((float)c.N[0], (float)c.N[1], (float)c.N[2], (float)c.W[0]);
-        o.m1 = make_float4((float)c.W[1], (float)c.W[2], (float)c.C[0], (float)c.C[1]);
-        o.m2 = make_float4((float)c.C[2], (float)c.C[3], (float)c.C[4], (float)c.C[5]);
-        o.m3 = make_float4((float)c.D[0], (float)c.D[1], (float)c.D[2], (float)c.D[3]);
-        o.m4 = make_float4((float)c.D[4], (float)c.D[5], (float)c.D[6], (float)c.D[7]);
-        o.m5 = make_float4((float)c.D[8], (float)c.D[9], 0.f, 0.f);
+        o.trM1 = d2f(c.trM1);
+        o.m0 = make_float4(d2f(c.N[0]), d2f(c.N[1]), d2f(c.N[2]), d2f(c.W[0]));
+        o.m1 = make_float4(d2f(c.W[1]), d2f(c.W[2]), d2f(c.C[0]), d2f(c.C[1]));
+        o.m2 = make_float4(d2f(c.C[2]), d2f(c.C[3]), d2f(c.C[4]), d2f(c.C[5]));
+        o.m3 = make_float4(d2f(c.D[0]), d2f(c.D[1]), d2f(c.D[2]), d2f(c.D[3]));
+        o.m4 = make_float4(d2f(c.D[4]), d2f(c.D[5]), d2f(c.D[6]), d2f(c.D[7]));
+        o.m5 = make_float4(d2f(c.D[8]), d2f(c.D[9]), 0.f, 0.f);
         n32[i] = o;
     }
     if (n64) {
@@ -1185,6 +1319,10 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
         const uint32_t* tri_of_slot = nullptr;
         int num_nodes = 0;
         unsigned st_h = 0;
+        // split tree: the internal nodes split at each level (int_nodes[off, off + count)), for
+        // the level-by-level refit
+        std::vector<std::pair<int, int>> split_levels;
+        int* int_nodes = split ? (int*)track(dalloc<int>(n, st)) : nullptr;
         auto check_input = [&]() {
             FWN_CUDA_CHECK(cudaMemcpyAsync(&st_h, status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
             FWN_CUDA_CHECK(cudaStreamSynchronize(st));
@@ -1320,6 +1458,11 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
                 k_split_children<<<grid_for(nact, 128), 128, 0, st>>>(
                     nact, node_base, K, seg_a[0], seg_a[1], seg_a[2], lflags, first, last, parent,
                     left, right, next_count, seg_b[0], seg_b[1], seg_b[2], box_b, child_next);
+                const int lvl_off = split_levels.empty() ? 0 : split_levels.back().first + split_levels.back().second;
+                if (lvl_off + nact > n) throw Error(FWN_INTERNAL, "split build internal node overflow");
+                FWN_CUDA_CHECK(cudaMemcpyAsync(int_nodes + lvl_off, seg_a[2], nact * sizeof(int),
+                                               cudaMemcpyDeviceToDevice, st));
+                split_levels.emplace_back(lvl_off, nact);
                 // lflags now holds the exclusive scan of the left flags (a slot's flag is the
                 // step from its entry to the next)
                 k_split_scatter<<<grid_for(n, 256), 256, 0, st>>>(n, *cur, *nxt, lflags, seg_a[0],
@@ -1366,7 +1509,13 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
         if (NL > 0)
             k_refit<<<grid_for(NL, 128), 128, 0, st>>>(NL, leaf_list, keys, parent, first, last, left,
                                                        right, pos, tri_of_slot, d_V, d_F, voff,
-                                                       stage, visit, status, split);
+                                                       stage, visit, status, split, !split);
+        // split tree: the internal nodes level by level, deepest first (a node's children are
+        // one level below it), one thread per node of a dense list; the atomic ascent leaves
+        // most lanes of its warps idle on GB300's narrow FP64 pipe
+        for (auto it = split_levels.rbegin(); it != split_levels.rend(); ++it)
+            k_refit_level<<<grid_for(it->second, 128), 128, 0, st>>>(
+                it->second, int_nodes + it->first, left, right, pos, stage, status);
         FWN_CUDA_CHECK(cudaGetLastError());
         FWN_CUDA_CHECK(cudaMalloc(&e.tris, (size_t)n * sizeof(TriF32)));
         FWN_CUDA_CHECK(cudaMalloc(&e.sorted_tri, (size_t)n * sizeof(int)));
@@ -1389,8 +1538,9 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
             FWN_CUDA_CHECK(cudaMemsetAsync(rlist, 0, sizeof(int), st));
             k_radius_list<<<grid_for(num_nodes, 256), 256, 0, st>>>(num_nodes, keys, first, last,
                                                                     flags, rlist + 1, rlist);
-            k_node_radius_small<<<sms * 16, 256, 0, st>>>(rlist + 1, rlist, first, last, pos,
-                                                          stage, e.tris, r2bits);
+            k_node_radius_small<<<sms * 8, 32 * kRadiusWarps, 0, st>>>(rlist + 1, rlist, first,
+                                                                       last, pos, stage, e.tris,
+                                                                       r2bits);
             k_node_radius<<<sms * 4, 256, 0, st>>>(num_nodes, rchunk, first, last, pos, stage,
                                                    e.tris, r2bits);
         }

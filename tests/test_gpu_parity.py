@@ -585,3 +585,23 @@ def test_save_load_round_trip(torch_cuda, tmp_path, builder):
     w2, i2 = f2.query_forest(Qd, qoff)
     torch_cuda.cuda.synchronize()
     assert torch_cuda.equal(w1, w2) and torch_cuda.equal(i1, i2)
+
+
+@pytest.mark.parametrize("builder", [0, 1])
+def test_fp32_records_round_fp64_records(torch_cuda, builder):
+    """Every coefficient of an FP32 node record is its FP64 record's value rounded to nearest
+    even (the build converts on the integer pipes; numpy's cast is the IEEE reference), and the
+    centre and radius, float values by construction, are equal."""
+    g = np.load(GOLDEN / "displaced.npz")
+    eng = _engine(g["V"], g["F"], leaf_size=8, builder=builder, records=BOTH)
+    n = eng.export_nodes()
+    f32, f64 = n["f32"], n["f64"]
+    pairs = [(slice(0, 4), slice(0, 4)),      # P, r
+             (slice(7, 8), slice(6, 7)),      # trM1
+             (slice(8, 14), slice(7, 13)),    # N, W
+             (slice(14, 20), slice(13, 19)),  # C
+             (slice(20, 30), slice(19, 29))]  # D
+    for a, b in pairs:
+        np.testing.assert_array_equal(f32[:, a], f64[:, b].astype(np.float32))
+    np.testing.assert_array_equal(f32[:, 0:4].astype(np.float64), f64[:, 0:4])
+    assert np.count_nonzero(f32[:, 8:30]) > 0.9 * f32[:, 8:30].size
