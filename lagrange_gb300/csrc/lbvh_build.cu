@@ -867,6 +867,52 @@ __global__ void k_refit(int num_leaves, const int* __restrict__ leaf_list,
     }
 }
 
+// The refit's leaf list grouped by triangle count (a counting sort over 1..16), so that the 32
+// leaves of a warp run the same number of triangle iterations: the FP64 pipe costs the same for
+// a warp instruction whatever the number of active lanes.
+constexpr int kLeafSizes = 17;  // counts 0..16 (WARP_LEAF_MAX); 0 does not occur
+
+__device__ __forceinline__ int leaf_size_of(const int* __restrict__ first,
+                                            const int* __restrict__ last, int u) {
+    return min(max(last[u] - first[u] + 1, 0), kLeafSizes - 1);
+}
+
+__global__ void k_leaf_hist(int nl, const int* __restrict__ leaves, const int* __restrict__ first,
+                            const int* __restrict__ last, int* __restrict__ hist) {
+    __shared__ int h[kLeafSizes];
+    if (threadIdx.x < kLeafSizes) h[threadIdx.x] = 0;
+    __syncthreads();
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nl) atomicAdd(&h[leaf_size_of(first, last, leaves[k])], 1);
+    __syncthreads();
+    if (threadIdx.x < kLeafSizes && h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], h[threadIdx.x]);
+}
+
+__global__ void k_leaf_offsets(int* __restrict__ hist) {  // one thread: exclusive scan in place
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int acc = 0;
+    for (int i = 0; i < kLeafSizes; ++i) {
+        const int c = hist[i];
+        hist[i] = acc;
+        acc += c;
+    }
+}
+
+__global__ void k_leaf_sort(int nl, const int* __restrict__ leaves, const int* __restrict__ first,
+                            const int* __restrict__ last, int* __restrict__ offset,
+                            int* __restrict__ sorted) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nl) return;
+    const int u = leaves[k];
+    const int sz = leaf_size_of(first, last, u);
+    const unsigned peers = __match_any_sync(__activemask(), sz);
+    const int leader = __ffs(peers) - 1;
+    int base = 0;
+    if ((int)(threadIdx.x & 31) == leader) base = atomicAdd(&offset[sz], __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    sorted[base + __popc(peers & ((1u << (threadIdx.x & 31)) - 1u))] = u;
+}
+
 // The internal nodes of one level of a split tree (nodes[0 .. count)): each combines its two
 // children, whose records the leaf pass or the previous (deeper) level wrote.
 __global__ void k_refit_level(int count, const int* __restrict__ nodes,
@@ -1506,6 +1552,16 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
         else e.stage = stage;
         FWN_CUDA_CHECK(cudaMemsetAsync(visit, 0, (size_t)nint * sizeof(int), st));
         FWN_CUDA_CHECK(cudaMemsetAsync(leaf_count, 0, sizeof(int), st));
+        if (NL > 0) {
+            int* hist = (int*)track(dalloc<int>(kLeafSizes, st));
+            int* leaf_sorted = (int*)track(dalloc<int>(NL, st));
+            FWN_CUDA_CHECK(cudaMemsetAsync(hist, 0, kLeafSizes * sizeof(int), st));
+            k_leaf_hist<<<grid_for(NL, 256), 256, 0, st>>>(NL, leaf_list, first, last, hist);
+            k_leaf_offsets<<<1, 32, 0, st>>>(hist);
+            k_leaf_sort<<<grid_for(NL, 256), 256, 0, st>>>(NL, leaf_list, first, last, hist,
+                                                          leaf_sorted);
+            leaf_list = leaf_sorted;
+        }
         if (NL > 0)
             k_refit<<<grid_for(NL, 128), 128, 0, st>>>(NL, leaf_list, keys, parent, first, last, left,
                                                        right, pos, tri_of_slot, d_V, d_F, voff,
