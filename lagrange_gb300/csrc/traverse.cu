@@ -483,24 +483,29 @@ struct WarpSmem {
     float res[32 * QPL * WARP_LEAF_MAX];
 };
 
-template <bool STATS, int QPL, bool PAIRED = false>
+// UEND: every slot of the warp walks the same subtree, ending at uend (one mesh: its subtree is
+// the whole node range, and no skip link points past it), so a finished slot's resume index is
+// uend itself and the per-slot end test drops out of every step.
+template <bool STATS, int QPL, bool PAIRED = false, bool UEND = false>
 __device__ __forceinline__ void warp_walk(const NodeF32* __restrict__ nodes,
                                           const TriF32* __restrict__ tris, Slot (&sl)[QPL],
                                           float cond, float beta, WarpSmem<QPL>& sm,
-                                          QCounters& qc, unsigned* __restrict__ status) {
+                                          QCounters& qc, unsigned* __restrict__ status,
+                                          int uend = DONE) {
     const int lane = threadIdx.x & 31;
     const unsigned lt = lanemask_lt();
-    int lo = DONE;
+    const int stop = UEND ? uend : DONE;
+    int lo = stop;
 #pragma unroll
     for (int j = 0; j < QPL; ++j) {
-        if (sl[j].resume >= sl[j].end) sl[j].resume = DONE;
+        if (sl[j].resume >= (UEND ? uend : sl[j].end)) sl[j].resume = stop;
         lo = min(lo, sl[j].resume);
     }
     int cursor = __reduce_min_sync(0xffffffffu, lo);
     float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
     int4 b = make_int4(0, 0, 0, 0);
-    if (cursor != DONE) load_sector0(nodes + cursor, a, b);
-    while (cursor != DONE) {
+    if (cursor != stop) load_sector0(nodes + cursor, a, b);
+    while (cursor != stop) {
         const NodeF32* nd = nodes + cursor;
         float4 m0, m1, m2, m3, m4, m5;
         ld_v8(&nd->m0, m0, m1);
@@ -511,7 +516,7 @@ __device__ __forceinline__ void warp_walk(const NodeF32* __restrict__ nodes,
         const bool leafnode = b.z > 0;
         bool do_far[QPL], need_leaf[QPL];
         float dx[QPL], dy[QPL], dz[QPL], d2[QPL];
-        int lo2 = DONE;
+        int lo2 = stop;
 #pragma unroll
         for (int j = 0; j < QPL; ++j) {
             const bool active = sl[j].resume == cursor;
@@ -519,7 +524,8 @@ __device__ __forceinline__ void warp_walk(const NodeF32* __restrict__ nodes,
                                       dy[j], dz[j], d2[j]);
             if (STATS && active) ++qc.nodes;
             int nr = (far || leafnode) ? b.x : cursor + 1;
-            nr = nr >= sl[j].end ? DONE : nr;
+            if constexpr (UEND) nr = min(nr, uend);  // a well-formed tree never exceeds it
+            else nr = nr >= sl[j].end ? DONE : nr;
             sl[j].resume = active ? nr : sl[j].resume;
             do_far[j] = active && far;
             need_leaf[j] = active && !far && leafnode;
@@ -528,7 +534,7 @@ __device__ __forceinline__ void warp_walk(const NodeF32* __restrict__ nodes,
         const int nc = __reduce_min_sync(0xffffffffu, lo2);
         float4 an = a;
         int4 bn = b;
-        if (nc != DONE) load_sector0(nodes + nc, an, bn);  // next step's test sector, in flight
+        if (nc != stop) load_sector0(nodes + nc, an, bn);  // next step's test sector, in flight
         if constexpr (PAIRED && QPL == 2) {
             // both slots' Taylor terms in one paired evaluation when any lane of either is far
             if (__any_sync(0xffffffffu, do_far[0] || do_far[1])) {
@@ -649,7 +655,8 @@ k_query_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
         sl[j].resume = valid ? mi.root : DONE;
         sl[j].end = mi.end;
     }
-    warp_walk<STATS, QPL, PAIRED>(nodes, tris, sl, mi.cond, beta, smem[w], qc, status);
+    warp_walk<STATS, QPL, PAIRED, true>(nodes, tris, sl, mi.cond, beta, smem[w], qc, status,
+                                         mi.end);
 #pragma unroll
     for (int j = 0; j < QPL; ++j) {
         if (qi[j] < 0) continue;
@@ -707,7 +714,8 @@ k_query_grid(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
         sl[q].end = mi.end;
     }
     QCounters qc;
-    warp_walk<false, QPL, PAIRED>(nodes, tris, sl, mi.cond, beta, smem[w], qc, status);
+    warp_walk<false, QPL, PAIRED, true>(nodes, tris, sl, mi.cond, beta, smem[w], qc, status,
+                                         mi.end);
 #pragma unroll
     for (int q = 0; q < QPL; ++q)
         if (out[q] >= 0) write_result(sl[q], out[q], omega, inside);
