@@ -605,3 +605,35 @@ def test_fp32_records_round_fp64_records(torch_cuda, builder):
         np.testing.assert_array_equal(f32[:, a], f64[:, b].astype(np.float32))
     np.testing.assert_array_equal(f32[:, 0:4].astype(np.float64), f64[:, 0:4])
     assert np.count_nonzero(f32[:, 8:30]) > 0.9 * f32[:, 8:30].size
+
+
+def test_known_answers_on_the_engine(torch_cuda):
+    """The closed-form cases on the GPU engine, mixed and FP64 forms: a closed sphere gives w = 1
+    inside and 0 outside, reversed orientation gives -w, two disjoint spheres add, a sphere
+    nested in another gives 2, the unit cube gives |w| = 1 at its centre and an open box 5/6
+    (within the beta = 2 far-field error for the tree, 1e-9 with beta -> infinity)."""
+    V, F = W.uv_sphere()
+    Q = np.array([[0, 0, 0], [0.3, -0.2, 0.5], [2, 0, 0], [0, 0, -1.2]], np.float32)
+    for kw, tol in (({}, 1e-2), ({"beta": 1e30}, 1e-6)):
+        w, ins = _q(_engine(V, F), torch_cuda, Q, **kw)
+        np.testing.assert_allclose(w / FOUR_PI, [1, 1, 0, 0], atol=tol)
+        np.testing.assert_array_equal(ins, [1, 1, 0, 0])
+        wr, insr = _q(_engine(V, F[:, [0, 2, 1]]), torch_cuda, Q, **kw)
+        np.testing.assert_allclose(wr, -w, atol=tol * FOUR_PI)
+        assert not insr.any()
+    V2 = np.concatenate([V, V + np.float32(3.0), V * np.float32(0.5)])
+    F2 = np.concatenate([F, F + len(V), F + 2 * len(V)]).astype(np.int32)
+    Q2 = np.array([[0.1, 0, 0], [3, 3, 3], [1.5, 1.5, 1.5], [0.8, 0, 0]], np.float32)
+    e2 = _engine(V2, F2)
+    for kw, tol in (({}, 1e-2), ({"beta": 1e30}, 1e-6)):
+        w, _ = _q(e2, torch_cuda, Q2, **kw)
+        np.testing.assert_allclose(w / FOUR_PI, [2, 1, 0, 1], atol=tol)
+        _, _, w64 = _q(e2, torch_cuda, Q2, precision=fwn.PRECISION_FP64, omega_f64=True, **kw)
+        np.testing.assert_allclose(w64 / FOUR_PI, [2, 1, 0, 1], atol=tol)
+    cv = np.array([[x, y, z] for x in (0, 1) for y in (0, 1) for z in (0, 1)], np.float32)
+    quads = [(0, 1, 3, 2), (4, 6, 7, 5), (0, 4, 5, 1), (2, 3, 7, 6), (0, 2, 6, 4), (1, 5, 7, 3)]
+    cf = np.array([t for a, b, c, d in quads for t in ((a, b, c), (a, c, d))], np.int32)
+    cen = np.array([[0.5, 0.5, 0.5]], np.float32)
+    for faces, want in ((cf, 1.0), (cf[2:], 5 / 6)):
+        w, _ = _q(_engine(cv, faces), torch_cuda, cen, beta=1e30)
+        assert abs(abs(w[0]) / FOUR_PI - want) < 1e-6
