@@ -120,25 +120,6 @@ template <class Fn> fwn_status guarded(Fn&& fn) {
     }
 }
 
-void validate_config(const fwn_config& c) {
-    if (!(c.beta > 0.f) || !std::isfinite(c.beta)) throw Error(FWN_INVALID_ARG, "beta must be finite and > 0");
-    if (c.leaf_size < 1 || c.leaf_size > 16) throw Error(FWN_INVALID_ARG, "leaf_size must be in [1, 16]");
-    if (!(c.records & (FWN_RECORDS_F32 | FWN_RECORDS_F64)))
-        throw Error(FWN_INVALID_ARG, "records must include FWN_RECORDS_F32 or FWN_RECORDS_F64");
-    if (c.precision != FWN_PRECISION_MIXED && c.precision != FWN_PRECISION_FP64)
-        throw Error(FWN_INVALID_ARG, "unknown precision");
-    if (c.traversal < FWN_TRAVERSAL_AUTO || c.traversal > FWN_TRAVERSAL_WARP)
-        throw Error(FWN_INVALID_ARG, "unknown traversal");
-    if (c.block_size < 0 || c.block_size > 1024 || c.block_size % 32 != 0)
-        throw Error(FWN_INVALID_ARG, "block_size must be 0 or a multiple of 32 <= 1024");
-    if (!(c.fp64_near_scale >= 0.f) || !std::isfinite(c.fp64_near_scale))
-        throw Error(FWN_INVALID_ARG, "fp64_near_scale must be finite and >= 0");
-    if (!(c.fp64_cond >= 0.f) || !std::isfinite(c.fp64_cond))
-        throw Error(FWN_INVALID_ARG, "fp64_cond must be finite and >= 0");
-    if (c.tuning < 0 || c.tuning > 6) throw Error(FWN_INVALID_ARG, "tuning must be in [0, 6]");
-    if (c.builder != FWN_BUILDER_LBVH && c.builder != FWN_BUILDER_SPLIT)
-        throw Error(FWN_INVALID_ARG, "builder must be FWN_BUILDER_LBVH or FWN_BUILDER_SPLIT");
-}
 
 struct OwnedStream {
     cudaStream_t s = nullptr;
@@ -201,6 +182,27 @@ void check_mesh_args(const void* V, int64_t nv, const void* F, int64_t nf) {
 }
 
 }  // namespace
+
+void validate_config(const fwn_config& c) {
+    if (!(c.beta > 0.f) || !std::isfinite(c.beta)) throw Error(FWN_INVALID_ARG, "beta must be finite and > 0");
+    if (c.leaf_size < 1 || c.leaf_size > 16) throw Error(FWN_INVALID_ARG, "leaf_size must be in [1, 16]");
+    if (!(c.records & (FWN_RECORDS_F32 | FWN_RECORDS_F64)))
+        throw Error(FWN_INVALID_ARG, "records must include FWN_RECORDS_F32 or FWN_RECORDS_F64");
+    if (c.precision != FWN_PRECISION_MIXED && c.precision != FWN_PRECISION_FP64)
+        throw Error(FWN_INVALID_ARG, "unknown precision");
+    if (c.traversal < FWN_TRAVERSAL_AUTO || c.traversal > FWN_TRAVERSAL_WARP)
+        throw Error(FWN_INVALID_ARG, "unknown traversal");
+    if (c.block_size < 0 || c.block_size > 1024 || c.block_size % 32 != 0)
+        throw Error(FWN_INVALID_ARG, "block_size must be 0 or a multiple of 32 <= 1024");
+    if (!(c.fp64_near_scale >= 0.f) || !std::isfinite(c.fp64_near_scale))
+        throw Error(FWN_INVALID_ARG, "fp64_near_scale must be finite and >= 0");
+    if (!(c.fp64_cond >= 0.f) || !std::isfinite(c.fp64_cond))
+        throw Error(FWN_INVALID_ARG, "fp64_cond must be finite and >= 0");
+    if (c.tuning < 0 || c.tuning > 6) throw Error(FWN_INVALID_ARG, "tuning must be in [0, 6]");
+    if (c.builder != FWN_BUILDER_LBVH && c.builder != FWN_BUILDER_SPLIT)
+        throw Error(FWN_INVALID_ARG, "builder must be FWN_BUILDER_LBVH or FWN_BUILDER_SPLIT");
+}
+
 }  // namespace fwn
 
 using namespace fwn;

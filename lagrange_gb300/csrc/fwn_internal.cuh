@@ -205,6 +205,9 @@ struct Engine {
     ~Engine();
 };
 
+// Throws FWN_INVALID_ARG naming the first field of c out of range (fwn_capi.cu).
+void validate_config(const fwn_config& c);
+
 // Queries launch on the current device with the engine's device pointers, so the current device
 // must be the one the engine was built on (a stream passed by the caller belongs to it as well).
 inline void require_engine_device(const Engine& e) {

@@ -187,6 +187,11 @@ extern "C" FWN_API fwn_status fwn_load(const char* path, fwn_handle* out) {
                                 (uint64_t)E * (hd.has64 ? sizeof(NodeF64) : 0) +
                                 (uint64_t)nf * (sizeof(TriF32) + sizeof(int));
         if (hd.payload_bytes != expect) throw Error(FWN_INVALID_ARG, "engine file holds inconsistent sizes");
+        // the record sets are the ones in the file (the FP64 staging moments are not saved); the
+        // rest of the configuration must pass the same checks as a build's
+        fwn_config cfg = hd.cfg;
+        cfg.records = (hd.has32 ? FWN_RECORDS_F32 : 0) | (hd.has64 ? FWN_RECORDS_F64 : 0);
+        validate_config(cfg);
         Fnv sum;
         std::vector<MeshInfo> meshes((size_t)M);
         std::vector<NodeF32> n32(hd.has32 ? (size_t)E : 0);
@@ -207,14 +212,13 @@ extern "C" FWN_API fwn_status fwn_load(const char* path, fwn_handle* out) {
         for (int s : sorted)
             if (s < 0 || (int64_t)s >= nf) throw Error(FWN_INVALID_ARG, "engine file holds an inconsistent triangle id");
         std::unique_ptr<Engine> e(new Engine());
-        e->cfg = hd.cfg;
+        e->cfg = cfg;
         FWN_CUDA_CHECK(cudaGetDevice(&e->device));
         e->nv = hd.nv;
         e->nf = nf;
         e->nmeshes = M;
         e->num_nodes = E;
         e->num_leaves = hd.num_leaves;
-        e->cfg.records &= ~FWN_RECORDS_MOMENTS;  // the FP64 staging moments are not saved
         e->nodes32 = to_device(n32);
         e->nodes64 = to_device(n64);
         e->tris = to_device(tris);

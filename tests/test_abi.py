@@ -132,7 +132,7 @@ def test_load_refuses_bad_files_before_device_work(engine_lib, tmp_path):
     assert L.fwn_save(None, b"x") == 6
 
 
-def _engine_file(path, *, skip=1, tri_count=1, root=0, end=1, tri_id=0, flip=False):
+def _engine_file(path, *, skip=1, tri_count=1, root=0, end=1, tri_id=0, flip=False, leaf=8):
     """A one-mesh, one-leaf engine file laid out as fwn_save writes it (header, MeshInfo,
     NodeF32, TriF32, triangle id), with a correct FNV-1a 64 checksum unless `flip`."""
     import struct
@@ -145,7 +145,8 @@ def _engine_file(path, *, skip=1, tri_count=1, root=0, end=1, tri_id=0, flip=Fal
         h = ((h ^ b) * 1099511628211) & 0xFFFFFFFFFFFFFFFF
     if flip:
         payload[70] ^= 1
-    cfg = bytes(fwn.config_default())
+    cfg = bytes(fwn.config_default(leaf_size=8))
+    cfg = cfg[:4] + struct.pack("<i", leaf) + cfg[8:]  # leaf_size follows beta
     assert len(cfg) == 64
     header = (b"FWNGB300" + struct.pack("<II", 1, 144) + cfg +
               struct.pack("<5q2i2Q", 3, 1, 1, 1, 1, 1, 0, len(payload), h))
@@ -170,7 +171,7 @@ def test_load_checks_payload_before_device_work(engine_lib, tmp_path):
              ({"skip": 2}, "inconsistent node"), ({"tri_count": 2}, "inconsistent node"),
              ({"tri_count": 17}, "inconsistent node"), ({"root": 1}, "mesh root"),
              ({"end": 2}, "mesh root"), ({"tri_id": 1}, "triangle id"),
-             ({"tri_id": -1}, "triangle id")]
+             ({"tri_id": -1}, "triangle id"), ({"leaf": 99}, "leaf_size")]
     for i, (kw, what) in enumerate(cases):
         st, msg = status(_engine_file(tmp_path / f"c{i}.fwn", **kw))
         assert st == 1 and what in msg and not h.value, (kw, msg)

@@ -637,3 +637,35 @@ def test_known_answers_on_the_engine(torch_cuda):
     for faces, want in ((cf, 1.0), (cf[2:], 5 / 6)):
         w, _ = _q(_engine(cv, faces), torch_cuda, cen, beta=1e30)
         assert abs(abs(w[0]) / FOUR_PI - want) < 1e-6
+
+
+@pytest.mark.parametrize("builder", [0, 1])
+def test_forest_many_ragged_meshes(torch_cuda, oracle_mod, builder):
+    """3,000 meshes of 0 to 24 triangles (every fifth one empty, some without queries), with
+    0 to 9 queries each: one forest build and one persistent query against the FP64 brute
+    force of each mesh (beta -> infinity: exact sums, so the mixed form is within 1e-5)."""
+    rng = np.random.default_rng(21)
+    Vs, Fs, Qs = [], [], []
+    for m in range(3000):
+        nf = 0 if m % 5 == 0 else int(rng.integers(1, 25))
+        nv = 3 * nf
+        Vs.append(rng.normal(size=(nv, 3)).astype(np.float32) + np.float32(m % 7))
+        Fs.append(np.arange(nv, dtype=np.int32).reshape(-1, 3))
+        Qs.append(rng.normal(size=(int(rng.integers(0, 10)), 3)).astype(np.float32) + np.float32(m % 7))
+    voff = np.concatenate([[0], np.cumsum([len(v) for v in Vs])]).astype(np.int64)
+    foff = np.concatenate([[0], np.cumsum([len(f) for f in Fs])]).astype(np.int64)
+    qoff = np.concatenate([[0], np.cumsum([len(q) for q in Qs])]).astype(np.int64)
+    V, F, Q = np.concatenate(Vs), np.concatenate(Fs), np.concatenate(Qs)
+    forest = fwn.Forest(V, voff, F, foff, records=BOTH, leaf_size=4, builder=builder)
+    torch = torch_cuda
+    Qd = torch.from_numpy(Q).cuda()
+    w, ins = forest.query_forest(Qd, qoff, beta=1e30)
+    w64, _ = forest.query_forest(Qd, qoff, precision=fwn.PRECISION_FP64, beta=1e30)
+    torch.cuda.synchronize()
+    w, w64, ins = w.cpu().numpy(), w64.cpu().numpy(), ins.cpu().numpy()
+    ref = np.concatenate([oracle_mod.brute_f64(Vs[m], Fs[m], Qs[m]) if len(Qs[m]) else
+                          np.zeros(0) for m in range(3000)])
+    np.testing.assert_allclose(w64, ref, rtol=0, atol=1e-6)
+    np.testing.assert_allclose(w, ref, rtol=0, atol=1e-5 * FOUR_PI)
+    empty = np.repeat(np.arange(3000) % 5 == 0, np.diff(qoff))
+    assert np.all(w[empty] == 0) and not ins[empty].any()
