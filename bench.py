@@ -87,6 +87,7 @@ def parse():
     p.add_argument("--workload", default="icosphere",
                    choices=["icosphere", "soup", "uvsphere", "forest", "voxel"])
     p.add_argument("--nu", type=int, default=None)
+    p.add_argument("--meshes", type=int, default=512)  # forest workload: number of meshes
     p.add_argument("--queries", type=int, default=None)
     p.add_argument("--leaf", type=int, default=0)  # 0: the autotuner picks (untimed)
     p.add_argument("--tuning", type=int, default=0)  # with --leaf: warp-schedule variant (0 auto)
@@ -1011,11 +1012,11 @@ def run_forest(args, rank, world, local):
     from lagrange_gb300 import workloads as W
 
     t0 = time.perf_counter()
-    fo = W.batched_forest_workload() if args.workload == "forest" else W.voxel_workload(
+    fo = W.batched_forest_workload(n_meshes=args.meshes) if args.workload == "forest" else W.voxel_workload(
         nu=args.nu or 500)
     gen_s = time.perf_counter() - t0
     result = measure_forest(fo, dev, dist, rank, world, leaf=args.leaf, builder=args.builder,
-                            steps=args.steps,
+                            tuning=args.tuning, steps=args.steps,
                             warmup=args.warmup, e2e=not args.no_e2e, cpu=not args.no_cpu,
                             fp64=not args.no_fp64, clocks=not args.no_clocks,
                             grid=args.workload == "voxel", local=local)
@@ -1023,8 +1024,8 @@ def run_forest(args, rank, world, local):
     return result
 
 
-def measure_forest(fo, dev, dist, rank, world, *, leaf=0, builder=0, steps=10, warmup=3, e2e=True,
-                   cpu=True, fp64=True, clocks=True, grid=False, local=0):
+def measure_forest(fo, dev, dist, rank, world, *, leaf=0, builder=0, tuning=0, steps=10,
+                   warmup=3, e2e=True, cpu=True, fp64=True, clocks=True, grid=False, local=0):
     """Measures one forest workload (see run_forest) and returns its result dict."""
     import torch
     import lagrange_gb300 as fwn
@@ -1034,7 +1035,7 @@ def measure_forest(fo, dev, dist, rank, world, *, leaf=0, builder=0, steps=10, w
     Fd = torch.from_numpy(fo.F).to(dev)
     Qd = torch.from_numpy(fo.Q).to(dev)
     L = fwn.library()
-    tuned, tuning = None, 0
+    tuned = None
     if leaf == 0:  # builder and leaf size picked by the forest autotuner on this forest (untimed)
         r = fwn.autotune_forest(Vd, fo.voff, Fd, fo.foff, Qd, fo.qoff)
         leaf, tuning, builder = rank0_choice(dist, (r["leaf_size"], r["tuning"], r["builder"]), dev)
