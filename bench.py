@@ -1001,8 +1001,8 @@ def run_ours(args, rank, world, local):
 
 
 def run_forest(args, rank, world, local):
-    """Batched workloads: `forest` (512 uneven spheres/tori, seed 3) and `voxel` (4 x 5M-triangle
-    meshes, each on a 256^3 voxel-centre grid). Build: one launch per stage over all meshes.
+    """Batched workloads: `forest` (512 uneven spheres/tori, seed 3; `--meshes` for fewer) and
+    `voxel` (4 x 5M-triangle meshes, each on a 256^3 voxel-centre grid). Build: one launch per stage over all meshes.
     Mixed query: one persistent launch over all meshes, captured in a CUDA graph and replayed.
     Plain form: FP64 everywhere, one launch per mesh."""
     import torch
@@ -1021,6 +1021,8 @@ def run_forest(args, rank, world, local):
                             fp64=not args.no_fp64, clocks=not args.no_clocks,
                             grid=args.workload == "voxel", local=local)
     result["config"]["generation_s"] = gen_s
+    if dist is not None:
+        dist.destroy_process_group()
     return result
 
 
@@ -1238,7 +1240,9 @@ def main():
     if args.impl == "reference":
         run_reference(args, rank, world)
     elif args.workload in ("forest", "voxel"):
-        run_forest(args, rank, world, local)
+        result = run_forest(args, rank, world, local)
+        if rank == 0:
+            print(json.dumps(result), flush=True)
     else:
         run_ours(args, rank, world, local)
 
