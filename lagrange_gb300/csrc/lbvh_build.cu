@@ -944,34 +944,81 @@ __global__ void k_refit_level(int count, const int* __restrict__ nodes,
 // the order, so it equals the serial one bit for bit.
 constexpr int kRadiusChunk = 2048;
 
-// Largest vertex_r2 over slots [s0, s1), one warp: a first pass takes the largest float estimate
-// M of |v - P|^2 over the run (the ScreenedMax bound: an estimate is within 6e-7 of its exact
-// value while no step underflows), a second pass takes the exact FP64 term of the vertices whose
-// estimate reaches M (1 - 1e-5) only (or all of them near float's underflow or overflow). The
-// vertex with the largest exact term always qualifies, so the result is the plain FP64 maximum
-// bit for bit, at a few FP64 terms per run instead of three per triangle.
+// Float estimate of |v - P|^2 (P a float value; every step rounded once, so within 6e-7 of the
+// exact value while no step underflows).
+__device__ __forceinline__ float vertex_est(float x, float y, float z, const float* Pf) {
+    const float dx = x - Pf[0], dy = y - Pf[1], dz = z - Pf[2];
+    return (dx * dx + dy * dy) + dz * dz;
+}
+
+// One lane's share of a one-pass radius screen: the running maximum m of the estimates, and the
+// two largest estimates (with their vertices) among the vertices that came within 1e-5 of the
+// running maximum when they were seen, plus the largest such estimate pushed out of the two. A
+// vertex whose estimate reaches the final threshold M (1 - 1e-5) (M the warp's maximum, at least
+// every running maximum) was within 1e-5 of the running maximum when seen, so it is one of the
+// two or it raised `dropped` to the threshold; in that case (ties, e.g. a node centred on a
+// sphere) the caller makes a second pass over its slots.
+struct LaneTop2 {
+    float m = 0.f;
+    float e0 = -INFINITY, e1 = -INFINITY, dropped = -INFINITY;
+    float x0 = 0.f, y0 = 0.f, z0 = 0.f, x1 = 0.f, y1 = 0.f, z1 = 0.f;
+    __device__ __forceinline__ void add(float x, float y, float z, float e) {
+        if (!(e < m * 0.99999f - 1e-37f)) {
+            if (e > e0) {
+                dropped = fmaxf(dropped, e1);
+                e1 = e0; x1 = x0; y1 = y0; z1 = z0;
+                e0 = e; x0 = x; y0 = y; z0 = z;
+            } else if (e > e1) {
+                dropped = fmaxf(dropped, e1);
+                e1 = e; x1 = x; y1 = y; z1 = z;
+            } else {
+                dropped = fmaxf(dropped, e);
+            }
+        }
+        m = fmaxf(m, e);
+    }
+    __device__ __forceinline__ void add_slot(const TriF32& t, const float* Pf) {
+        const float4 t0 = t.t0, t1 = t.t1, t2 = t.t2;
+        add(t0.x, t0.y, t0.z, vertex_est(t0.x, t0.y, t0.z, Pf));
+        add(t0.w, t1.x, t1.y, vertex_est(t0.w, t1.x, t1.y, Pf));
+        add(t1.z, t1.w, t2.x, vertex_est(t1.z, t1.w, t2.x, Pf));
+    }
+};
+
+// The warp's threshold after a one-pass screen, and whether a second pass is needed (some lane
+// dropped a vertex that reaches it, or the estimates left float's range).
+__device__ __forceinline__ bool top2_threshold(const LaneTop2& t, float& thr) {
+    float m = t.m;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    thr = m * 0.99999f - 1e-37f;
+    return __any_sync(0xffffffffu, !(m < INFINITY) || !(t.dropped < thr));
+}
+
+// Largest vertex_r2 over slots [s0, s1), one warp: a one-pass float screen (LaneTop2), then the
+// exact FP64 term of the vertices whose estimate reaches M (1 - 1e-5) only, M being the largest
+// estimate (a second pass over the slots finds them when the two kept per lane may not hold them
+// all, or near float's underflow or overflow, where every vertex is taken). The vertex with the
+// largest exact term always qualifies, so the result is the plain FP64 maximum bit for bit, at a
+// few FP64 terms per run instead of three per triangle.
 __device__ __forceinline__ double slots_r2(const TriF32* __restrict__ tris, int s0, int s1,
                                            const double* P, int lane) {
     const float Pf[3] = {d2f(P[0]), d2f(P[1]), d2f(P[2])};
-    auto est = [&](float x, float y, float z) {
-        const float dx = x - Pf[0], dy = y - Pf[1], dz = z - Pf[2];
-        return (dx * dx + dy * dy) + dz * dz;
-    };
-    float m = 0.f;
-    for (int s = s0 + lane; s < s1; s += 32) {
-        const float4 t0 = tris[s].t0, t1 = tris[s].t1, t2 = tris[s].t2;
-        m = fmaxf(m, fmaxf(est(t0.x, t0.y, t0.z), fmaxf(est(t0.w, t1.x, t1.y), est(t1.z, t1.w, t2.x))));
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    const bool all = !(m < INFINITY);
-    const float thr = m * 0.99999f - 1e-37f;
+    LaneTop2 t;
+    for (int s = s0 + lane; s < s1; s += 32) t.add_slot(tris[s], Pf);
+    float thr;
     double r2 = 0.0;
-    for (int s = s0 + lane; s < s1; s += 32) {
-        const float4 t0 = tris[s].t0, t1 = tris[s].t1, t2 = tris[s].t2;
-        if (all || est(t0.x, t0.y, t0.z) >= thr) r2 = fmax(r2, vertex_r2(t0.x, t0.y, t0.z, P));
-        if (all || est(t0.w, t1.x, t1.y) >= thr) r2 = fmax(r2, vertex_r2(t0.w, t1.x, t1.y, P));
-        if (all || est(t1.z, t1.w, t2.x) >= thr) r2 = fmax(r2, vertex_r2(t1.z, t1.w, t2.x, P));
+    if (top2_threshold(t, thr)) {
+        const bool all = !(thr < INFINITY);
+        for (int s = s0 + lane; s < s1; s += 32) {
+            const float4 t0 = tris[s].t0, t1 = tris[s].t1, t2 = tris[s].t2;
+            if (all || vertex_est(t0.x, t0.y, t0.z, Pf) >= thr) r2 = fmax(r2, vertex_r2(t0.x, t0.y, t0.z, P));
+            if (all || vertex_est(t0.w, t1.x, t1.y, Pf) >= thr) r2 = fmax(r2, vertex_r2(t0.w, t1.x, t1.y, P));
+            if (all || vertex_est(t1.z, t1.w, t2.x, Pf) >= thr) r2 = fmax(r2, vertex_r2(t1.z, t1.w, t2.x, P));
+        }
+    } else {
+        if (t.e0 >= thr) r2 = vertex_r2(t.x0, t.y0, t.z0, P);
+        if (t.e1 >= thr) r2 = fmax(r2, vertex_r2(t.x1, t.y1, t.z1, P));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) r2 = fmax(r2, __shfl_xor_sync(0xffffffffu, r2, o));
@@ -1011,12 +1058,13 @@ __global__ void k_radius_list(int num_nodes, const uint64_t* __restrict__ keys,
 }
 
 // One warp per listed node (grid-stride), all lanes on its slot run. The float screen runs per
-// node; the vertices that pass it (a few per node) queue in the warp's shared buffer across the
+// node in one pass (LaneTop2; a second pass only on ties); the vertices that pass it (a few per
+// node) queue in the warp's shared buffer across the
 // warp's nodes and get their exact FP64 terms 32 at a time, one per lane, so the FP64 pipe (2
 // operations per SM per cycle on GB300, whatever the number of active lanes) sees full warps;
 // each term goes to its node's maximum by atomicMax on the bit pattern (r2bits starts at 0).
 constexpr int kRadiusWarps = 8;      // warps per block of k_node_radius_small
-constexpr int kRadiusQueue = 128;    // queued vertices per warp (one flush of 32 + 3 x 32 added)
+constexpr int kRadiusQueue = 64;     // queued vertices per warp (< 32 left + 32 added)
 
 struct RadiusQueue {
     float x[kRadiusQueue], y[kRadiusQueue], z[kRadiusQueue];
@@ -1048,25 +1096,44 @@ k_node_radius_small(const int* __restrict__ list, const int* __restrict__ count,
     const int total = *count;
     const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
     int queued = 0;  // warp-uniform
+    // queue one vertex per lane where c holds (a warp-wide step), evaluating full groups of 32
+    auto enqueue = [&](bool c, float x, float y, float z, int node) {
+        const unsigned bal = __ballot_sync(0xffffffffu, c);
+        if (c) {
+            const int k = queued + __popc(bal & lt);
+            q.x[k] = x;
+            q.y[k] = y;
+            q.z[k] = z;
+            q.node[k] = node;
+        }
+        queued += __popc(bal);
+        while (queued >= 32) {  // evaluate 32, move the rest down (each lane its own column)
+            radius_flush(q, 32, stage, r2bits, lane);
+            for (int k = 32 + lane; k < queued; k += 32) {
+                q.x[k - 32] = q.x[k];
+                q.y[k - 32] = q.y[k];
+                q.z[k - 32] = q.z[k];
+                q.node[k - 32] = q.node[k];
+            }
+            __syncwarp();
+            queued -= 32;
+        }  // queued < 32 here: the next step adds at most 32 (< kRadiusQueue)
+    };
     for (int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); w < total; w += nwarps) {
         const int v = list[w];
         const int i = pos[v];
         const int s0 = first[v], s1 = last[v] + 1;
         const float Pf[3] = {d2f(stage[i].P[0]), d2f(stage[i].P[1]), d2f(stage[i].P[2])};
-        auto est = [&](float x, float y, float z) {
-            const float dx = x - Pf[0], dy = y - Pf[1], dz = z - Pf[2];
-            return (dx * dx + dy * dy) + dz * dz;
-        };
-        float m = 0.f;
-        for (int s = s0 + lane; s < s1; s += 32) {
-            const float4 t0 = tris[s].t0, t1 = tris[s].t1, t2 = tris[s].t2;
-            m = fmaxf(m, fmaxf(est(t0.x, t0.y, t0.z), fmaxf(est(t0.w, t1.x, t1.y), est(t1.z, t1.w, t2.x))));
+        LaneTop2 t;
+        for (int s = s0 + lane; s < s1; s += 32) t.add_slot(tris[s], Pf);
+        float thr;
+        if (!top2_threshold(t, thr)) {  // the two kept per lane hold every candidate
+            enqueue(t.e0 >= thr, t.x0, t.y0, t.z0, i);
+            enqueue(t.e1 >= thr, t.x1, t.y1, t.z1, i);
+            continue;
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-        const bool all = !(m < INFINITY);
-        const float thr = m * 0.99999f - 1e-37f;
-        for (int base = s0; base < s1; base += 32) {  // warp-uniform trip count
+        const bool all = !(thr < INFINITY);
+        for (int base = s0; base < s1; base += 32) {  // second pass, warp-uniform trip count
             const int s = base + lane;
             float vx[3] = {0.f, 0.f, 0.f}, vy[3] = {0.f, 0.f, 0.f}, vz[3] = {0.f, 0.f, 0.f};
             if (s < s1) {
@@ -1076,29 +1143,9 @@ k_node_radius_small(const int* __restrict__ list, const int* __restrict__ count,
                 vx[2] = t1.z; vy[2] = t1.w; vz[2] = t2.x;
             }
 #pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                const bool c = s < s1 && (all || est(vx[j], vy[j], vz[j]) >= thr);
-                const unsigned bal = __ballot_sync(0xffffffffu, c);
-                if (c) {
-                    const int k = queued + __popc(bal & lt);
-                    q.x[k] = vx[j];
-                    q.y[k] = vy[j];
-                    q.z[k] = vz[j];
-                    q.node[k] = i;
-                }
-                queued += __popc(bal);
-            }
-            while (queued >= 32) {  // evaluate 32, move the rest down (each lane its own column)
-                radius_flush(q, 32, stage, r2bits, lane);
-                for (int k = 32 + lane; k < queued; k += 32) {
-                    q.x[k - 32] = q.x[k];
-                    q.y[k - 32] = q.y[k];
-                    q.z[k - 32] = q.z[k];
-                    q.node[k - 32] = q.node[k];
-                }
-                __syncwarp();
-                queued -= 32;
-            }  // queued < 32 here, so the next slot block adds at most 96: < kRadiusQueue
+            for (int j = 0; j < 3; ++j)
+                enqueue(s < s1 && (all || vertex_est(vx[j], vy[j], vz[j], Pf) >= thr), vx[j], vy[j],
+                        vz[j], i);
         }
     }
     if (queued > 0) radius_flush(q, queued, stage, r2bits, lane);
