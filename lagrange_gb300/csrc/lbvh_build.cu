@@ -657,23 +657,44 @@ __device__ __forceinline__ double vertex_r2(float x, float y, float z, const dou
     return fmad(dx, dx, fmad(dy, dy, dz * dz));
 }
 
-// Running maximum of vertex_r2 over a stream of vertices, with FP64 only where it can matter:
-// GB300's FP64 rate is a small fraction of FP32, so each vertex first gets a float estimate
-// e = |v - P|^2 (P is a float value; every step rounded once: relative error below 6e-7 while no
-// step underflows) and its exact FP64 term is taken only when e comes within 1e-5 of the
-// largest estimate seen so far (or the estimates are near float's underflow or overflow). The
-// vertex with the largest exact term always passes (its estimate is within 1.2e-6 of every
-// other vertex's or above), so the maximum equals the plain FP64 maximum bit for bit.
-struct ScreenedMax {
-    float m = 0.f;     // largest estimate so far
-    double r2 = 0.0;   // largest exact term among the vertices that passed
-    __device__ __forceinline__ void add(float x, float y, float z, const float* Pf, const double* P) {
-        const float dx = x - Pf[0], dy = y - Pf[1], dz = z - Pf[2];
-        const float e = (dx * dx + dy * dy) + dz * dz;
-        if (!(m < INFINITY) || e >= m * 0.99999f - 1e-37f) {
-            r2 = fmax(r2, vertex_r2(x, y, z, P));
-            m = fmaxf(m, e);
+// Float estimate of |v - P|^2 (P a float value; every step rounded once, so within 6e-7 of the
+// exact value while no step underflows).
+__device__ __forceinline__ float vertex_est(float x, float y, float z, const float* Pf) {
+    const float dx = x - Pf[0], dy = y - Pf[1], dz = z - Pf[2];
+    return (dx * dx + dy * dy) + dz * dz;
+}
+
+// One lane's share of a one-pass radius screen: the running maximum m of the estimates, and the
+// two largest estimates (with their vertices) among the vertices that came within 1e-5 of the
+// running maximum when they were seen, plus the largest such estimate pushed out of the two. A
+// vertex whose estimate reaches the final threshold M (1 - 1e-5) (M the warp's maximum, at least
+// every running maximum) was within 1e-5 of the running maximum when seen, so it is one of the
+// two or it raised `dropped` to the threshold; in that case (ties, e.g. a node centred on a
+// sphere) the caller makes a second pass over its slots.
+struct LaneTop2 {
+    float m = 0.f;
+    float e0 = -INFINITY, e1 = -INFINITY, dropped = -INFINITY;
+    float x0 = 0.f, y0 = 0.f, z0 = 0.f, x1 = 0.f, y1 = 0.f, z1 = 0.f;
+    __device__ __forceinline__ void add(float x, float y, float z, float e) {
+        if (!(e < m * 0.99999f - 1e-37f)) {
+            if (e > e0) {
+                dropped = fmaxf(dropped, e1);
+                e1 = e0; x1 = x0; y1 = y0; z1 = z0;
+                e0 = e; x0 = x; y0 = y; z0 = z;
+            } else if (e > e1) {
+                dropped = fmaxf(dropped, e1);
+                e1 = e; x1 = x; y1 = y; z1 = z;
+            } else {
+                dropped = fmaxf(dropped, e);
+            }
         }
+        m = fmaxf(m, e);
+    }
+    __device__ __forceinline__ void add_slot(const TriF32& t, const float* Pf) {
+        const float4 t0 = t.t0, t1 = t.t1, t2 = t.t2;
+        add(t0.x, t0.y, t0.z, vertex_est(t0.x, t0.y, t0.z, Pf));
+        add(t0.w, t1.x, t1.y, vertex_est(t0.w, t1.x, t1.y, Pf));
+        add(t1.z, t1.w, t2.x, vertex_est(t1.z, t1.w, t2.x, Pf));
     }
 };
 
@@ -741,19 +762,37 @@ __device__ void leaf_moments(const float* __restrict__ V, const int32_t* __restr
         }
         for (int j = 0; j < 3; ++j) R.M1[3 * i + j] = fmad(N[i], e[j], M1[3 * i + j]);
     }
-    ScreenedMax sm;
+    // radius: the leaf's farthest vertex from P, screened in float in one pass (LaneTop2 on this
+    // thread's own vertices), with exact FP64 terms for the one or two candidates kept, or for
+    // every vertex reaching the threshold in a second pass when ties may have pushed one out
     const float Pf[3] = {d2f(P[0]), d2f(P[1]), d2f(P[2])};
-    for (int s = f; s <= l; ++s) {
+    auto vertex_of = [&](int s, int j) {
         const int64_t t = tri_of_slot[s];
         const int m = (int)(keys[s] >> MORTON_BITS);
-        const int64_t vb = voff[m];
+        return V + 3 * (voff[m] + F[3 * t + j]);
+    };
+    LaneTop2 top;
+    for (int s = f; s <= l; ++s)
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-            const float* vp = V + 3 * (vb + F[3 * t + j]);
-            sm.add(vp[0], vp[1], vp[2], Pf, P);
+            const float* vp = vertex_of(s, j);
+            top.add(vp[0], vp[1], vp[2], vertex_est(vp[0], vp[1], vp[2], Pf));
         }
+    const float thr = top.m * 0.99999f - 1e-37f;
+    double r2 = 0.0;
+    if (!(top.m < INFINITY) || !(top.dropped < thr)) {
+        const bool all = !(top.m < INFINITY);
+        for (int s = f; s <= l; ++s)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const float* vp = vertex_of(s, j);
+                if (all || vertex_est(vp[0], vp[1], vp[2], Pf) >= thr)
+                    r2 = fmax(r2, vertex_r2(vp[0], vp[1], vp[2], P));
+            }
+    } else {
+        if (top.e0 >= thr) r2 = vertex_r2(top.x0, top.y0, top.z0, P);
+        if (top.e1 >= thr) r2 = fmax(r2, vertex_r2(top.x1, top.y1, top.z1, P));
     }
-    const double r2 = sm.r2;
     for (int a = 0; a < 3; ++a) {
         R.P[a] = P[a];
         R.N[a] = N[a];
@@ -943,47 +982,6 @@ __global__ void k_refit_level(int count, const int* __restrict__ nodes,
 // on the bit pattern (non-negative doubles order like their bits). A maximum does not depend on
 // the order, so it equals the serial one bit for bit.
 constexpr int kRadiusChunk = 2048;
-
-// Float estimate of |v - P|^2 (P a float value; every step rounded once, so within 6e-7 of the
-// exact value while no step underflows).
-__device__ __forceinline__ float vertex_est(float x, float y, float z, const float* Pf) {
-    const float dx = x - Pf[0], dy = y - Pf[1], dz = z - Pf[2];
-    return (dx * dx + dy * dy) + dz * dz;
-}
-
-// One lane's share of a one-pass radius screen: the running maximum m of the estimates, and the
-// two largest estimates (with their vertices) among the vertices that came within 1e-5 of the
-// running maximum when they were seen, plus the largest such estimate pushed out of the two. A
-// vertex whose estimate reaches the final threshold M (1 - 1e-5) (M the warp's maximum, at least
-// every running maximum) was within 1e-5 of the running maximum when seen, so it is one of the
-// two or it raised `dropped` to the threshold; in that case (ties, e.g. a node centred on a
-// sphere) the caller makes a second pass over its slots.
-struct LaneTop2 {
-    float m = 0.f;
-    float e0 = -INFINITY, e1 = -INFINITY, dropped = -INFINITY;
-    float x0 = 0.f, y0 = 0.f, z0 = 0.f, x1 = 0.f, y1 = 0.f, z1 = 0.f;
-    __device__ __forceinline__ void add(float x, float y, float z, float e) {
-        if (!(e < m * 0.99999f - 1e-37f)) {
-            if (e > e0) {
-                dropped = fmaxf(dropped, e1);
-                e1 = e0; x1 = x0; y1 = y0; z1 = z0;
-                e0 = e; x0 = x; y0 = y; z0 = z;
-            } else if (e > e1) {
-                dropped = fmaxf(dropped, e1);
-                e1 = e; x1 = x; y1 = y; z1 = z;
-            } else {
-                dropped = fmaxf(dropped, e);
-            }
-        }
-        m = fmaxf(m, e);
-    }
-    __device__ __forceinline__ void add_slot(const TriF32& t, const float* Pf) {
-        const float4 t0 = t.t0, t1 = t.t1, t2 = t.t2;
-        add(t0.x, t0.y, t0.z, vertex_est(t0.x, t0.y, t0.z, Pf));
-        add(t0.w, t1.x, t1.y, vertex_est(t0.w, t1.x, t1.y, Pf));
-        add(t1.z, t1.w, t2.x, vertex_est(t1.z, t1.w, t2.x, Pf));
-    }
-};
 
 // The warp's threshold after a one-pass screen, and whether a second pass is needed (some lane
 // dropped a vertex that reaches it, or the estimates left float's range).
