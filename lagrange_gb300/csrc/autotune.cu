@@ -74,6 +74,12 @@ bool cache_lookup(const char* path, const std::string& key, fwn_tune_result* out
         std::memset(&r, 0, sizeof(r));
         if (!(is >> k >> r.leaf_size >> r.traversal >> r.block_size >> r.tuning >> r.builder >> r.ms))
             continue;
+        // an entry a caller could not apply (edited or damaged file) is ignored: tune again
+        if (r.leaf_size < 1 || r.leaf_size > 16 || r.traversal < FWN_TRAVERSAL_AUTO ||
+            r.traversal > FWN_TRAVERSAL_WARP || r.block_size < 0 || r.block_size > 1024 ||
+            r.block_size % 32 != 0 || r.tuning < 0 || r.tuning > 6 ||
+            (r.builder != FWN_BUILDER_LBVH && r.builder != FWN_BUILDER_SPLIT))
+            continue;
         if (k == key) {
             r.from_cache = 1;
             *out = r;

@@ -28,6 +28,11 @@ def test_autotune_choice_and_cache(tmp_path):
     assert r2["from_cache"] == 1 and r2["candidates"] == 0
     assert r2["config"] == r["config"]
     assert len(cache.read_text().splitlines()) == 1
+    # an entry out of range (an edited or damaged file) is ignored and the mesh tuned again
+    key = cache.read_text().split()[0]
+    cache.write_text(f"{key} 99 2 128 17 0 1.0\n")
+    r3 = fwn.autotune(wl.V, wl.F, wl.Q, cache_path=str(cache))
+    assert r3["from_cache"] == 0 and r3["candidates"] == 72 and r3["leaf_size"] in (4, 8, 12, 16)
     # the tuned engine agrees with the plain FP64 form built with the same leaf size
     eng = fwn.FastWindingNumber(wl.V, wl.F, records=fwn.RECORDS_F32 | fwn.RECORDS_F64,
                                 **r["config"])
