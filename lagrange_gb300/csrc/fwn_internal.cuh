@@ -12,6 +12,7 @@
 
 #include <cuda_runtime.h>
 #include <nvtx3/nvToolsExt.h>
+#include <stddef.h>
 #include <stdint.h>
 
 #include <stdexcept>
@@ -99,6 +100,9 @@ struct __align__(32) StageRec {
     double pad;      // 288 B: records start on 32 B sectors, so reads of one record share them
 };
 static_assert(sizeof(StageRec) == 288, "StageRec must be 9 sectors");
+static_assert(offsetof(StageRec, area) == 24 && offsetof(StageRec, N) == 32 &&
+                  offsetof(StageRec, M1) == 56 && offsetof(StageRec, M2) == 128,
+              "the refit reads a record as P, area, N, M1 (128 B) then M2, in 16 B pairs");
 
 // ---------------------------------------------------------------------------------------------
 // Errors

@@ -702,7 +702,7 @@ __device__ void leaf_moments(const float* __restrict__ V, const int32_t* __restr
                              const int64_t* __restrict__ voff, const uint64_t* __restrict__ keys,
                              const uint32_t* __restrict__ tri_of_slot, int f, int l,
                              StageRec& R) {
-    double A = 0.0, S[3] = {0.0, 0.0, 0.0}, Cs[3] = {0.0, 0.0, 0.0}, c0[3] = {0.0, 0.0, 0.0};
+    double A = 0.0, S[3] = {0.0, 0.0, 0.0}, c0[3] = {0.0, 0.0, 0.0};
     double N[3] = {0.0, 0.0, 0.0}, M1[9], M2[18];
     for (int i = 0; i < 9; ++i) M1[i] = 0.0;
     for (int i = 0; i < 18; ++i) M2[i] = 0.0;
@@ -727,7 +727,6 @@ __device__ void leaf_moments(const float* __restrict__ V, const int32_t* __restr
             for (int a = 0; a < 3; ++a) c0[a] = c[a];
         for (int a = 0; a < 3; ++a) {
             S[a] = fmad(a_t, c[a], S[a]);
-            Cs[a] = Cs[a] + c[a];
             d[a] = c[a] - c0[a];
         }
         A = A + a_t;
@@ -746,6 +745,15 @@ __device__ void leaf_moments(const float* __restrict__ V, const int32_t* __restr
             for (int q = 0; q < 6; ++q) M2[6 * i + q] = fmad(nn[i], Q[q], M2[6 * i + q]);
         }
     }
+    // a leaf of zero area is centred at the plain mean of its centroids (Cs / count); that sum is
+    // only needed then, so it is formed in a second pass, with the same additions in the same order
+    double Cs[3] = {0.0, 0.0, 0.0};
+    if (!(A > 0.0))
+        for (int s = f; s <= l; ++s) {
+            double v[3][3];
+            load_tri_d(V, F, voff[(int)(keys[s] >> MORTON_BITS)], tri_of_slot[s], v);
+            for (int a = 0; a < 3; ++a) Cs[a] = Cs[a] + ((v[0][a] + v[1][a]) + v[2][a]) * kThird;
+        }
     const double cnt = (double)(l - f + 1);
     double P[3], e[3];
     for (int a = 0; a < 3; ++a) {
@@ -806,27 +814,35 @@ __device__ void leaf_moments(const float* __restrict__ V, const int32_t* __restr
 // threads of the same launch wrote them; otherwise plain cached loads (an earlier launch wrote
 // them), so the fields of one record share its L1 sectors.
 template <bool CG>
-__device__ __forceinline__ double ld_rec(const double* p) {
-    if constexpr (CG) return __ldcg(p);
-    else return *p;
+__device__ __forceinline__ double2 ld_rec2(const double* p) {  // p 16 B aligned
+    const double2* q = reinterpret_cast<const double2*>(p);
+    if constexpr (CG) return __ldcg(q);
+    else return *q;
 }
 
 template <bool CG>
 __device__ void combine_moments(const StageRec* __restrict__ a_, const StageRec* __restrict__ b_,
                                 StageRec& R) {
-    auto ldcg_d = [](const double* p) { return ld_rec<CG>(p); };
-    double Pa[3], Pb[3], Na[3], Nb[3], M1a[9], M1b[9];
-    const double Aa = ldcg_d(&a_->area), Ab = ldcg_d(&b_->area);
-    for (int i = 0; i < 3; ++i) {
-        Pa[i] = ldcg_d(&a_->P[i]);
-        Pb[i] = ldcg_d(&b_->P[i]);
-        Na[i] = ldcg_d(&a_->N[i]);
-        Nb[i] = ldcg_d(&b_->N[i]);
+    // a record as doubles: P[0..2], area, N[0..2], M1[0..8] (the first 128 B), then M2[0..17];
+    // records are 32 B aligned, so every even index starts a 16 B pair
+    const double* ra = reinterpret_cast<const double*>(a_);
+    const double* rb = reinterpret_cast<const double*>(b_);
+    double ha[16], hb[16];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        const double2 x = ld_rec2<CG>(ra + 2 * k), y = ld_rec2<CG>(rb + 2 * k);
+        ha[2 * k] = x.x;
+        ha[2 * k + 1] = x.y;
+        hb[2 * k] = y.x;
+        hb[2 * k + 1] = y.y;
     }
-    for (int i = 0; i < 9; ++i) {
-        M1a[i] = ldcg_d(&a_->M1[i]);
-        M1b[i] = ldcg_d(&b_->M1[i]);
-    }
+    const double* Pa = ha;
+    const double* Pb = hb;
+    const double Aa = ha[3], Ab = hb[3];
+    const double* Na = ha + 4;
+    const double* Nb = hb + 4;
+    const double* M1a = ha + 7;
+    const double* M1b = hb + 7;
     const double A = Aa + Ab;
     double P[3], ea[3], eb[3];
     for (int i = 0; i < 3; ++i) {
@@ -843,15 +859,21 @@ __device__ void combine_moments(const StageRec* __restrict__ a_, const StageRec*
     }
     const int SJ[6] = {0, 1, 2, 0, 0, 1};
     const int SK[6] = {0, 1, 2, 1, 2, 2};
+#pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
-        for (int q = 0; q < 6; ++q) {
-            const int j = SJ[q], k = SK[q];
-            const double ta = fmad(Na[i], ea[j] * ea[k],
-                                   fmad(M1a[3 * i + k], ea[j], fmad(M1a[3 * i + j], ea[k], ldcg_d(&a_->M2[6 * i + q]))));
-            const double tb = fmad(Nb[i], eb[j] * eb[k],
-                                   fmad(M1b[3 * i + k], eb[j], fmad(M1b[3 * i + j], eb[k], ldcg_d(&b_->M2[6 * i + q]))));
-            R.M2[6 * i + q] = ta + tb;
+        for (int q = 0; q < 6; q += 2) {
+            const double2 ma = ld_rec2<CG>(ra + 16 + 6 * i + q), mb = ld_rec2<CG>(rb + 16 + 6 * i + q);
+            const double m2a[2] = {ma.x, ma.y}, m2b[2] = {mb.x, mb.y};
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int j = SJ[q + h], k = SK[q + h];
+                const double ta = fmad(Na[i], ea[j] * ea[k],
+                                       fmad(M1a[3 * i + k], ea[j], fmad(M1a[3 * i + j], ea[k], m2a[h])));
+                const double tb = fmad(Nb[i], eb[j] * eb[k],
+                                       fmad(M1b[3 * i + k], eb[j], fmad(M1b[3 * i + j], eb[k], m2b[h])));
+                R.M2[6 * i + q + h] = ta + tb;
+            }
         }
     R.area = A;
     R.r = 0.0;  // exact radius about P from the node's vertices: k_node_radius, after the refit
@@ -954,7 +976,7 @@ __global__ void k_leaf_sort(int nl, const int* __restrict__ leaves, const int* _
 
 // The internal nodes of one level of a split tree (nodes[0 .. count)): each combines its two
 // children, whose records the leaf pass or the previous (deeper) level wrote.
-__global__ void k_refit_level(int count, const int* __restrict__ nodes,
+__global__ void __launch_bounds__(128, 4) k_refit_level(int count, const int* __restrict__ nodes,
                               const int* __restrict__ left, const int* __restrict__ right,
                               const int* __restrict__ pos, StageRec* __restrict__ stage,
                               unsigned* __restrict__ status) {
