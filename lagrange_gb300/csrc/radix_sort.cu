@@ -281,16 +281,29 @@ __device__ __forceinline__ int block_scan_1024(int v, int* wt, int* total) {
     return res;
 }
 
+static_assert(SCAN_IPT == 4, "a thread's items are one int4");
+
+// A thread's SCAN_IPT consecutive items: one 16 B load where the run is whole and aligned.
+__device__ __forceinline__ void load_items(const int* __restrict__ data, int64_t i0, int64_t n,
+                                           int (&v)[SCAN_IPT]) {
+    if (i0 + SCAN_IPT <= n && (reinterpret_cast<uintptr_t>(data + i0) & 15) == 0) {
+        const int4 x = *reinterpret_cast<const int4*>(data + i0);
+        v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+    } else {
+#pragma unroll
+        for (int j = 0; j < SCAN_IPT; ++j) v[j] = i0 + j < n ? data[i0 + j] : 0;
+    }
+}
+
 __global__ void __launch_bounds__(SCAN_THREADS)
 k_scan_tile_sums(const int* __restrict__ data, int64_t n, int* __restrict__ sums) {
     __shared__ int wt[32];
     const int64_t base = (int64_t)blockIdx.x * SCAN_TILE;
+    int v[SCAN_IPT];
+    load_items(data, base + (int64_t)threadIdx.x * SCAN_IPT, n, v);
     int s = 0;
 #pragma unroll
-    for (int j = 0; j < SCAN_IPT; ++j) {
-        int64_t i = base + (int64_t)threadIdx.x * SCAN_IPT + j;
-        if (i < n) s += data[i];
-    }
+    for (int j = 0; j < SCAN_IPT; ++j) s += v[j];
     int total;
     block_scan_1024(s, wt, &total);
     if (threadIdx.x == 0) sums[blockIdx.x] = total;
@@ -313,21 +326,26 @@ __global__ void __launch_bounds__(SCAN_THREADS)
 k_scan_tiles(int* __restrict__ data, int64_t n, const int* __restrict__ sums) {
     __shared__ int wt[32];
     const int64_t base = (int64_t)blockIdx.x * SCAN_TILE;
+    const int64_t i0 = base + (int64_t)threadIdx.x * SCAN_IPT;
     int v[SCAN_IPT];
+    load_items(data, i0, n, v);
     int s = 0;
 #pragma unroll
-    for (int j = 0; j < SCAN_IPT; ++j) {
-        int64_t i = base + (int64_t)threadIdx.x * SCAN_IPT + j;
-        v[j] = i < n ? data[i] : 0;
-        s += v[j];
-    }
+    for (int j = 0; j < SCAN_IPT; ++j) s += v[j];
     int total;
     int ex = block_scan_1024(s, wt, &total) + sums[blockIdx.x];
+    int o[SCAN_IPT];
 #pragma unroll
     for (int j = 0; j < SCAN_IPT; ++j) {
-        int64_t i = base + (int64_t)threadIdx.x * SCAN_IPT + j;
-        if (i < n) data[i] = ex;
+        o[j] = ex;
         ex += v[j];
+    }
+    if (i0 + SCAN_IPT <= n && (reinterpret_cast<uintptr_t>(data + i0) & 15) == 0) {
+        *reinterpret_cast<int4*>(data + i0) = make_int4(o[0], o[1], o[2], o[3]);
+    } else {
+#pragma unroll
+        for (int j = 0; j < SCAN_IPT; ++j)
+            if (i0 + j < n) data[i0 + j] = o[j];
     }
 }
 
