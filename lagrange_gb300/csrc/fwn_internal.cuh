@@ -153,7 +153,7 @@ struct NvtxRange {
 // returns freed memory to the driver at every synchronisation, so a host-synchronous call would
 // map all of its scratch again on every call.) During stream capture the allocation goes to the
 // default pool instead, so that it becomes a graph memory node. Freed with cudaFreeAsync.
-constexpr uint64_t kScratchRetainBytes = uint64_t(8) << 30;
+constexpr uint64_t kScratchRetainBytes = uint64_t(16) << 30;
 void* scratch_alloc(size_t bytes, cudaStream_t stream);
 
 struct Scratch {

@@ -235,6 +235,21 @@ __device__ __forceinline__ bool is_big(const uint64_t* keys, const int* first, c
 }
 
 // ---- K3b: collapse + DFS layout ---------------------------------------------------------------
+// Position in a list for the lanes where `pred` holds: one atomicAdd per warp on the list's
+// counter (a single counter bumped by every thread serialises at L2). Every active lane of the
+// warp calls it at the same point; the order within the list is immaterial to its users.
+__device__ __forceinline__ int warp_append(int* __restrict__ counter, bool pred) {
+    const unsigned mask = __activemask();
+    const unsigned bal = __ballot_sync(mask, pred);
+    if (!bal) return -1;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(bal) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(counter, __popc(bal));
+    base = __shfl_sync(mask, base, leader);
+    return pred ? base + __popc(bal & ((1u << lane) - 1u)) : -1;
+}
+
 // flags: bit0 emitted, bit1 leaf
 __global__ void k_emit_count(int n, int K, const uint64_t* __restrict__ keys,
                              const int* __restrict__ parent, const int* __restrict__ first,
@@ -250,8 +265,8 @@ __global__ void k_emit_count(int n, int K, const uint64_t* __restrict__ keys,
     if (emitted) atomicAdd(&cnt_first[first[u]], 1);
     // emitted leaves (never a node spanning meshes: such a node is "big") feed the refit, one
     // thread each; the list order does not matter (each node's arithmetic is fixed)
-    if (emitted && leaf && !is_cross(keys, first, last, u))
-        leaf_list[atomicAdd(leaf_list_len, 1)] = u;
+    const int at = warp_append(leaf_list_len, emitted && leaf && !is_cross(keys, first, last, u));
+    if (at >= 0) leaf_list[at] = u;
 }
 
 __global__ void k_positions(int num_nodes, const int* __restrict__ parent,
@@ -512,9 +527,8 @@ __global__ void k_split_children(int nact, int node_base, int K, const int* __re
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
         const int cb = c == 0 ? b : mid, ce = c == 0 ? mid : e;
-        int k = -1;
-        if (ce - cb > K) {
-            k = atomicAdd(next_count, 1);
+        const int k = warp_append(next_count, ce - cb > K);
+        if (k >= 0) {
             n_start[k] = cb;
             n_end[k] = ce;
             n_node[k] = node_base + 2 * sg + c;
@@ -574,7 +588,8 @@ __global__ void k_split_emit(int num_nodes, const int* __restrict__ nfirst,
     const bool leaf = nleft[u] < 0;
     flags[u] = (uint8_t)(1 | (leaf ? 2 : 0));
     atomicAdd(&cnt_first[nfirst[u]], 1);
-    if (leaf) leaf_list[atomicAdd(leaf_list_len, 1)] = u;
+    const int at = warp_append(leaf_list_len, leaf);
+    if (at >= 0) leaf_list[at] = u;
 }
 
 __global__ void k_split_mesh_roots(int nmeshes, const int* __restrict__ root_node,
@@ -1073,8 +1088,9 @@ __global__ void k_radius_list(int num_nodes, const uint64_t* __restrict__ keys,
                               int* __restrict__ count) {
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= num_nodes) return;
-    if (internal_emitted(keys, first, last, flags, u) && last[u] - first[u] + 1 <= kRadiusChunk)
-        list[atomicAdd(count, 1)] = u;
+    const int at = warp_append(count, internal_emitted(keys, first, last, flags, u) &&
+                                          last[u] - first[u] + 1 <= kRadiusChunk);
+    if (at >= 0) list[at] = u;
 }
 
 // One warp per listed node (grid-stride), all lanes on its slot run. The float screen runs per
@@ -1253,7 +1269,7 @@ __global__ void k_convert(int num_nodes, const uint64_t* __restrict__ keys, cons
     const bool leaf = (fl & 2) && !cross;
     const int tb = first[u];
     const int tc = leaf ? (last[u] - first[u] + 1) : 0;
-    if (leaf) atomicAdd(leaf_count, 1);
+    warp_append(leaf_count, leaf);  // counts the leaves (one atomic per warp)
     Coeffs c;
     StageRec R;
     if (!cross) {
@@ -1337,10 +1353,12 @@ __global__ void k_tri_records(int n, const uint32_t* __restrict__ tri_of_slot,
     sorted_tri[s] = (int)t;
 }
 
+// Build temporaries come from the library's stream-ordered pool, which keeps freed memory mapped
+// across synchronisations (up to kScratchRetainBytes): a rebuild, or the next mesh of a batch,
+// reuses it instead of mapping gigabytes of new pages (the device's default pool returns freed
+// memory at every synchronisation).
 template <class T> T* dalloc(size_t count, cudaStream_t s) {
-    void* p = nullptr;
-    if (count) FWN_CUDA_CHECK(cudaMallocAsync(&p, count * sizeof(T), s));
-    return static_cast<T*>(p);
+    return count ? static_cast<T*>(scratch_alloc(count * sizeof(T), s)) : nullptr;
 }
 
 inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
