@@ -1394,7 +1394,7 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
                                    cudaMemcpyHostToDevice, st));
     FWN_CUDA_CHECK(cudaMemcpyAsync(foff, foff_h, (nmeshes + 1) * sizeof(int64_t),
                                    cudaMemcpyHostToDevice, st));
-    e.meshes = static_cast<MeshInfo*>(scratch_alloc(nmeshes * sizeof(MeshInfo), st));
+    FWN_CUDA_CHECK(cudaMalloc(&e.meshes, nmeshes * sizeof(MeshInfo)));
     e.meshes_h = new MeshInfo[nmeshes];
     unsigned* enc = dalloc<unsigned>(6 * nmeshes, st);
     unsigned* status = dalloc<unsigned>(1, st);
@@ -1658,10 +1658,8 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
             k_refit_level<<<grid_for(it->second, 128), 128, 0, st>>>(
                 it->second, int_nodes + it->first, left, right, pos, stage, status);
         FWN_CUDA_CHECK(cudaGetLastError());
-        // the engine's own arrays come from the library's pool too (freed with the engine): a
-        // rebuild reuses their pages instead of mapping them again
-        e.tris = static_cast<TriF32*>(scratch_alloc((size_t)n * sizeof(TriF32), st));
-        e.sorted_tri = static_cast<int*>(scratch_alloc((size_t)n * sizeof(int), st));
+        FWN_CUDA_CHECK(cudaMalloc(&e.tris, (size_t)n * sizeof(TriF32)));
+        FWN_CUDA_CHECK(cudaMalloc(&e.sorted_tri, (size_t)n * sizeof(int)));
         k_tri_records<<<grid_for(n, 256), 256, 0, st>>>(n, tri_of_slot, keys, d_V, d_F, voff,
                                                         e.tris, e.sorted_tri);
         // exact radii of the internal nodes from the triangle records: one warp per node of at
@@ -1688,10 +1686,8 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
                                                    e.tris, r2bits);
         }
         FWN_CUDA_CHECK(cudaGetLastError());
-        if (e.cfg.records & FWN_RECORDS_F32)
-            e.nodes32 = static_cast<NodeF32*>(scratch_alloc(E * sizeof(NodeF32), st));
-        if (e.cfg.records & FWN_RECORDS_F64)
-            e.nodes64 = static_cast<NodeF64*>(scratch_alloc(E * sizeof(NodeF64), st));
+        if (e.cfg.records & FWN_RECORDS_F32) FWN_CUDA_CHECK(cudaMalloc(&e.nodes32, E * sizeof(NodeF32)));
+        if (e.cfg.records & FWN_RECORDS_F64) FWN_CUDA_CHECK(cudaMalloc(&e.nodes64, E * sizeof(NodeF64)));
         k_convert<<<grid_for(num_nodes, 128), 128, 0, st>>>(num_nodes, keys, first, last, flags, pos,
                                                             skip, stage, r2bits, e.nodes32,
                                                             e.nodes64, leaf_count);
