@@ -1635,6 +1635,10 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
         StageRec* stage = dalloc<StageRec>(E, st);
         if (!(e.cfg.records & FWN_RECORDS_MOMENTS)) track(stage);
         else e.stage = stage;
+        // the refit reads the records in 16 B pairs: the pool's allocations are 256 B aligned,
+        // and a build that got less stops here rather than launch misaligned vector loads
+        if (reinterpret_cast<uintptr_t>(stage) % alignof(StageRec) != 0)
+            throw Error(FWN_INTERNAL, "staging records are not 32 B aligned");
         FWN_CUDA_CHECK(cudaMemsetAsync(visit, 0, (size_t)nint * sizeof(int), st));
         FWN_CUDA_CHECK(cudaMemsetAsync(leaf_count, 0, sizeof(int), st));
         if (NL > 0) {
