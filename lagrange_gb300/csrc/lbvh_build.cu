@@ -10,8 +10,13 @@
 //       positions + escape ("skip") links with one scan:  pos(v) = base[first(v)] + rank(v),
 //       skip(v) = base[last(v)+1], where base = exclusive scan of #emitted nodes per first leaf
 //       and rank(v) = #ancestors sharing first(v)
-//   K4  bottom-up FP64 refit of order-0/1/2 moments (atomic-counter ascent; the second child to
-//       arrive combines), then conversion to 128 B FP32 / 256 B FP64 records in DFS order
+//   K4  bottom-up FP64 refit of order-0/1/2 moments: leaves grouped by triangle count, one
+//       thread each; parents by recentring children (LBVH: atomic-counter ascent, the second
+//       child to arrive combines; split tree: level by level over dense per-level lists)
+//   K4a exact node radii (farthest vertex, float screen + FP64 terms for the candidates), then
+//       conversion to 128 B FP32 / 256 B FP64 records in DFS order
+// The alternative top-down builder (FWN_BUILDER_SPLIT) replaces K1-K3b with level-synchronous
+// midpoint splits of each segment's centroid box and shares K4-K4a.
 //
 // This translation unit is compiled with -fmad=false: every floating-point operation is
 // individually rounded, in the order written, so the CPU restatement of the same build
