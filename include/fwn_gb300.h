@@ -102,7 +102,10 @@ typedef struct fwn_config {
                               register cap. 1: 1 query per lane, 72 registers; 2: 1, no cap;
                               3: 1, 64 registers; 4: 2 queries per lane, 64 registers; 5: 2, 80;
                               6: as 4 with both query slots' Taylor terms in paired f32x2
-                              arithmetic (same results bit for bit).
+                              arithmetic (same results bit for bit); 7: as 6 reading the node
+                              records from a structure-of-arrays copy (eight float4 arrays,
+                              128 B more per node) that a build with tuning 7 keeps: the layout
+                              comparison, one mesh's point queries only (grids and forests run 6).
                               0 (default): 4 for batches that fill the GPU, else 3 */
     int32_t builder;       /* FWN_BUILDER_*. Default FWN_BUILDER_LBVH */
     int32_t reserved[5];

@@ -90,6 +90,7 @@ Engine::~Engine() {
                       cudaSetDevice(device) == cudaSuccess;
     if (nodes32) cudaFree(nodes32);
     if (nodes64) cudaFree(nodes64);
+    if (soa) cudaFree(soa);
     if (tris) cudaFree(tris);
     if (sorted_tri) cudaFree(sorted_tri);
     if (meshes) cudaFree(meshes);
@@ -198,7 +199,7 @@ void validate_config(const fwn_config& c) {
         throw Error(FWN_INVALID_ARG, "fp64_near_scale must be finite and >= 0");
     if (!(c.fp64_cond >= 0.f) || !std::isfinite(c.fp64_cond))
         throw Error(FWN_INVALID_ARG, "fp64_cond must be finite and >= 0");
-    if (c.tuning < 0 || c.tuning > 6) throw Error(FWN_INVALID_ARG, "tuning must be in [0, 6]");
+    if (c.tuning < 0 || c.tuning > 7) throw Error(FWN_INVALID_ARG, "tuning must be in [0, 7]");
     if (c.builder != FWN_BUILDER_LBVH && c.builder != FWN_BUILDER_SPLIT)
         throw Error(FWN_INVALID_ARG, "builder must be FWN_BUILDER_LBVH or FWN_BUILDER_SPLIT");
 }

@@ -197,6 +197,7 @@ struct Engine {
     int64_t num_nodes = 0, num_leaves = 0;
     NodeF32* nodes32 = nullptr;
     NodeF64* nodes64 = nullptr;
+    float4* soa = nullptr;         // the FP32 records as 8 float4 arrays (tuning 7 builds only)
     TriF32* tris = nullptr;
     int* sorted_tri = nullptr;     // original triangle id per leaf slot
     MeshInfo* meshes = nullptr;    // device

@@ -1323,6 +1323,17 @@ __global__ void k_convert(int num_nodes, const uint64_t* __restrict__ keys, cons
     }
 }
 
+// Structure-of-arrays copy of the FP32 records (tuning variant 7): float4 k of node i goes to
+// soa[k * num_nodes + i].
+__global__ void k_aos_to_soa(int64_t num_nodes, const NodeF32* __restrict__ n32,
+                             float4* __restrict__ soa) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= num_nodes) return;
+    const float4* r = reinterpret_cast<const float4*>(n32 + i);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) soa[k * num_nodes + i] = r[k];
+}
+
 __global__ void k_tri_records(int n, const uint32_t* __restrict__ tri_of_slot,
                               const uint64_t* __restrict__ keys, const float* __restrict__ V,
                               const int32_t* __restrict__ F, const int64_t* __restrict__ voff,
@@ -1701,6 +1712,11 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
                                                             skip, stage, r2bits, e.nodes32,
                                                             e.nodes64, leaf_count);
         FWN_CUDA_CHECK(cudaGetLastError());
+        if (e.cfg.tuning == 7 && e.nodes32 && E > 0) {  // the structure-of-arrays layout variant
+            FWN_CUDA_CHECK(cudaMalloc(&e.soa, (size_t)E * sizeof(NodeF32)));
+            k_aos_to_soa<<<grid_for(E, 256), 256, 0, st>>>(E, e.nodes32, e.soa);
+            FWN_CUDA_CHECK(cudaGetLastError());
+        }
         int lc = 0;
         FWN_CUDA_CHECK(cudaMemcpyAsync(&lc, leaf_count, sizeof(int), cudaMemcpyDeviceToHost, st));
         FWN_CUDA_CHECK(cudaMemcpyAsync(&st_h, status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
@@ -1718,6 +1734,7 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
     cudaEventDestroy(ev0);
     cudaEventDestroy(ev1);
     e.device_bytes = (int64_t)e.num_nodes * ((e.nodes32 ? sizeof(NodeF32) : 0) +
+                                             (e.soa ? sizeof(NodeF32) : 0) +
                                              (e.nodes64 ? sizeof(NodeF64) : 0) +
                                              (e.stage ? sizeof(StageRec) : 0)) +
                      (int64_t)nf * (sizeof(TriF32) + sizeof(int)) + nmeshes * sizeof(MeshInfo);

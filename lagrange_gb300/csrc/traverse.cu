@@ -486,12 +486,27 @@ struct WarpSmem {
 // UEND: every slot of the warp walks the same subtree, ending at uend (one mesh: its subtree is
 // the whole node range, and no skip link points past it), so a finished slot's resume index is
 // uend itself and the per-slot end test drops out of every step.
-template <bool STATS, int QPL, bool PAIRED = false, bool UEND = false>
+// SOA: the node records as eight float4 arrays of num_nodes entries each (soa[k * stride + i]:
+// k = 0 the test sector's (P, r), 1 its (skip, tri_begin, tri_count, trM1), 2-7 the coefficient
+// float4s) instead of one 128 B record per node: the structure-of-arrays layout, kept as tuning
+// variant 7 for the layout comparison.
+template <bool STATS, int QPL, bool PAIRED = false, bool UEND = false, bool SOA = false>
 __device__ __forceinline__ void warp_walk(const NodeF32* __restrict__ nodes,
                                           const TriF32* __restrict__ tris, Slot (&sl)[QPL],
                                           float cond, float beta, WarpSmem<QPL>& sm,
                                           QCounters& qc, unsigned* __restrict__ status,
-                                          int uend = DONE) {
+                                          int uend = DONE, const float4* __restrict__ soa = nullptr,
+                                          int64_t stride = 0) {
+    auto sector0 = [&](int i, float4& a, int4& b) {
+        if constexpr (SOA) {
+            a = __ldg(soa + i);
+            const float4 h = __ldg(soa + stride + i);
+            b = make_int4(__float_as_int(h.x), __float_as_int(h.y), __float_as_int(h.z),
+                          __float_as_int(h.w));
+        } else {
+            load_sector0(nodes + i, a, b);
+        }
+    };
     const int lane = threadIdx.x & 31;
     const unsigned lt = lanemask_lt();
     const int stop = UEND ? uend : DONE;
@@ -504,13 +519,19 @@ __device__ __forceinline__ void warp_walk(const NodeF32* __restrict__ nodes,
     int cursor = __reduce_min_sync(0xffffffffu, lo);
     float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
     int4 b = make_int4(0, 0, 0, 0);
-    if (cursor != stop) load_sector0(nodes + cursor, a, b);
+    if (cursor != stop) sector0(cursor, a, b);
     while (cursor != stop) {
-        const NodeF32* nd = nodes + cursor;
         float4 m0, m1, m2, m3, m4, m5;
-        ld_v8(&nd->m0, m0, m1);
-        ld_v8(&nd->m2, m2, m3);
-        ld_v8(&nd->m4, m4, m5);
+        if constexpr (SOA) {
+            const float4* c = soa + 2 * stride + cursor;
+            m0 = __ldg(c); m1 = __ldg(c + stride); m2 = __ldg(c + 2 * stride);
+            m3 = __ldg(c + 3 * stride); m4 = __ldg(c + 4 * stride); m5 = __ldg(c + 5 * stride);
+        } else {
+            const NodeF32* nd = nodes + cursor;
+            ld_v8(&nd->m0, m0, m1);
+            ld_v8(&nd->m2, m2, m3);
+            ld_v8(&nd->m4, m4, m5);
+        }
         // far test of every slot on every lane (only slots whose resume index is the cursor use
         // the result), with no divergent branch around it and the resume update as selects
         const bool leafnode = b.z > 0;
@@ -534,7 +555,7 @@ __device__ __forceinline__ void warp_walk(const NodeF32* __restrict__ nodes,
         const int nc = __reduce_min_sync(0xffffffffu, lo2);
         float4 an = a;
         int4 bn = b;
-        if (nc != stop) load_sector0(nodes + nc, an, bn);  // next step's test sector, in flight
+        if (nc != stop) sector0(nc, an, bn);  // next step's test sector, in flight
         if constexpr (PAIRED && QPL == 2) {
             // both slots' Taylor terms in one paired evaluation when any lane of either is far
             if (__any_sync(0xffffffffu, do_far[0] || do_far[1])) {
@@ -628,13 +649,14 @@ __device__ __forceinline__ void write_result(const Slot& s, int64_t qi, float* _
 // One mesh: each warp takes the next 32 * QPL queries of the (sorted) order. With sorted_omega
 // the results go, coalesced, to position k of the sorted order (k_scatter_results then writes
 // them to the callers' indices in one pass); otherwise to the callers' indices directly.
-template <bool STATS, int MINB, int QPL, bool PAIRED = false>
+template <bool STATS, int MINB, int QPL, bool PAIRED = false, bool SOA = false>
 __global__ void __launch_bounds__(WARP_BLOCK, MINB)
 k_query_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
              const MeshInfo mi, const float* __restrict__ Q, const uint32_t* __restrict__ order,
              int64_t n, float beta, float* __restrict__ omega, uint8_t* __restrict__ inside,
              float* __restrict__ sorted_omega, unsigned* __restrict__ status,
-             unsigned long long* __restrict__ stats) {
+             unsigned long long* __restrict__ stats, const float4* __restrict__ soa,
+             int64_t soa_stride) {
     __shared__ WarpSmem<QPL> smem[WARP_BLOCK / 32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t base = ((int64_t)blockIdx.x * (WARP_BLOCK / 32) + w) * (32 * QPL);
@@ -655,8 +677,8 @@ k_query_warp(const NodeF32* __restrict__ nodes, const TriF32* __restrict__ tris,
         sl[j].resume = valid ? mi.root : DONE;
         sl[j].end = mi.end;
     }
-    warp_walk<STATS, QPL, PAIRED, true>(nodes, tris, sl, mi.cond, beta, smem[w], qc, status,
-                                         mi.end);
+    warp_walk<STATS, QPL, PAIRED, true, SOA>(nodes, tris, sl, mi.cond, beta, smem[w], qc, status,
+                                              mi.end, soa, soa_stride);
 #pragma unroll
     for (int j = 0; j < QPL; ++j) {
         if (qi[j] < 0) continue;
@@ -1025,14 +1047,17 @@ int warp_variant(int tuning, int64_t n) {
     return n >= 4 * wave ? 4 : 3;
 }
 
-template <int MINB, int QPL, bool PAIRED = false>
+template <int MINB, int QPL, bool PAIRED = false, bool SOA = false>
 void launch_query_warp(const Engine& e, const MeshInfo& mi, const float* d_points,
                        const uint32_t* order, int64_t n, float beta, float* d_omega,
                        uint8_t* d_inside, float* sorted_omega, unsigned* d_status,
                        cudaStream_t st) {
-    k_query_warp<false, MINB, QPL, PAIRED><<<grid_for(n, WARP_BLOCK * QPL), WARP_BLOCK, 0, st>>>(
+    if (SOA && !e.soa && e.num_nodes > 0)
+        throw Error(FWN_INVALID_ARG, "tuning 7 (structure-of-arrays records) needs an engine built "
+                                     "with tuning 7");
+    k_query_warp<false, MINB, QPL, PAIRED, SOA><<<grid_for(n, WARP_BLOCK * QPL), WARP_BLOCK, 0, st>>>(
         e.nodes32, e.tris, mi, d_points, order, n, beta, d_omega, d_inside, sorted_omega,
-        d_status, nullptr);
+        d_status, nullptr, e.soa, e.num_nodes);
 }
 
 // The warp walk of one mesh's queries. With a sort order and a free n-float buffer
@@ -1049,6 +1074,7 @@ void launch_query_warp_variant(int variant, const Engine& e, const MeshInfo& mi,
         case 4: launch_query_warp<8, 2>(e, mi, d_points, order, n, beta, d_omega, d_inside, so, d_status, st); break;
         case 5: launch_query_warp<6, 2>(e, mi, d_points, order, n, beta, d_omega, d_inside, so, d_status, st); break;
         case 6: launch_query_warp<8, 2, true>(e, mi, d_points, order, n, beta, d_omega, d_inside, so, d_status, st); break;
+        case 7: launch_query_warp<8, 2, true, true>(e, mi, d_points, order, n, beta, d_omega, d_inside, so, d_status, st); break;
         default: launch_query_warp<8, 1>(e, mi, d_points, order, n, beta, d_omega, d_inside, so, d_status, st); break;
     }
     if (so) k_scatter_results<<<grid_for(n, 256), 256, 0, st>>>(so, order, n, d_omega, d_inside);
@@ -1072,7 +1098,7 @@ QueryArgs resolve_query_args(const Engine& e, const fwn_query_opts* o) {
         if (o->beta > 0.f) a.beta = o->beta;
         if (o->tuning > 0) a.tuning = o->tuning;
     }
-    if (a.tuning < 0 || a.tuning > 6) throw Error(FWN_INVALID_ARG, "tuning must be in [0, 6]");
+    if (a.tuning < 0 || a.tuning > 7) throw Error(FWN_INVALID_ARG, "tuning must be in [0, 7]");
     if (a.precision != FWN_PRECISION_MIXED && a.precision != FWN_PRECISION_FP64)
         throw Error(FWN_INVALID_ARG, "unknown precision");
     // AUTO: the warp walk for the mixed form; for the FP64 form the plain thread-per-query walk
@@ -1156,9 +1182,9 @@ void query_mesh(const Engine& e, int mesh, const QueryArgs& a, const float* d_po
     } else if (a.traversal == FWN_TRAVERSAL_WARP) {
         if (want_stats) {  // counters: no register cap, the variant's queries per lane
             if (warp_variant(a.tuning, n) >= 4)
-                k_query_warp<true, 1, 2><<<grid_for(n, WARP_BLOCK * 2), WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, nullptr, d_status, d_stats);
+                k_query_warp<true, 1, 2><<<grid_for(n, WARP_BLOCK * 2), WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, nullptr, d_status, d_stats, nullptr, 0);
             else
-                k_query_warp<true, 1, 1><<<grid_for(n, WARP_BLOCK), WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, nullptr, d_status, d_stats);
+                k_query_warp<true, 1, 1><<<grid_for(n, WARP_BLOCK), WARP_BLOCK, 0, st>>>(e.nodes32, e.tris, mi, d_points, order, n, a.beta, d_omega, d_inside, nullptr, d_status, d_stats, nullptr, 0);
         } else
             launch_query_warp_variant(warp_variant(a.tuning, n), e, mi, d_points, order, n, a.beta,
                                       d_omega, d_inside, d_status, st, sorted_omega);
@@ -1202,7 +1228,8 @@ void query_grid(const Engine& e, int mesh, const QueryArgs& a, const float origi
     if (!e.nodes32) throw Error(FWN_INVALID_ARG, "engine was built without FP32 records (FWN_RECORDS_F32)");
     // schedule variants as in the point query (warp_variant); two voxels per lane stack two
     // 4 x 4 x 2 layers in one brick
-    const int v = warp_variant(a.tuning, nx * ny * nz);
+    // (variant 7, the structure-of-arrays records, exists for one mesh's point walk: grids run 6)
+    const int v = std::min(warp_variant(a.tuning, nx * ny * nz), 6);
     const int qpl = v >= 4 ? 2 : 1;
     const int64_t bx = (nx + 3) / 4, by = (ny + 3) / 4, bz = (nz + 2 * qpl - 1) / (2 * qpl);
     const int64_t nbricks = bx * by * bz;
@@ -1287,7 +1314,8 @@ void query_forest(const Engine& e, const QueryArgs& a, const float* d_points,
     FWN_CUDA_CHECK(cudaGetDevice(&dev));
     FWN_CUDA_CHECK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     // schedule variants as in the point query (warp_variant)
-    const int v = warp_variant(a.tuning, n);
+    // (variant 7, the structure-of-arrays records, exists for one mesh's point walk: forests run 6)
+    const int v = std::min(warp_variant(a.tuning, n), 6);
     const int qpl = v >= 4 ? 2 : 1;
     auto kern = v == 1 ? k_forest_warp<7, 1> : v == 2 ? k_forest_warp<1, 1> : v == 4 ? k_forest_warp<8, 2>
               : v == 5 ? k_forest_warp<6, 2> : v == 6 ? k_forest_warp<8, 2, true> : k_forest_warp<8, 1>;

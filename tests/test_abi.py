@@ -55,7 +55,7 @@ def test_invalid_arguments_rejected_on_host(engine_lib):
     for field, val, frag in (("beta", 0.0, "beta"), ("leaf_size", 17, "leaf_size"),
                              ("leaf_size", 0, "leaf_size"), ("records", 4, "records"),
                              ("block_size", 48, "block_size"), ("precision", 7, "precision"),
-                             ("fp64_near_scale", -1.0, "fp64_near_scale"), ("tuning", 7, "tuning"),
+                             ("fp64_near_scale", -1.0, "fp64_near_scale"), ("tuning", 8, "tuning"),
                              ("tuning", -1, "tuning"), ("fp64_cond", -1.0, "fp64_cond"),
                              ("builder", 2, "builder")):
         cfg = fwn.config_default(**{field: val})

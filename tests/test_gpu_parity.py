@@ -471,15 +471,15 @@ def test_non_finite_queries(torch_cuda):
 
 
 def test_warp_schedule_variants_agree(torch_cuda):
-    """Every warp-schedule variant (1-6: one or two queries per lane, register caps, paired
-    f32x2 Taylor terms) computes the same terms in the same order with explicit roundings: the
-    results equal variant 3's bit for bit (and the FP64 form's within 2e-6). The allocation-free
-    entry point follows the handle's variant too."""
+    """Every warp-schedule variant (1-7: one or two queries per lane, register caps, paired
+    f32x2 Taylor terms, structure-of-arrays records) computes the same terms in the same order
+    with explicit roundings: the results equal variant 3's bit for bit (and the FP64 form's
+    within 2e-6). The allocation-free entry point follows the handle's variant too."""
     torch = torch_cuda
     wl = W.displaced_icosphere_workload(nu=40, n_queries=50_000)
     Q = torch.from_numpy(wl.Q).cuda()
     ref = None
-    for tuning in (3, 1, 2, 4, 5, 6):
+    for tuning in (3, 1, 2, 4, 5, 6, 7):
         eng = _engine(wl.V, wl.F, tuning=tuning)
         w, ins = _q(eng, torch, wl.Q)
         if ref is None:
