@@ -337,14 +337,16 @@ FWN_API fwn_status fwn_forest_query(fwn_handle h, const float* d_points,
 FWN_API fwn_status fwn_save(fwn_handle h, const char* path);
 
 /* Reads an engine written by fwn_save onto the current device (the FP64 staging moments kept for
- * fwn_export_moments are not saved). The header, the sizes, the checksum and every node's skip
- * link and triangle range are checked before any device work: a foreign, truncated or corrupt
- * file returns FWN_INVALID_ARG. Queries on the loaded engine equal those on the saved one.
+ * fwn_export_moments, and the structure-of-arrays copy of tuning 7, are not saved). The header,
+ * the sizes, the configuration (the checks of a build), the checksum and every node's skip link
+ * and triangle range are checked before any device work: a foreign, truncated or corrupt file
+ * returns FWN_INVALID_ARG. Queries on the loaded engine equal those on the saved one.
  * Synchronous. */
 FWN_API fwn_status fwn_load(const char* path, fwn_handle* out);
 
 /* No counterpart in the reference (a diagnostic). Usage of the library's per-device pool of
- * stream-ordered query scratch (zeros if no call has used the pool on `device` yet): bytes the
+ * stream-ordered scratch, which serves queries and builds and keeps up to 16 GB of freed memory
+ * mapped (zeros if no call has used the pool on `device` yet): bytes the
  * pool holds from the driver, bytes handed out, and the high-water mark of handed-out bytes since
  * the last reset (reset_high != 0 restarts it from the current value before reading). Any output
  * may be NULL. Host-side; no device work. */
