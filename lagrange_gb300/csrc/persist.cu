@@ -192,6 +192,7 @@ extern "C" FWN_API fwn_status fwn_load(const char* path, fwn_handle* out) {
         fwn_config cfg = hd.cfg;
         cfg.records = (hd.has32 ? FWN_RECORDS_F32 : 0) | (hd.has64 ? FWN_RECORDS_F64 : 0);
         validate_config(cfg);
+        if (cfg.tuning == 7) cfg.tuning = 6;  // no structure-of-arrays copy: the same walk on the records
         Fnv sum;
         std::vector<MeshInfo> meshes((size_t)M);
         std::vector<NodeF32> n32(hd.has32 ? (size_t)E : 0);
