@@ -579,6 +579,8 @@ def batched_summary(dev, *, steps=5, warmup=3, cpu=True, voxel=False):
     if "e2e" in r:
         out["e2e"] = {k: r["e2e"][k] for k in ("value", "unit", "ms_per_step", "h2d_bytes_per_step",
                                                 "d2h_bytes_per_step", "api")}
+        ph = r["e2e"].get("phases_ms_each") or {}
+        out["e2e"]["phases_ms_mean"] = {k: sum(v) / len(v) for k, v in ph.items() if v}
     return out
 
 

@@ -345,8 +345,9 @@ FWN_API fwn_status fwn_save(fwn_handle h, const char* path);
 FWN_API fwn_status fwn_load(const char* path, fwn_handle* out);
 
 /* No counterpart in the reference (a diagnostic). Usage of the library's per-device pool of
- * stream-ordered scratch, which serves queries and builds and keeps up to 16 GB of freed memory
- * mapped (zeros if no call has used the pool on `device` yet): bytes the
+ * stream-ordered query scratch, which keeps up to 8 GB of freed memory mapped (build temporaries
+ * use a second pool, not reported here; zeros if no call has used the pool on `device` yet):
+ * bytes the
  * pool holds from the driver, bytes handed out, and the high-water mark of handed-out bytes since
  * the last reset (reset_high != 0 restarts it from the current value before reading). Any output
  * may be NULL. Host-side; no device work. */

@@ -20,31 +20,49 @@ void set_last_error(const std::string& m) { g_last_error = m; }
 namespace {
 constexpr int kMaxDevices = 64;
 std::mutex g_pool_mutex;
-cudaMemPool_t g_pools[kMaxDevices] = {};  // created on first use, kept for the process lifetime
+// two pools per device, created on first use and kept for the process lifetime: one for query
+// scratch, one for build temporaries, so that the gigabytes a large build frees (in block sizes
+// of its own) never stand in for a query's scratch and push the query pool over its threshold
+cudaMemPool_t g_pools[2][kMaxDevices] = {};
+constexpr uint64_t kRetain[2] = {kScratchRetainBytes, kBuildRetainBytes};
 
-cudaMemPool_t scratch_pool(int dev) {
+cudaMemPool_t scratch_pool(int dev, int kind) {
     if (dev < 0 || dev >= kMaxDevices) throw Error(FWN_INTERNAL, "device ordinal out of range");
     std::lock_guard<std::mutex> lock(g_pool_mutex);
-    if (!g_pools[dev]) {
+    if (!g_pools[kind][dev]) {
         cudaMemPoolProps props = {};
         props.allocType = cudaMemAllocationTypePinned;
         props.location.type = cudaMemLocationTypeDevice;
         props.location.id = dev;
         cudaMemPool_t pool = nullptr;
         FWN_CUDA_CHECK(cudaMemPoolCreate(&pool, &props));
-        uint64_t keep = kScratchRetainBytes;
+        uint64_t keep = kRetain[kind];
         const cudaError_t err = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
         if (err != cudaSuccess) {
             cudaMemPoolDestroy(pool);
             FWN_CUDA_CHECK(err);
         }
-        g_pools[dev] = pool;
+        g_pools[kind][dev] = pool;
     }
-    return g_pools[dev];
+    return g_pools[kind][dev];
+}
+
+void* pool_alloc(size_t bytes, cudaStream_t st, int kind) {
+    void* p = nullptr;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    FWN_CUDA_CHECK(cudaStreamIsCapturing(st, &cs));
+    if (cs != cudaStreamCaptureStatusNone) {
+        FWN_CUDA_CHECK(cudaMallocAsync(&p, bytes, st));
+        return p;
+    }
+    int dev = 0;
+    FWN_CUDA_CHECK(cudaGetDevice(&dev));
+    FWN_CUDA_CHECK(cudaMallocFromPoolAsync(&p, bytes, scratch_pool(dev, kind), st));
+    return p;
 }
 }  // namespace
 
-// Usage of the scratch pool of `dev` (zeros when no call has created it yet); reset_high
+// Usage of the query scratch pool of `dev` (zeros when no call has created it yet); reset_high
 // restarts the high-water mark of used bytes from the current value.
 void scratch_pool_stats(int dev, bool reset_high, uint64_t* reserved, uint64_t* used,
                         uint64_t* used_high) {
@@ -52,7 +70,7 @@ void scratch_pool_stats(int dev, bool reset_high, uint64_t* reserved, uint64_t* 
     cudaMemPool_t pool = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_pool_mutex);
-        pool = g_pools[dev];
+        pool = g_pools[0][dev];
     }
     uint64_t r = 0, u = 0, h = 0;
     if (pool) {
@@ -69,19 +87,9 @@ void scratch_pool_stats(int dev, bool reset_high, uint64_t* reserved, uint64_t* 
     if (used_high) *used_high = h;
 }
 
-void* scratch_alloc(size_t bytes, cudaStream_t st) {
-    void* p = nullptr;
-    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    FWN_CUDA_CHECK(cudaStreamIsCapturing(st, &cs));
-    if (cs != cudaStreamCaptureStatusNone) {
-        FWN_CUDA_CHECK(cudaMallocAsync(&p, bytes, st));
-        return p;
-    }
-    int dev = 0;
-    FWN_CUDA_CHECK(cudaGetDevice(&dev));
-    FWN_CUDA_CHECK(cudaMallocFromPoolAsync(&p, bytes, scratch_pool(dev), st));
-    return p;
-}
+void* scratch_alloc(size_t bytes, cudaStream_t st) { return pool_alloc(bytes, st, 0); }
+
+void* build_alloc(size_t bytes, cudaStream_t st) { return pool_alloc(bytes, st, 1); }
 
 Engine::~Engine() {
     // free on the engine's device, then give the caller back its current device

@@ -153,8 +153,12 @@ struct NvtxRange {
 // returns freed memory to the driver at every synchronisation, so a host-synchronous call would
 // map all of its scratch again on every call.) During stream capture the allocation goes to the
 // default pool instead, so that it becomes a graph memory node. Freed with cudaFreeAsync.
-constexpr uint64_t kScratchRetainBytes = uint64_t(16) << 30;
+constexpr uint64_t kScratchRetainBytes = uint64_t(8) << 30;
 void* scratch_alloc(size_t bytes, cudaStream_t stream);
+// Build temporaries come from a second pool of the same kind, which keeps up to
+// kBuildRetainBytes mapped for the next build (a 42M-triangle forest's are ~10 GB).
+constexpr uint64_t kBuildRetainBytes = uint64_t(12) << 30;
+void* build_alloc(size_t bytes, cudaStream_t stream);
 
 struct Scratch {
     void* p = nullptr;

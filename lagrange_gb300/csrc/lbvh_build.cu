@@ -1369,12 +1369,12 @@ __global__ void k_tri_records(int n, const uint32_t* __restrict__ tri_of_slot,
     sorted_tri[s] = (int)t;
 }
 
-// Build temporaries come from the library's stream-ordered pool, which keeps freed memory mapped
-// across synchronisations (up to kScratchRetainBytes): a rebuild, or the next mesh of a batch,
-// reuses it instead of mapping gigabytes of new pages (the device's default pool returns freed
-// memory at every synchronisation).
+// Build temporaries come from the library's build pool, which keeps freed memory mapped across
+// synchronisations (up to kBuildRetainBytes): a rebuild, or the next mesh of a batch, reuses it
+// instead of mapping gigabytes of new pages (the device's default pool returns freed memory at
+// every synchronisation).
 template <class T> T* dalloc(size_t count, cudaStream_t s) {
-    return count ? static_cast<T*>(scratch_alloc(count * sizeof(T), s)) : nullptr;
+    return count ? static_cast<T*>(build_alloc(count * sizeof(T), s)) : nullptr;
 }
 
 inline unsigned grid_for(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
