@@ -56,6 +56,26 @@ def test_gather_sharded_round_trip():
         shard.gather_sharded(order, parts[:2], n)
 
 
+def test_forest_shard_and_gather_with_empty_meshes():
+    """Meshes without triangles or without queries (and more ranks than meshes with work) are
+    assigned and gathered like any other: every query lands back at its own offset."""
+    foff = np.array([0, 10, 10, 40, 40, 41, 100], np.int64)       # meshes 1 and 3 empty
+    voff = np.array([0, 12, 12, 50, 50, 53, 130], np.int64)
+    qoff = np.array([0, 5, 9, 9, 12, 12, 30], np.int64)            # meshes 2 and 4 no queries
+    vals = np.arange(qoff[-1], dtype=np.float64) * 1.5
+    for world in (1, 2, 4, 9):
+        shards = [shard.forest_shard(voff, foff, qoff, r, world) for r in range(world)]
+        assigned = sorted(m for sh in shards for m in sh[0])
+        assert assigned == list(range(len(foff) - 1))
+        parts = []
+        for meshes, vr, fr, qr, svoff, sfoff, sqoff in shards:
+            assert len(svoff) == len(meshes) + 1 and svoff[-1] == sum(e - s for s, e in vr)
+            assert sfoff[-1] == sum(e - s for s, e in fr) and sqoff[-1] == sum(e - s for s, e in qr)
+            parts.append(np.concatenate([vals[s:e] for s, e in qr]) if qr else np.zeros(0))
+        np.testing.assert_array_equal(shard.gather_forest(qoff, [sh[3] for sh in shards], parts),
+                                      vals)
+
+
 def _morton_order(P):
     """A spatially coherent order of the points (Morton code on a 1024^3 grid): stands in for the
     device's Hilbert order, which every rank computes the same way."""
