@@ -176,3 +176,11 @@ def test_load_checks_payload_before_device_work(engine_lib, tmp_path):
         st, msg = status(_engine_file(tmp_path / f"c{i}.fwn", **kw))
         assert st == 1 and what in msg and not h.value, (kw, msg)
 
+
+
+def test_cpp_class_compiles_and_links(engine_lib):
+    """The header-only C++ class (the drop-in surface of lagrange::winding::FastWindingNumber)
+    compiles with -Wall and links against the library; running it needs a GPU (test_cpp_class)."""
+    from lagrange_gb300 import build
+    exe = build.build_cpp_test()
+    assert exe.exists() and exe.stat().st_size > 0
