@@ -130,7 +130,7 @@ enum : unsigned {
     ST_BAD_INDEX = 1u,       // triangle index out of [0, nv)
     ST_NONFINITE = 2u,       // referenced vertex coordinate is NaN/inf
     ST_BAD_LINK = 4u,        // traversal met a skip link that does not advance
-    ST_REFIT_ORPHAN = 8u     // refit ascent inconsistency
+    ST_REFIT_ORPHAN = 8u     // refit inconsistency (missing child or parent)
 };
 
 // ---------------------------------------------------------------------------------------------

@@ -11,8 +11,8 @@
 //       skip(v) = base[last(v)+1], where base = exclusive scan of #emitted nodes per first leaf
 //       and rank(v) = #ancestors sharing first(v)
 //   K4  bottom-up FP64 refit of order-0/1/2 moments: leaves grouped by triangle count, one
-//       thread each; parents by recentring children (LBVH: atomic-counter ascent, the second
-//       child to arrive combines; split tree: level by level over dense per-level lists)
+//       thread each; parents by recentring children, level by level over dense lists (split
+//       tree: its levels; LBVH: node heights from an integer atomic-counter ascent)
 //   K4a exact node radii (farthest vertex, float screen + FP64 terms for the candidates), then
 //       conversion to 128 B FP32 / 256 B FP64 records in DFS order
 // The alternative top-down builder (FWN_BUILDER_SPLIT) replaces K1-K3b with level-synchronous
@@ -830,17 +830,12 @@ __device__ void leaf_moments(const float* __restrict__ V, const int32_t* __restr
     R.pad = 0.0;
 }
 
-// Children's records: CG = read through L2 (ld.global.cg), for the atomic ascent, where other
-// threads of the same launch wrote them; otherwise plain cached loads (an earlier launch wrote
-// them), so the fields of one record share its L1 sectors.
-template <bool CG>
+// Children's records: plain cached loads (an earlier launch wrote them), so the fields of one
+// record share its L1 sectors.
 __device__ __forceinline__ double2 ld_rec2(const double* p) {  // p 16 B aligned
-    const double2* q = reinterpret_cast<const double2*>(p);
-    if constexpr (CG) return __ldcg(q);
-    else return *q;
+    return *reinterpret_cast<const double2*>(p);
 }
 
-template <bool CG>
 __device__ void combine_moments(const StageRec* __restrict__ a_, const StageRec* __restrict__ b_,
                                 StageRec& R) {
     // a record as doubles: P[0..2], area, N[0..2], M1[0..8] (the first 128 B), then M2[0..17];
@@ -850,7 +845,7 @@ __device__ void combine_moments(const StageRec* __restrict__ a_, const StageRec*
     double ha[16], hb[16];
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
-        const double2 x = ld_rec2<CG>(ra + 2 * k), y = ld_rec2<CG>(rb + 2 * k);
+        const double2 x = ld_rec2(ra + 2 * k), y = ld_rec2(rb + 2 * k);
         ha[2 * k] = x.x;
         ha[2 * k + 1] = x.y;
         hb[2 * k] = y.x;
@@ -883,7 +878,7 @@ __device__ void combine_moments(const StageRec* __restrict__ a_, const StageRec*
     for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int q = 0; q < 6; q += 2) {
-            const double2 ma = ld_rec2<CG>(ra + 16 + 6 * i + q), mb = ld_rec2<CG>(rb + 16 + 6 * i + q);
+            const double2 ma = ld_rec2(ra + 16 + 6 * i + q), mb = ld_rec2(rb + 16 + 6 * i + q);
             const double m2a[2] = {ma.x, ma.y}, m2b[2] = {mb.x, mb.y};
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
@@ -901,51 +896,22 @@ __device__ void combine_moments(const StageRec* __restrict__ a_, const StageRec*
 }
 
 __device__ __forceinline__ void store_rec(StageRec* dst, const StageRec& R) {
-    // plain stores: they reach L2 before the __threadfence of the ascent
-    *dst = R;
+    *dst = R;  // read by a later launch (k_refit_level)
 }
 
+// The leaf pass: one emitted leaf per thread (k_refit_level then combines the internal nodes).
 __global__ void k_refit(int num_leaves, const int* __restrict__ leaf_list,
-                        const uint64_t* __restrict__ keys,
-                        const int* __restrict__ parent, const int* __restrict__ first,
-                        const int* __restrict__ last, const int* __restrict__ left,
-                        const int* __restrict__ right, const int* __restrict__ pos,
+                        const uint64_t* __restrict__ keys, const int* __restrict__ first,
+                        const int* __restrict__ last, const int* __restrict__ pos,
                         const uint32_t* __restrict__ tri_of_slot, const float* __restrict__ V,
                         const int32_t* __restrict__ F, const int64_t* __restrict__ voff,
-                        StageRec* __restrict__ stage, int* __restrict__ visit,
-                        unsigned* __restrict__ status, bool multi_root, bool ascend) {
+                        StageRec* __restrict__ stage) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= num_leaves) return;
-    const int e = leaf_list[k];  // one emitted leaf per thread
+    const int e = leaf_list[k];
     StageRec R;
     leaf_moments(V, F, voff, keys, tri_of_slot, first[e], last[e], R);
     store_rec(&stage[pos[e]], R);
-    if (!ascend) return;  // the internal nodes follow level by level (k_refit_level)
-    int v = e;
-    int guard = 0;
-    while (v != 0) {
-        const int p = parent[v];
-        if (p < 0) {  // a mesh root of a split tree; in the LBVH only node 0 has no parent
-            if (!multi_root) atomicOr(status, ST_REFIT_ORPHAN);
-            return;
-        }
-        if (is_cross(keys, first, last, p)) break;  // v is a mesh root
-        __threadfence();
-        if (atomicAdd(&visit[p], 1) == 0) return;  // first arrival: the sibling continues
-        __threadfence();
-        const int pl = pos[left[p]], pr = pos[right[p]];
-        if (pl < 0 || pr < 0) {
-            atomicOr(status, ST_REFIT_ORPHAN);
-            return;
-        }
-        combine_moments<true>(&stage[pl], &stage[pr], R);
-        store_rec(&stage[pos[p]], R);
-        v = p;
-        if (++guard > 4 * 64 + 64) {  // depth is bounded by key bits + index bits
-            atomicOr(status, ST_REFIT_ORPHAN);
-            return;
-        }
-    }
 }
 
 // The refit's leaf list grouped by triangle count (a counting sort over 1..16), so that the 32
@@ -994,8 +960,9 @@ __global__ void k_leaf_sort(int nl, const int* __restrict__ leaves, const int* _
     sorted[base + __popc(peers & ((1u << (threadIdx.x & 31)) - 1u))] = u;
 }
 
-// The internal nodes of one level of a split tree (nodes[0 .. count)): each combines its two
-// children, whose records the leaf pass or the previous (deeper) level wrote.
+// The internal nodes of one level of a split tree, or of one height of the LBVH
+// (nodes[0 .. count)): each combines its two children, whose records the leaf pass or an
+// earlier (deeper, or lower) list wrote.
 __global__ void __launch_bounds__(128, 4) k_refit_level(int count, const int* __restrict__ nodes,
                               const int* __restrict__ left, const int* __restrict__ right,
                               const int* __restrict__ pos, StageRec* __restrict__ stage,
@@ -1009,8 +976,88 @@ __global__ void __launch_bounds__(128, 4) k_refit_level(int count, const int* __
         return;
     }
     StageRec R;
-    combine_moments<false>(&stage[pos[l]], &stage[pos[r]], R);
+    combine_moments(&stage[pos[l]], &stage[pos[r]], R);
     store_rec(&stage[pos[p]], R);
+}
+
+// LBVH: the height of every emitted internal node (a leaf is 0, a node one more than its taller
+// child), by an integer ascent from the emitted leaves (the second child to arrive continues);
+// the FP64 combine then runs height by height over dense lists (k_refit_level), like the split
+// tree's levels, instead of on the ascent's ever sparser warps.
+constexpr int kMaxHeight = 4 * 64 + 64;  // key bits + index bits bound the depth
+
+__global__ void k_heights(int num_leaves, const int* __restrict__ leaf_list,
+                          const uint64_t* __restrict__ keys, const int* __restrict__ parent,
+                          const int* __restrict__ first, const int* __restrict__ last,
+                          int* __restrict__ visit, int* __restrict__ height,
+                          unsigned* __restrict__ status) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= num_leaves) return;
+    int v = leaf_list[k], h = 0;
+    for (int guard = 0; v != 0; ++guard) {
+        const int p = parent[v];
+        if (p < 0) {  // in the LBVH only node 0 has no parent
+            atomicOr(status, ST_REFIT_ORPHAN);
+            return;
+        }
+        if (is_cross(keys, first, last, p)) return;  // v is a mesh root
+        if (guard >= kMaxHeight - 1) {
+            atomicOr(status, ST_REFIT_ORPHAN);
+            return;
+        }
+        atomicMax(&height[p], h + 1);
+        __threadfence();
+        if (atomicAdd(&visit[p], 1) == 0) return;  // first arrival: the sibling continues
+        __threadfence();
+        h = atomicAdd(&height[p], 0);  // both children's contributions are in
+        v = p;
+    }
+}
+
+// Counting sort of the emitted internal nodes (not spanning meshes) by height: hist[h] counts,
+// then (after an exclusive scan) list[offset[h] + rank] = node.
+__device__ __forceinline__ bool refit_internal(const uint64_t* __restrict__ keys,
+                                               const int* __restrict__ first,
+                                               const int* __restrict__ last,
+                                               const uint8_t* __restrict__ flags, int u) {
+    const uint8_t fl = flags[u];
+    return (fl & 1) && !(fl & 2) && !is_cross(keys, first, last, u);
+}
+
+__global__ void k_height_hist(int nint, const uint64_t* __restrict__ keys,
+                              const int* __restrict__ first, const int* __restrict__ last,
+                              const uint8_t* __restrict__ flags, const int* __restrict__ height,
+                              int* __restrict__ hist) {
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= nint || !refit_internal(keys, first, last, flags, u)) return;
+    const int h = min(max(height[u], 0), kMaxHeight - 1);
+    const unsigned peers = __match_any_sync(__activemask(), h);
+    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&hist[h], __popc(peers));
+}
+
+__global__ void k_height_offsets(int* __restrict__ hist) {  // one thread: exclusive scan in place
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int acc = 0;
+    for (int i = 0; i < kMaxHeight; ++i) {
+        const int c = hist[i];
+        hist[i] = acc;
+        acc += c;
+    }
+}
+
+__global__ void k_height_sort(int nint, const uint64_t* __restrict__ keys,
+                              const int* __restrict__ first, const int* __restrict__ last,
+                              const uint8_t* __restrict__ flags, const int* __restrict__ height,
+                              int* __restrict__ offset, int* __restrict__ list) {
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= nint || !refit_internal(keys, first, last, flags, u)) return;
+    const int h = min(max(height[u], 0), kMaxHeight - 1);
+    const unsigned peers = __match_any_sync(__activemask(), h);
+    const int leader = __ffs(peers) - 1;
+    int base = 0;
+    if ((int)(threadIdx.x & 31) == leader) base = atomicAdd(&offset[h], __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    list[base + __popc(peers & ((1u << (threadIdx.x & 31)) - 1u))] = u;
 }
 
 // ---- K4a: exact node radii ------------------------------------------------------------------------
@@ -1259,17 +1306,26 @@ __device__ void derive_coeffs(const StageRec& R, Coeffs& c) {
     for (int i = 0; i < 10; ++i) c.D[i] = 7.5 * mono[i];
 }
 
-__global__ void k_convert(int num_nodes, const uint64_t* __restrict__ keys, const int* __restrict__ first,
+// The emitted node at each DFS position (node_of_pos[pos[u]] = u), so that the conversion runs
+// one thread per record: the LBVH's emitted nodes are scattered among its 2n - 1 Karras nodes,
+// and a thread per Karras node leaves the FP64 work of the conversion on sparse warps.
+__global__ void k_node_of_pos(int num_nodes, const uint8_t* __restrict__ flags,
+                              const int* __restrict__ pos, int* __restrict__ node_of_pos) {
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u < num_nodes && (flags[u] & 1)) node_of_pos[pos[u]] = u;
+}
+
+__global__ void k_convert(int num_records, const int* __restrict__ node_of_pos,
+                          const uint64_t* __restrict__ keys, const int* __restrict__ first,
                           const int* __restrict__ last, const uint8_t* __restrict__ flags,
-                          const int* __restrict__ pos, const int* __restrict__ skip,
+                          const int* __restrict__ skip,
                           StageRec* __restrict__ stage, const unsigned long long* __restrict__ r2bits,
                           NodeF32* __restrict__ n32, NodeF64* __restrict__ n64,
                           int* __restrict__ leaf_count) {
-    const int u = blockIdx.x * blockDim.x + threadIdx.x;
-    if (u >= num_nodes) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= num_records) return;
+    const int u = node_of_pos[i];
     const uint8_t fl = flags[u];
-    if (!(fl & 1)) return;
-    const int i = pos[u];
     const bool cross = is_cross(keys, first, last, u);
     const bool leaf = (fl & 2) && !cross;
     const int tb = first[u];
@@ -1668,11 +1724,36 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
             leaf_list = leaf_sorted;
         }
         if (NL > 0)
-            k_refit<<<grid_for(NL, 128), 128, 0, st>>>(NL, leaf_list, keys, parent, first, last, left,
-                                                       right, pos, tri_of_slot, d_V, d_F, voff,
-                                                       stage, visit, status, split, !split);
+            k_refit<<<grid_for(NL, 128), 128, 0, st>>>(NL, leaf_list, keys, first, last, pos,
+                                                       tri_of_slot, d_V, d_F, voff, stage);
+        if (!split && NL > 0 && n > 1) {
+            // LBVH: internal nodes height by height (k_heights, then a counting sort)
+            int* height = (int*)track(dalloc<int>(nint, st));
+            int* hist = (int*)track(dalloc<int>(kMaxHeight, st));
+            int* hlist = (int*)track(dalloc<int>(nint, st));
+            FWN_CUDA_CHECK(cudaMemsetAsync(height, 0, (size_t)nint * sizeof(int), st));
+            FWN_CUDA_CHECK(cudaMemsetAsync(hist, 0, kMaxHeight * sizeof(int), st));
+            k_heights<<<grid_for(NL, 128), 128, 0, st>>>(NL, leaf_list, keys, parent, first, last,
+                                                         visit, height, status);
+            k_height_hist<<<grid_for(nint, 256), 256, 0, st>>>(nint, keys, first, last, flags,
+                                                               height, hist);
+            std::vector<int> h_hist(kMaxHeight);
+            FWN_CUDA_CHECK(cudaMemcpyAsync(h_hist.data(), hist, kMaxHeight * sizeof(int),
+                                           cudaMemcpyDeviceToHost, st));
+            k_height_offsets<<<1, 32, 0, st>>>(hist);
+            k_height_sort<<<grid_for(nint, 256), 256, 0, st>>>(nint, keys, first, last, flags,
+                                                               height, hist, hlist);
+            FWN_CUDA_CHECK(cudaStreamSynchronize(st));
+            int off = 0;
+            for (int h = 0; h < kMaxHeight; ++h) {
+                if (h >= 1 && h_hist[h] > 0)
+                    k_refit_level<<<grid_for(h_hist[h], 128), 128, 0, st>>>(
+                        h_hist[h], hlist + off, left, right, pos, stage, status);
+                off += h_hist[h];
+            }
+        }
         // split tree: the internal nodes level by level, deepest first (a node's children are
-        // one level below it), one thread per node of a dense list; the atomic ascent leaves
+        // one level below it), one thread per node of a dense list; an atomic ascent would leave
         // most lanes of its warps idle on GB300's narrow FP64 pipe
         for (auto it = split_levels.rbegin(); it != split_levels.rend(); ++it)
             k_refit_level<<<grid_for(it->second, 128), 128, 0, st>>>(
@@ -1708,9 +1789,11 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
         FWN_CUDA_CHECK(cudaGetLastError());
         if (e.cfg.records & FWN_RECORDS_F32) FWN_CUDA_CHECK(cudaMalloc(&e.nodes32, E * sizeof(NodeF32)));
         if (e.cfg.records & FWN_RECORDS_F64) FWN_CUDA_CHECK(cudaMalloc(&e.nodes64, E * sizeof(NodeF64)));
-        k_convert<<<grid_for(num_nodes, 128), 128, 0, st>>>(num_nodes, keys, first, last, flags, pos,
-                                                            skip, stage, r2bits, e.nodes32,
-                                                            e.nodes64, leaf_count);
+        int* node_of_pos = (int*)track(dalloc<int>(E, st));
+        k_node_of_pos<<<grid_for(num_nodes, 256), 256, 0, st>>>(num_nodes, flags, pos, node_of_pos);
+        k_convert<<<grid_for(E, 128), 128, 0, st>>>(E, node_of_pos, keys, first, last, flags, skip,
+                                                    stage, r2bits, e.nodes32, e.nodes64,
+                                                    leaf_count);
         FWN_CUDA_CHECK(cudaGetLastError());
         if (e.cfg.tuning == 7 && e.nodes32 && E > 0) {  // the structure-of-arrays layout variant
             FWN_CUDA_CHECK(cudaMalloc(&e.soa, (size_t)E * sizeof(NodeF32)));
@@ -1722,7 +1805,7 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
         FWN_CUDA_CHECK(cudaMemcpyAsync(&st_h, status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
         FWN_CUDA_CHECK(cudaStreamSynchronize(st));
         e.num_leaves = lc;
-        if (st_h & ST_REFIT_ORPHAN) throw Error(FWN_INTERNAL, "refit ascent found an inconsistent tree");
+        if (st_h & ST_REFIT_ORPHAN) throw Error(FWN_INTERNAL, "refit found an inconsistent tree");
     }
     FWN_CUDA_CHECK(cudaEventRecord(ev1, st));
     FWN_CUDA_CHECK(cudaMemcpyAsync(e.meshes_h, e.meshes, nmeshes * sizeof(MeshInfo),
