@@ -130,7 +130,8 @@ enum : unsigned {
     ST_BAD_INDEX = 1u,       // triangle index out of [0, nv)
     ST_NONFINITE = 2u,       // referenced vertex coordinate is NaN/inf
     ST_BAD_LINK = 4u,        // traversal met a skip link that does not advance
-    ST_REFIT_ORPHAN = 8u     // refit inconsistency (missing child or parent)
+    ST_REFIT_ORPHAN = 8u,    // refit inconsistency (missing child or parent)
+    ST_BUILD_BOUND = 16u     // a split build passed its node or depth bound
 };
 
 // ---------------------------------------------------------------------------------------------

@@ -333,6 +333,10 @@ __global__ void k_mesh_roots(int nmeshes, const int64_t* __restrict__ foff, int 
 // kSpatialLevels + log2(n) whatever the geometry (midpoint splits of float boxes could otherwise
 // go on for hundreds of levels on adversarial inputs).
 constexpr int kSpatialLevels = 96;
+// Segments of at most kFinishSlots triangles leave the level loop: one block each finishes their
+// subtrees in shared memory (k_split_finish), with the same splits.
+constexpr int kFinishSlots = 1024;
+constexpr int kFinishThreads = 512;
 
 struct SplitSlots {
     int* perm;  // triangle id per slot
@@ -342,11 +346,24 @@ struct SplitSlots {
     int* seg;   // active segment of the slot at this level (-1: in a leaf)
 };
 
+// A level of at most kBoxCopyKeys segments accumulates its boxes in kBoxCopies copies (block b
+// adds to copy b % kBoxCopies, copies kBoxCopyKeys boxes apart), merged by k_split_decide: at the
+// top levels every block of the grid adds to the same one or two boxes, and one copy's six words
+// share an L2 slice that would serialise all of the grid's atomics.
+constexpr int kBoxCopies = 16;
+constexpr int kBoxCopyKeys = 256;
+constexpr int kBoxCopyStride = 6 * kBoxCopyKeys;  // words between copies
+
+__device__ __forceinline__ int box_copy_offset(bool copies) {
+    return copies ? (int)(blockIdx.x % kBoxCopies) * kBoxCopyStride : 0;
+}
+
 // Centroid boxes: lanes that add to the same box reduce together first (ordered-int encodings,
 // so min / max are integer reductions), then one atomic per group and axis. When the whole
 // block adds to one box (the top levels, where a segment spans many blocks) the block reduces
 // in shared memory and issues six atomics; otherwise each warp groups its lanes by box. Every
-// thread of the block must call it; threads with key < 0 add nothing.
+// thread of the block must call it; threads with key < 0 add nothing. `box` already points at
+// the block's copy (box_copy_offset).
 __device__ __forceinline__ void box_add(int key, float cx, float cy, float cz,
                                         unsigned* __restrict__ box) {
     __shared__ int s_key;
@@ -401,9 +418,19 @@ __device__ __forceinline__ void box_clear(unsigned* __restrict__ b) {
     }
 }
 
+// Clears box k in every copy that a level may use (all copies for k < kBoxCopyKeys).
+__device__ __forceinline__ void box_clear_level(unsigned* __restrict__ box, int k) {
+    if (k < kBoxCopyKeys) {
+#pragma unroll 1
+        for (int c = 0; c < kBoxCopies; ++c) box_clear(box + c * kBoxCopyStride + 6 * k);
+    } else {
+        box_clear(box + 6 * k);
+    }
+}
+
 __global__ void k_split_box_init(int nact, unsigned* __restrict__ box) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < nact) box_clear(box + 6 * i);
+    if (i < nact) box_clear_level(box, i);
 }
 
 // Validation, centroids and the first level's slots; the boxes of the first level's segments
@@ -413,7 +440,7 @@ __global__ void k_split_init(const float* __restrict__ V, const int32_t* __restr
                              int nmeshes, int64_t nf, const int* __restrict__ mesh_seg,
                              SplitSlots out, int* __restrict__ final_perm,
                              uint64_t* __restrict__ keys, unsigned* __restrict__ box,
-                             unsigned* __restrict__ status) {
+                             bool box_copies, unsigned* __restrict__ status) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int key = -1;
     float c[3] = {0.f, 0.f, 0.f};
@@ -449,22 +476,23 @@ __global__ void k_split_init(const float* __restrict__ V, const int32_t* __restr
         out.cy[t] = c[1];
         out.cz[t] = c[2];
         out.seg[t] = key;
-        if (key < 0) final_perm[t] = (int)t;  // the whole mesh is one leaf
+        if (key == -1) final_perm[t] = (int)t;  // the whole mesh is one leaf (-2: a small root)
         keys[t] = (uint64_t)m << MORTON_BITS;
     }
-    box_add(key, c[0], c[1], c[2], box);
+    box_add(key, c[0], c[1], c[2], box + box_copy_offset(box_copies));
 }
 
-__global__ void k_split_decide(int nact, bool by_position, const unsigned* __restrict__ box,
-                               int* __restrict__ axis_of, float* __restrict__ split_of,
-                               int* __restrict__ spatial_of) {
-    const int sg = blockIdx.x * blockDim.x + threadIdx.x;
-    if (sg >= nact) return;
+// The split of one segment from its centroid box (lo[a] = dec(box[a]), hi[a] = dec(box[3 + a])
+// at stride `stride`): the longest axis (the first on ties), its midpoint, and whether the split is
+// spatial (else by position).
+__device__ __forceinline__ void split_decide(const unsigned* __restrict__ box, int stride,
+                                             bool by_position, int& axis_out, float& split_out,
+                                             int& spatial_out) {
     float lo[3], hi[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        lo[a] = dec_float(box[6 * sg + a]);
-        hi[a] = dec_float(box[6 * sg + 3 + a]);
+        lo[a] = dec_float(box[a * stride]);
+        hi[a] = dec_float(box[(3 + a) * stride]);
     }
     int axis = 0;
     float ext = hi[0] - lo[0];
@@ -477,9 +505,30 @@ __global__ void k_split_decide(int nact, bool by_position, const unsigned* __res
         }
     }
     const float split = (lo[axis] + hi[axis]) * 0.5f;
-    axis_of[sg] = axis;
-    split_of[sg] = split;
-    spatial_of[sg] = (!by_position && ext > 0.f && split > lo[axis]) ? 1 : 0;
+    axis_out = axis;
+    split_out = split;
+    spatial_out = (!by_position && ext > 0.f && split > lo[axis]) ? 1 : 0;
+}
+
+__global__ void k_split_decide(int nact, bool by_position, const unsigned* __restrict__ box,
+                               int* __restrict__ axis_of, float* __restrict__ split_of,
+                               int* __restrict__ spatial_of) {
+    const int sg = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sg >= nact) return;
+    unsigned b[6];
+#pragma unroll
+    for (int a = 0; a < 6; ++a) b[a] = box[6 * sg + a];
+    if (nact <= kBoxCopyKeys) {  // merge the copies (all loads in flight together)
+#pragma unroll
+        for (int c = 1; c < kBoxCopies; ++c) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                b[a] = min(b[a], box[c * kBoxCopyStride + 6 * sg + a]);
+                b[3 + a] = max(b[3 + a], box[c * kBoxCopyStride + 6 * sg + 3 + a]);
+            }
+        }
+    }
+    split_decide(b, 1, by_position, axis_of[sg], split_of[sg], spatial_of[sg]);
 }
 
 __global__ void k_split_flags(int64_t n, SplitSlots cur, const int* __restrict__ s_start,
@@ -504,18 +553,23 @@ __global__ void k_split_flags(int64_t n, SplitSlots cur, const int* __restrict__
     flags[i] = f;  // flags[n] = 0: the scan's total entry
 }
 
-// Children of every active segment (lf = exclusive scan of the left flags): the two nodes, and
-// for each child of > K triangles a slot of the next level (allocated with an atomic counter,
-// its box cleared); child_next[2s + c] = that slot or -1 for a leaf. The next level's order of
-// segments is immaterial: positions come from the node ranges alone.
-__global__ void k_split_children(int nact, int node_base, int K, const int* __restrict__ s_start,
-                                 const int* __restrict__ s_end, const int* __restrict__ s_node,
-                                 const int* __restrict__ lf, int* __restrict__ nfirst,
-                                 int* __restrict__ nlast, int* __restrict__ nparent,
-                                 int* __restrict__ nleft, int* __restrict__ nright,
-                                 int* __restrict__ next_count, int* __restrict__ n_start,
+// Children of every active segment (lf = exclusive scan of the left flags): the two nodes (at
+// depth level + 1), and for each child of more than kFinishSlots triangles a slot of the next
+// level (allocated with an atomic counter, its box cleared); a child of K < size <= kFinishSlots
+// triangles goes to the small list {start, end, node, depth} that k_split_finish completes.
+// child_next[2s + c] = the next level's slot, -2 for a small child or -1 for a leaf. The order
+// of segments in either list is immaterial: positions come from the node ranges alone.
+// counts[0] / counts[1]: the next level's segments / the small list's length.
+__global__ void k_split_children(int nact, int node_base, int level, int K,
+                                 const int* __restrict__ s_start, const int* __restrict__ s_end,
+                                 const int* __restrict__ s_node, const int* __restrict__ lf,
+                                 int* __restrict__ nfirst, int* __restrict__ nlast,
+                                 int* __restrict__ nparent, int* __restrict__ nleft,
+                                 int* __restrict__ nright, int* __restrict__ depth_of,
+                                 int* __restrict__ counts, int* __restrict__ n_start,
                                  int* __restrict__ n_end, int* __restrict__ n_node,
-                                 unsigned* __restrict__ n_box, int* __restrict__ child_next) {
+                                 unsigned* __restrict__ n_box, int4* __restrict__ small,
+                                 int* __restrict__ child_next) {
     const int sg = blockIdx.x * blockDim.x + threadIdx.x;
     if (sg >= nact) return;
     const int b = s_start[sg], e = s_end[sg], mid = b + (lf[e] - lf[b]);
@@ -529,17 +583,20 @@ __global__ void k_split_children(int nact, int node_base, int K, const int* __re
     nleft[l] = nright[l] = nleft[r] = nright[r] = -1;
     nleft[p] = l;
     nright[p] = r;
+    depth_of[l] = depth_of[r] = level + 1;
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
         const int cb = c == 0 ? b : mid, ce = c == 0 ? mid : e;
-        const int k = warp_append(next_count, ce - cb > K);
+        const int k = warp_append(&counts[0], ce - cb > kFinishSlots);
         if (k >= 0) {
             n_start[k] = cb;
             n_end[k] = ce;
-            n_node[k] = node_base + 2 * sg + c;
-            box_clear(n_box + 6 * k);
+            n_node[k] = l + c;
+            box_clear_level(n_box, k);
         }
-        child_next[2 * sg + c] = k;
+        const int j = warp_append(&counts[1], ce - cb > K && ce - cb <= kFinishSlots);
+        if (j >= 0) small[j] = make_int4(cb, ce, l + c, level + 1);
+        child_next[2 * sg + c] = k >= 0 ? k : j >= 0 ? -2 : -1;
     }
 }
 
@@ -549,7 +606,8 @@ __global__ void k_split_children(int nact, int node_base, int K, const int* __re
 __global__ void k_split_scatter(int64_t n, SplitSlots cur, SplitSlots nxt,
                                 const int* __restrict__ lf, const int* __restrict__ s_start,
                                 const int* __restrict__ s_end, const int* __restrict__ child_next,
-                                int* __restrict__ final_perm, unsigned* __restrict__ n_box) {
+                                int* __restrict__ final_perm, unsigned* __restrict__ n_box,
+                                const int* __restrict__ next_count) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int key = -1;
     float cx = 0.f, cy = 0.f, cz = 0.f;
@@ -563,7 +621,7 @@ __global__ void k_split_scatter(int64_t n, SplitSlots cur, SplitSlots nxt,
             const bool left = lf[i + 1] != lf[i];  // the exclusive scan steps where the flag is set
             const int64_t dest = left ? b + left_before : b + nl + ((int)(i - b) - left_before);
             const int k = child_next[2 * sg + (left ? 0 : 1)];
-            if (k >= 0) {
+            if (k >= 0 || k == -2) {  // active next level, or a small segment's slots
                 cx = cur.cx[i];
                 cy = cur.cy[i];
                 cz = cur.cz[i];
@@ -571,15 +629,220 @@ __global__ void k_split_scatter(int64_t n, SplitSlots cur, SplitSlots nxt,
                 nxt.cx[dest] = cx;
                 nxt.cy[dest] = cy;
                 nxt.cz[dest] = cz;
-                nxt.seg[dest] = k;
-                key = k;
+                nxt.seg[dest] = k >= 0 ? k : -1;
+                key = k >= 0 ? k : -1;
             } else {
                 final_perm[dest] = cur.perm[i];
                 nxt.seg[dest] = -1;
             }
         }
     }
-    box_add(key, cx, cy, cz, n_box);
+    box_add(key, cx, cy, cz, n_box + box_copy_offset(*next_count <= kBoxCopyKeys));
+}
+
+// A small segment in shared memory. Sub-segments are named by their first position, so a
+// split names its children itself (b and mid); the slots carry their original local index, and
+// centroids stay where they were loaded.
+struct FinishShared {
+    float c[3][kFinishSlots];              // centroid of each original local slot
+    int perm[kFinishSlots];                // triangle of each original local slot
+    unsigned short orig[2][kFinishSlots];  // original local slot at each position
+    short sid[2][kFinishSlots];            // first position of the position's segment (-1: leaf)
+    short send[2][kFinishSlots];           // end of the segment that starts at a position
+    int snode[2][kFinishSlots];            // node of the segment that starts at a position
+    unsigned box[6][kFinishSlots];         // centroid box of the segment that starts there
+    int scan[kFinishSlots + 1];
+    int wsum[kFinishThreads / 32];
+    int ns[2], rank, node_base;
+};
+
+// Exclusive scan of a[0 .. count) in shared memory by the whole block (count <= 8 * blockDim).
+__device__ void block_exclusive_scan(int* a, int count, int* wsum) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarps = blockDim.x >> 5;
+    const int per = (count + blockDim.x - 1) / blockDim.x;
+    const int b = min(tid * per, count), e = min(b + per, count);
+    int sum = 0;
+    for (int i = b; i < e; ++i) sum += a[i];
+    int x = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int w = lane < nwarps ? wsum[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < nwarps) wsum[lane] = w;
+    }
+    __syncthreads();
+    int run = x - sum + (warp > 0 ? wsum[warp - 1] : 0);
+    for (int i = b; i < e; ++i) {
+        const int v = a[i];
+        a[i] = run;
+        run += v;
+    }
+    __syncthreads();
+}
+
+// One block per small segment small[blockIdx.x] = {start, end, node, depth}: its subtree, split
+// by split by the level loop's rules (split_decide and the flags, children and stable partition
+// of k_split_flags / k_split_children / k_split_scatter) in shared memory. The slots are in A for
+// an even depth and in B for an odd one (the level that made the segment wrote them there, and
+// later levels write only other segments' ranges). Each step's node ids are one allocation from
+// node_count.
+__global__ void __launch_bounds__(kFinishThreads) k_split_finish(
+    const int4* __restrict__ small, SplitSlots A, SplitSlots B, int K, int* __restrict__ node_count,
+    int cap, int* __restrict__ nfirst, int* __restrict__ nlast, int* __restrict__ nparent,
+    int* __restrict__ nleft, int* __restrict__ nright, int* __restrict__ depth_of,
+    int* __restrict__ final_perm, unsigned* __restrict__ status) {
+    extern __shared__ __align__(16) unsigned char finish_smem[];
+    FinishShared& S = *reinterpret_cast<FinishShared*>(finish_smem);
+    const int4 seg = small[blockIdx.x];
+    const int gb = seg.x, size = seg.y - seg.x, d0 = seg.w, tid = threadIdx.x;
+    if (size > kFinishSlots || size <= K) {  // never made so by k_split_children
+        if (tid == 0) atomicOr(status, ST_BUILD_BOUND);
+        return;
+    }
+    const SplitSlots& X = (d0 & 1) ? B : A;
+    for (int i = tid; i < size; i += kFinishThreads) {
+        S.c[0][i] = X.cx[gb + i];
+        S.c[1][i] = X.cy[gb + i];
+        S.c[2][i] = X.cz[gb + i];
+        S.perm[i] = X.perm[gb + i];
+        S.orig[0][i] = (unsigned short)i;
+        S.sid[0][i] = 0;
+    }
+    if (tid == 0) {
+        S.ns[0] = 1;
+        S.send[0][0] = (short)size;
+        S.snode[0][0] = seg.z;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            S.box[a][0] = 0xffffffffu;
+            S.box[3 + a][0] = 0u;
+        }
+    }
+    __syncthreads();
+    int cur = 0;
+    for (int depth = d0;; ++depth) {
+        const int ns = S.ns[cur];
+        if (ns == 0) break;
+        if (depth > kSpatialLevels + 64) {  // position splits halve every segment
+            if (tid == 0) atomicOr(status, ST_BUILD_BOUND);
+            return;
+        }
+        // centroid boxes: lanes of one segment reduce together, then one atomic per axis
+        for (int i0 = 0; i0 < size; i0 += kFinishThreads) {
+            const int i = i0 + tid;
+            const int key = i < size ? S.sid[cur][i] : -1;
+            const unsigned act = __ballot_sync(0xffffffffu, key >= 0);
+            if (key >= 0) {
+                const unsigned peers = __match_any_sync(act, key);
+                const bool leader = (tid & 31) == __ffs(peers) - 1;
+                const int o = S.orig[cur][i];
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    const unsigned ev = enc_float(S.c[a][o]);
+                    const unsigned lo = __reduce_min_sync(peers, ev), hi = __reduce_max_sync(peers, ev);
+                    if (leader) {
+                        atomicMin(&S.box[a][key], lo);
+                        atomicMax(&S.box[3 + a][key], hi);
+                    }
+                }
+            }
+        }
+        // the step's node ids (every active segment splits): the atomic's result is stored only
+        // after the flags, so the block does not wait for it at the next barrier
+        int nb = 0;
+        if (tid == 0) {
+            nb = atomicAdd(node_count, 2 * ns);
+            S.rank = 0;
+            S.ns[cur ^ 1] = 0;
+        }
+        __syncthreads();
+        // left flags, each slot deciding its segment's split from the box
+        const bool by_position = depth >= kSpatialLevels;
+        for (int i = tid; i <= size; i += kFinishThreads) {
+            int f = 0;
+            if (i < size) {
+                const int b = S.sid[cur][i];
+                if (b >= 0) {
+                    int axis, spatial;
+                    float split;
+                    split_decide(&S.box[0][b], kFinishSlots, by_position, axis, split, spatial);
+                    const int e = S.send[cur][b];
+                    f = spatial ? (S.c[axis][S.orig[cur][i]] < split ? 1 : 0)
+                                : ((i - b) < (e - b) / 2 ? 1 : 0);
+                }
+            }
+            S.scan[i] = f;
+        }
+        if (tid == 0) S.node_base = nb;
+        __syncthreads();
+        if (S.node_base + 2 * ns > cap) {  // uniform: no node of this step could be written
+            if (tid == 0) atomicOr(status, ST_BUILD_BOUND);
+            return;
+        }
+        block_exclusive_scan(S.scan, size + 1, S.wsum);
+        // stable partition; a segment's first position makes its two nodes and next segments
+        const int node_base = S.node_base;
+        for (int i = tid; i < size; i += kFinishThreads) {
+            const int b = S.sid[cur][i];
+            if (b < 0) {
+                S.sid[cur ^ 1][i] = -1;  // no moving slot lands outside its own segment
+                continue;
+            }
+            const int e = S.send[cur][b];
+            const int fb = S.scan[b], mid = b + (S.scan[e] - fb), left_before = S.scan[i] - fb;
+            const bool left = S.scan[i + 1] != S.scan[i];
+            const int dest = left ? b + left_before : mid + ((i - b) - left_before);
+            const int cb = left ? b : mid, ce = left ? mid : e;
+            if (i == b) {
+                const int p = S.snode[cur][b];
+                const int l = node_base + 2 * atomicAdd(&S.rank, 1), r = l + 1;  // r < cap
+                nfirst[l] = gb + b;
+                nlast[l] = gb + mid - 1;
+                nfirst[r] = gb + mid;
+                nlast[r] = gb + e - 1;
+                nparent[l] = p;
+                nparent[r] = p;
+                nleft[l] = nright[l] = nleft[r] = nright[r] = -1;
+                nleft[p] = l;
+                nright[p] = r;
+                depth_of[l] = depth_of[r] = depth + 1;
+#pragma unroll
+                for (int c = 0; c < 2; ++c) {
+                    const int xb = c == 0 ? b : mid, xe = c == 0 ? mid : e;
+                    if (xe - xb > K) {
+                        S.send[cur ^ 1][xb] = (short)xe;
+                        S.snode[cur ^ 1][xb] = l + c;
+#pragma unroll
+                        for (int a = 0; a < 3; ++a) {
+                            S.box[a][xb] = 0xffffffffu;
+                            S.box[3 + a][xb] = 0u;
+                        }
+                        atomicAdd(&S.ns[cur ^ 1], 1);
+                    }
+                }
+            }
+            const int o = S.orig[cur][i];
+            if (ce - cb > K) {
+                S.sid[cur ^ 1][dest] = (short)cb;
+                S.orig[cur ^ 1][dest] = (unsigned short)o;
+            } else {
+                S.sid[cur ^ 1][dest] = -1;
+                final_perm[gb + dest] = S.perm[o];
+            }
+        }
+        __syncthreads();
+        cur ^= 1;
+    }
 }
 
 // Node flags of the split tree (every node emitted; leaves = no children), the per-first-slot
@@ -1027,9 +1290,10 @@ __device__ __forceinline__ bool refit_internal(const uint64_t* __restrict__ keys
 __global__ void k_height_hist(int nint, const uint64_t* __restrict__ keys,
                               const int* __restrict__ first, const int* __restrict__ last,
                               const uint8_t* __restrict__ flags, const int* __restrict__ height,
-                              int* __restrict__ hist) {
+                              int* __restrict__ hist, unsigned* __restrict__ status) {
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= nint || !refit_internal(keys, first, last, flags, u)) return;
+    if (height[u] < 0 || height[u] >= kMaxHeight) atomicOr(status, ST_REFIT_ORPHAN);
     const int h = min(max(height[u], 0), kMaxHeight - 1);
     const unsigned peers = __match_any_sync(__activemask(), h);
     if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&hist[h], __popc(peers));
@@ -1522,10 +1786,8 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
         const uint32_t* tri_of_slot = nullptr;
         int num_nodes = 0;
         unsigned st_h = 0;
-        // split tree: the internal nodes split at each level (int_nodes[off, off + count)), for
-        // the level-by-level refit
-        std::vector<std::pair<int, int>> split_levels;
-        int* int_nodes = split ? (int*)track(dalloc<int>(n, st)) : nullptr;
+        // split tree: every node's depth (roots 0), the order of the level-by-level refit
+        int* depth_of = split ? (int*)track(dalloc<int>(cap, st)) : nullptr;
         auto check_input = [&]() {
             FWN_CUDA_CHECK(cudaMemcpyAsync(&st_h, status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
             FWN_CUDA_CHECK(cudaStreamSynchronize(st));
@@ -1573,9 +1835,11 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
                                                                  last, pos, skip, e.meshes);
         } else {
             NvtxRange trace_tree("fwn build: top-down splits + DFS layout");
-            // roots: one node per non-empty mesh; a mesh of > K triangles is an active segment
+            // roots: one node per non-empty mesh; a mesh of > kFinishSlots triangles is an active
+            // segment of the first level, one of K < size <= kFinishSlots a small segment
             std::vector<int> root_node(nmeshes, -1), mesh_seg(nmeshes, -1);
             std::vector<int> h_first, h_last, s_start, s_end, s_node;
+            std::vector<int4> h_small;
             for (int64_t m = 0; m < nmeshes; ++m) {
                 const int64_t b = foff_h[m], en = foff_h[m + 1];
                 if (en <= b) continue;
@@ -1583,11 +1847,14 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
                 root_node[m] = id;
                 h_first.push_back((int)b);
                 h_last.push_back((int)(en - 1));
-                if (en - b > K) {
+                if (en - b > kFinishSlots) {
                     mesh_seg[m] = (int)s_start.size();
                     s_start.push_back((int)b);
                     s_end.push_back((int)en);
                     s_node.push_back(id);
+                } else if (en - b > K) {
+                    mesh_seg[m] = -2;
+                    h_small.push_back(make_int4((int)b, (int)en, id, 0));
                 }
             }
             const int nroots = (int)h_first.size();
@@ -1604,14 +1871,20 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
             }
             int* lflags = (int*)track(dalloc<int>(n + 1, st));
             int* child_next = (int*)track(dalloc<int>(2 * (size_t)smax, st));
-            int* next_count = (int*)track(dalloc<int>(1, st));
+            int* counts = (int*)track(dalloc<int>(3, st));  // next level, small list, node ids
+            int4* small = (int4*)track(dalloc<int4>(smax, st));
+            if (!h_small.empty())
+                FWN_CUDA_CHECK(cudaMemcpyAsync(small, h_small.data(), h_small.size() * sizeof(int4),
+                                               cudaMemcpyHostToDevice, st));
+            FWN_CUDA_CHECK(cudaMemsetAsync(depth_of, 0, (size_t)cap * sizeof(int), st));
             int* seg_a[3], *seg_b[3];  // start, end, node of this level / the next
             for (int k = 0; k < 3; ++k) {
                 seg_a[k] = (int*)track(dalloc<int>(smax, st));
                 seg_b[k] = (int*)track(dalloc<int>(smax, st));
             }
-            unsigned* box_a = (unsigned*)track(dalloc<unsigned>(6 * (size_t)smax, st));
-            unsigned* box_b = (unsigned*)track(dalloc<unsigned>(6 * (size_t)smax, st));
+            const size_t box_words = std::max(6 * (size_t)smax, (size_t)kBoxCopies * kBoxCopyStride);
+            unsigned* box_a = (unsigned*)track(dalloc<unsigned>(box_words, st));
+            unsigned* box_b = (unsigned*)track(dalloc<unsigned>(box_words, st));
             int* axis_of = (int*)track(dalloc<int>(smax, st));
             float* split_of = (float*)track(dalloc<float>(smax, st));
             int* spatial_of = (int*)track(dalloc<int>(smax, st));
@@ -1640,10 +1913,11 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
             }
             k_split_init<<<grid_for(n, 256), 256, 0, st>>>(d_V, d_F, voff, foff, (int)nmeshes, nf,
                                                            d_mesh_seg, A, final_perm, skeys, box_a,
-                                                           status);
+                                                           nact <= kBoxCopyKeys, status);
             FWN_CUDA_CHECK(cudaGetLastError());
             check_input();
             int node_base = nroots;
+            int nsmall = (int)h_small.size();
             SplitSlots* cur = &A;
             SplitSlots* nxt = &B;
             int level = 0;
@@ -1657,31 +1931,48 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
                                                                    axis_of, split_of, spatial_of,
                                                                    lflags);
                 exclusive_scan_i32(lflags, n + 1, scan_tmp, st);
-                FWN_CUDA_CHECK(cudaMemsetAsync(next_count, 0, sizeof(int), st));
+                const int h_counts[2] = {0, nsmall};
+                FWN_CUDA_CHECK(cudaMemcpyAsync(counts, h_counts, sizeof(h_counts),
+                                               cudaMemcpyHostToDevice, st));
                 k_split_children<<<grid_for(nact, 128), 128, 0, st>>>(
-                    nact, node_base, K, seg_a[0], seg_a[1], seg_a[2], lflags, first, last, parent,
-                    left, right, next_count, seg_b[0], seg_b[1], seg_b[2], box_b, child_next);
-                const int lvl_off = split_levels.empty() ? 0 : split_levels.back().first + split_levels.back().second;
-                if (lvl_off + nact > n) throw Error(FWN_INTERNAL, "split build internal node overflow");
-                FWN_CUDA_CHECK(cudaMemcpyAsync(int_nodes + lvl_off, seg_a[2], nact * sizeof(int),
-                                               cudaMemcpyDeviceToDevice, st));
-                split_levels.emplace_back(lvl_off, nact);
+                    nact, node_base, level, K, seg_a[0], seg_a[1], seg_a[2], lflags, first, last,
+                    parent, left, right, depth_of, counts, seg_b[0], seg_b[1], seg_b[2], box_b,
+                    small, child_next);
                 // lflags now holds the exclusive scan of the left flags (a slot's flag is the
                 // step from its entry to the next)
                 k_split_scatter<<<grid_for(n, 256), 256, 0, st>>>(n, *cur, *nxt, lflags, seg_a[0],
                                                                  seg_a[1], child_next, final_perm,
-                                                                 box_b);
+                                                                 box_b, counts);
                 FWN_CUDA_CHECK(cudaGetLastError());
                 node_base += 2 * nact;
-                int next = 0;
-                FWN_CUDA_CHECK(cudaMemcpyAsync(&next, next_count, sizeof(int),
-                                               cudaMemcpyDeviceToHost, st));
+                int next[2] = {0, 0};
+                FWN_CUDA_CHECK(cudaMemcpyAsync(next, counts, sizeof(next), cudaMemcpyDeviceToHost,
+                                               st));
                 FWN_CUDA_CHECK(cudaStreamSynchronize(st));
-                nact = next;
+                nact = next[0];
+                nsmall = next[1];
                 ++level;
                 std::swap(cur, nxt);
                 std::swap(box_a, box_b);
                 for (int k = 0; k < 3; ++k) std::swap(seg_a[k], seg_b[k]);
+            }
+            if (nsmall > 0) {  // the small segments' subtrees, one block each
+                FWN_CUDA_CHECK(cudaMemcpyAsync(counts + 2, &node_base, sizeof(int),
+                                               cudaMemcpyHostToDevice, st));
+                FWN_CUDA_CHECK(cudaFuncSetAttribute(k_split_finish,
+                                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    (int)sizeof(FinishShared)));
+                k_split_finish<<<nsmall, kFinishThreads, sizeof(FinishShared), st>>>(
+                    small, A, B, K, counts + 2, cap, first, last, parent, left, right, depth_of,
+                    final_perm, status);
+                FWN_CUDA_CHECK(cudaGetLastError());
+                FWN_CUDA_CHECK(cudaMemcpyAsync(&node_base, counts + 2, sizeof(int),
+                                               cudaMemcpyDeviceToHost, st));
+                FWN_CUDA_CHECK(cudaMemcpyAsync(&st_h, status, sizeof(unsigned),
+                                               cudaMemcpyDeviceToHost, st));
+                FWN_CUDA_CHECK(cudaStreamSynchronize(st));
+                if ((st_h & ST_BUILD_BOUND) || node_base > cap)
+                    throw Error(FWN_INTERNAL, "split build passed its node or depth bound");
             }
             num_nodes = node_base;
             keys = skeys;
@@ -1726,38 +2017,40 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
         if (NL > 0)
             k_refit<<<grid_for(NL, 128), 128, 0, st>>>(NL, leaf_list, keys, first, last, pos,
                                                        tri_of_slot, d_V, d_F, voff, stage);
-        if (!split && NL > 0 && n > 1) {
-            // LBVH: internal nodes height by height (k_heights, then a counting sort)
-            int* height = (int*)track(dalloc<int>(nint, st));
+        if (NL > 0 && n > 1) {
+            // internal nodes level by level, one thread per node of a dense list (an atomic
+            // ascent would leave most lanes of its warps idle on GB300's narrow FP64 pipe): the
+            // split tree deepest first by node depth, the LBVH lowest first by node height
+            // (k_heights); the lists come from one counting sort by that key
+            const int count = split ? num_nodes : nint;
+            int* key = depth_of;
+            if (!split) {
+                key = (int*)track(dalloc<int>(nint, st));
+                FWN_CUDA_CHECK(cudaMemsetAsync(key, 0, (size_t)nint * sizeof(int), st));
+                k_heights<<<grid_for(NL, 128), 128, 0, st>>>(NL, leaf_list, keys, parent, first,
+                                                             last, visit, key, status);
+            }
             int* hist = (int*)track(dalloc<int>(kMaxHeight, st));
-            int* hlist = (int*)track(dalloc<int>(nint, st));
-            FWN_CUDA_CHECK(cudaMemsetAsync(height, 0, (size_t)nint * sizeof(int), st));
+            int* order = (int*)track(dalloc<int>(count, st));
             FWN_CUDA_CHECK(cudaMemsetAsync(hist, 0, kMaxHeight * sizeof(int), st));
-            k_heights<<<grid_for(NL, 128), 128, 0, st>>>(NL, leaf_list, keys, parent, first, last,
-                                                         visit, height, status);
-            k_height_hist<<<grid_for(nint, 256), 256, 0, st>>>(nint, keys, first, last, flags,
-                                                               height, hist);
+            k_height_hist<<<grid_for(count, 256), 256, 0, st>>>(count, keys, first, last, flags, key,
+                                                                hist, status);
             std::vector<int> h_hist(kMaxHeight);
             FWN_CUDA_CHECK(cudaMemcpyAsync(h_hist.data(), hist, kMaxHeight * sizeof(int),
                                            cudaMemcpyDeviceToHost, st));
             k_height_offsets<<<1, 32, 0, st>>>(hist);
-            k_height_sort<<<grid_for(nint, 256), 256, 0, st>>>(nint, keys, first, last, flags,
-                                                               height, hist, hlist);
+            k_height_sort<<<grid_for(count, 256), 256, 0, st>>>(count, keys, first, last, flags, key,
+                                                                hist, order);
             FWN_CUDA_CHECK(cudaStreamSynchronize(st));
-            int off = 0;
-            for (int h = 0; h < kMaxHeight; ++h) {
-                if (h >= 1 && h_hist[h] > 0)
+            std::vector<int> off(kMaxHeight + 1, 0);
+            for (int h = 0; h < kMaxHeight; ++h) off[h + 1] = off[h] + h_hist[h];
+            for (int t = 0; t < kMaxHeight; ++t) {
+                const int h = split ? kMaxHeight - 1 - t : t;
+                if (h_hist[h] > 0)
                     k_refit_level<<<grid_for(h_hist[h], 128), 128, 0, st>>>(
-                        h_hist[h], hlist + off, left, right, pos, stage, status);
-                off += h_hist[h];
+                        h_hist[h], order + off[h], left, right, pos, stage, status);
             }
         }
-        // split tree: the internal nodes level by level, deepest first (a node's children are
-        // one level below it), one thread per node of a dense list; an atomic ascent would leave
-        // most lanes of its warps idle on GB300's narrow FP64 pipe
-        for (auto it = split_levels.rbegin(); it != split_levels.rend(); ++it)
-            k_refit_level<<<grid_for(it->second, 128), 128, 0, st>>>(
-                it->second, int_nodes + it->first, left, right, pos, stage, status);
         FWN_CUDA_CHECK(cudaGetLastError());
         FWN_CUDA_CHECK(cudaMalloc(&e.tris, (size_t)n * sizeof(TriF32)));
         FWN_CUDA_CHECK(cudaMalloc(&e.sorted_tri, (size_t)n * sizeof(int)));
