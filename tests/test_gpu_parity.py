@@ -550,6 +550,41 @@ def test_split_builder_degenerate_geometry(torch_cuda, oracle_mod):
             assert got["tri_count"].max() <= leaf
 
 
+@pytest.mark.parametrize("leaf", [1, 8, 16])
+def test_split_builder_finisher_boundaries(torch_cuda, oracle_mod, leaf):
+    """The top-down builder hands every segment of at most 1024 triangles to a per-block
+    finisher in shared memory. Meshes on either side of that size (1024 / 1025, 2048 / 2049
+    triangles, scattered random triangles), a mesh of 1024 and one of 3000 copies of a single
+    triangle (every split by position, inside the finisher and before it) and small meshes, in
+    one forest and one at a time: the device trees equal their CPU restatement bit for bit."""
+    rng = np.random.default_rng(5)
+    tri = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    meshes = []
+    for nf in (1024, 1025, 2048, 2049, 513, 9, 8, 1):
+        V = rng.uniform(-1, 1, size=(3 * nf, 3)).astype(np.float32)
+        meshes.append((V, np.arange(3 * nf, dtype=np.int32).reshape(nf, 3)))
+    for nf in (1024, 3000):
+        meshes.append((np.tile(tri, (nf, 1)), np.arange(3 * nf, dtype=np.int32).reshape(nf, 3)))
+    voff = np.concatenate([[0], np.cumsum([len(v) for v, _ in meshes])]).astype(np.int64)
+    foff = np.concatenate([[0], np.cumsum([len(f) for _, f in meshes])]).astype(np.int64)
+    V = np.concatenate([v for v, _ in meshes])
+    F = np.concatenate([f for _, f in meshes])
+    keys = ("skip", "tri_begin", "tri_count", "sorted_tri", "mesh_root")
+    forest = fwn.Forest(V, voff, F, foff, records=BOTH, leaf_size=leaf, builder=1)
+    got = forest.export_tree()
+    ref = oracle_mod.LbvhTree(V, F, leaf_size=leaf, voff=voff, foff=foff, builder=1).export()
+    for k in keys:
+        np.testing.assert_array_equal(got[k], ref[k], err_msg=k)
+    np.testing.assert_array_equal(got["center_radius"], ref["center_radius"])
+    for Vm, Fm in meshes[:2] + meshes[-2:]:
+        got = _engine(Vm, Fm, leaf_size=leaf, builder=1).export_tree()
+        ref = oracle_mod.LbvhTree(Vm, Fm, leaf_size=leaf, builder=1).export()
+        for k in keys:
+            np.testing.assert_array_equal(got[k], ref[k], err_msg=k)
+        np.testing.assert_array_equal(got["center_radius"], ref["center_radius"])
+        assert got["tri_count"].max() <= leaf
+
+
 @pytest.mark.parametrize("builder", [0, 1])
 def test_save_load_round_trip(torch_cuda, tmp_path, builder):
     """An engine written with fwn_save and read back with fwn_load has the same tree and answers
