@@ -255,6 +255,31 @@ __device__ __forceinline__ int warp_append(int* __restrict__ counter, bool pred)
     return pred ? base + __popc(bal & ((1u << lane) - 1u)) : -1;
 }
 
+// The same with one atomicAdd per block, for kernels over millions of threads (one counter
+// bumped once per warp still serialises ~n / 32 atomics at one L2 address). Every thread of the
+// block calls it at the same point (blockDim a multiple of 32, no thread returned before).
+__device__ __forceinline__ int block_append(int* __restrict__ counter, bool pred) {
+    __shared__ int s_warp[32];
+    __shared__ int s_base;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned bal = __ballot_sync(0xffffffffu, pred);
+    if (lane == 0) s_warp[warp] = __popc(bal);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            const int c = s_warp[w];
+            s_warp[w] = acc;
+            acc += c;
+        }
+        s_base = acc ? atomicAdd(counter, acc) : 0;
+    }
+    __syncthreads();
+    const int at = pred ? s_base + s_warp[warp] + __popc(bal & ((1u << lane) - 1u)) : -1;
+    __syncthreads();  // the shared words are reused by the next call
+    return at;
+}
+
 // flags: bit0 emitted, bit1 leaf
 __global__ void k_emit_count(int n, int K, const uint64_t* __restrict__ keys,
                              const int* __restrict__ parent, const int* __restrict__ first,
@@ -262,15 +287,18 @@ __global__ void k_emit_count(int n, int K, const uint64_t* __restrict__ keys,
                              uint8_t* __restrict__ flags, int* __restrict__ leaf_list,
                              int* __restrict__ leaf_list_len) {
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
-    if (u >= 2 * n - 1) return;
-    const int pu = parent[u];
-    const bool emitted = (u == 0) || (pu >= 0 && is_big(keys, first, last, pu, K));
-    const bool leaf = (u >= n - 1) || !is_big(keys, first, last, u, K);
-    flags[u] = (uint8_t)((emitted ? 1 : 0) | (leaf ? 2 : 0));
-    if (emitted) atomicAdd(&cnt_first[first[u]], 1);
+    bool pred = false;
+    if (u < 2 * n - 1) {
+        const int pu = parent[u];
+        const bool emitted = (u == 0) || (pu >= 0 && is_big(keys, first, last, pu, K));
+        const bool leaf = (u >= n - 1) || !is_big(keys, first, last, u, K);
+        flags[u] = (uint8_t)((emitted ? 1 : 0) | (leaf ? 2 : 0));
+        if (emitted) atomicAdd(&cnt_first[first[u]], 1);
+        pred = emitted && leaf && !is_cross(keys, first, last, u);
+    }
     // emitted leaves (never a node spanning meshes: such a node is "big") feed the refit, one
     // thread each; the list order does not matter (each node's arithmetic is fixed)
-    const int at = warp_append(leaf_list_len, emitted && leaf && !is_cross(keys, first, last, u));
+    const int at = block_append(leaf_list_len, pred);
     if (at >= 0) leaf_list[at] = u;
 }
 
@@ -852,11 +880,13 @@ __global__ void k_split_emit(int num_nodes, const int* __restrict__ nfirst,
                              int* __restrict__ cnt_first, int* __restrict__ leaf_list,
                              int* __restrict__ leaf_list_len) {
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
-    if (u >= num_nodes) return;
-    const bool leaf = nleft[u] < 0;
-    flags[u] = (uint8_t)(1 | (leaf ? 2 : 0));
-    atomicAdd(&cnt_first[nfirst[u]], 1);
-    const int at = warp_append(leaf_list_len, leaf);
+    bool leaf = false;
+    if (u < num_nodes) {
+        leaf = nleft[u] < 0;
+        flags[u] = (uint8_t)(1 | (leaf ? 2 : 0));
+        atomicAdd(&cnt_first[nfirst[u]], 1);
+    }
+    const int at = block_append(leaf_list_len, leaf);
     if (at >= 0) leaf_list[at] = u;
 }
 
@@ -1211,16 +1241,22 @@ __global__ void k_leaf_offsets(int* __restrict__ hist) {  // one thread: exclusi
 __global__ void k_leaf_sort(int nl, const int* __restrict__ leaves, const int* __restrict__ first,
                             const int* __restrict__ last, int* __restrict__ offset,
                             int* __restrict__ sorted) {
+    __shared__ int cnt[kLeafSizes];   // the block's leaves per size (ranks from shared atomics)
+    __shared__ int base[kLeafSizes];  // where they go: one global atomic per non-zero size
+    if (threadIdx.x < kLeafSizes) cnt[threadIdx.x] = 0;
+    __syncthreads();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= nl) return;
-    const int u = leaves[k];
-    const int sz = leaf_size_of(first, last, u);
-    const unsigned peers = __match_any_sync(__activemask(), sz);
-    const int leader = __ffs(peers) - 1;
-    int base = 0;
-    if ((int)(threadIdx.x & 31) == leader) base = atomicAdd(&offset[sz], __popc(peers));
-    base = __shfl_sync(peers, base, leader);
-    sorted[base + __popc(peers & ((1u << (threadIdx.x & 31)) - 1u))] = u;
+    int u = -1, sz = 0, rank = 0;
+    if (k < nl) {
+        u = leaves[k];
+        sz = leaf_size_of(first, last, u);
+        rank = atomicAdd(&cnt[sz], 1);
+    }
+    __syncthreads();
+    if (threadIdx.x < kLeafSizes && cnt[threadIdx.x])
+        base[threadIdx.x] = atomicAdd(&offset[threadIdx.x], cnt[threadIdx.x]);
+    __syncthreads();
+    if (u >= 0) sorted[base[sz] + rank] = u;
 }
 
 // The internal nodes of one level of a split tree, or of one height of the LBVH
@@ -1291,12 +1327,17 @@ __global__ void k_height_hist(int nint, const uint64_t* __restrict__ keys,
                               const int* __restrict__ first, const int* __restrict__ last,
                               const uint8_t* __restrict__ flags, const int* __restrict__ height,
                               int* __restrict__ hist, unsigned* __restrict__ status) {
+    __shared__ int h_s[kMaxHeight];  // the block's counts, then one atomic per non-zero entry
+    for (int i = threadIdx.x; i < kMaxHeight; i += blockDim.x) h_s[i] = 0;
+    __syncthreads();
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
-    if (u >= nint || !refit_internal(keys, first, last, flags, u)) return;
-    if (height[u] < 0 || height[u] >= kMaxHeight) atomicOr(status, ST_REFIT_ORPHAN);
-    const int h = min(max(height[u], 0), kMaxHeight - 1);
-    const unsigned peers = __match_any_sync(__activemask(), h);
-    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&hist[h], __popc(peers));
+    if (u < nint && refit_internal(keys, first, last, flags, u)) {
+        if (height[u] < 0 || height[u] >= kMaxHeight) atomicOr(status, ST_REFIT_ORPHAN);
+        atomicAdd(&h_s[min(max(height[u], 0), kMaxHeight - 1)], 1);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kMaxHeight; i += blockDim.x)
+        if (h_s[i]) atomicAdd(&hist[i], h_s[i]);
 }
 
 __global__ void k_height_offsets(int* __restrict__ hist) {  // one thread: exclusive scan in place
@@ -1313,15 +1354,21 @@ __global__ void k_height_sort(int nint, const uint64_t* __restrict__ keys,
                               const int* __restrict__ first, const int* __restrict__ last,
                               const uint8_t* __restrict__ flags, const int* __restrict__ height,
                               int* __restrict__ offset, int* __restrict__ list) {
+    __shared__ int cnt[kMaxHeight];   // the block's nodes per key (ranks from shared atomics)
+    __shared__ int base[kMaxHeight];  // where they go: one global atomic per non-zero key
+    for (int i = threadIdx.x; i < kMaxHeight; i += blockDim.x) cnt[i] = 0;
+    __syncthreads();
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
-    if (u >= nint || !refit_internal(keys, first, last, flags, u)) return;
-    const int h = min(max(height[u], 0), kMaxHeight - 1);
-    const unsigned peers = __match_any_sync(__activemask(), h);
-    const int leader = __ffs(peers) - 1;
-    int base = 0;
-    if ((int)(threadIdx.x & 31) == leader) base = atomicAdd(&offset[h], __popc(peers));
-    base = __shfl_sync(peers, base, leader);
-    list[base + __popc(peers & ((1u << (threadIdx.x & 31)) - 1u))] = u;
+    int h = -1, rank = 0;
+    if (u < nint && refit_internal(keys, first, last, flags, u)) {
+        h = min(max(height[u], 0), kMaxHeight - 1);
+        rank = atomicAdd(&cnt[h], 1);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kMaxHeight; i += blockDim.x)
+        if (cnt[i]) base[i] = atomicAdd(&offset[i], cnt[i]);
+    __syncthreads();
+    if (h >= 0) list[base[h] + rank] = u;
 }
 
 // ---- K4a: exact node radii ------------------------------------------------------------------------
@@ -1403,9 +1450,9 @@ __global__ void k_radius_list(int num_nodes, const uint64_t* __restrict__ keys,
                               const uint8_t* __restrict__ flags, int* __restrict__ list,
                               int* __restrict__ count) {
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
-    if (u >= num_nodes) return;
-    const int at = warp_append(count, internal_emitted(keys, first, last, flags, u) &&
-                                          last[u] - first[u] + 1 <= kRadiusChunk);
+    const bool pred = u < num_nodes && internal_emitted(keys, first, last, flags, u) &&
+                      last[u] - first[u] + 1 <= kRadiusChunk;
+    const int at = block_append(count, pred);
     if (at >= 0) list[at] = u;
 }
 
@@ -1587,14 +1634,14 @@ __global__ void k_convert(int num_records, const int* __restrict__ node_of_pos,
                           NodeF32* __restrict__ n32, NodeF64* __restrict__ n64,
                           int* __restrict__ leaf_count) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int u = i < num_records ? node_of_pos[i] : 0;
+    const bool cross = i < num_records && is_cross(keys, first, last, u);
+    const bool leaf = i < num_records && (flags[u] & 2) && !cross;
+    const int nleaf = __syncthreads_count(leaf);  // counts the leaves, one atomic per block
+    if (threadIdx.x == 0 && nleaf) atomicAdd(leaf_count, nleaf);
     if (i >= num_records) return;
-    const int u = node_of_pos[i];
-    const uint8_t fl = flags[u];
-    const bool cross = is_cross(keys, first, last, u);
-    const bool leaf = (fl & 2) && !cross;
     const int tb = first[u];
     const int tc = leaf ? (last[u] - first[u] + 1) : 0;
-    warp_append(leaf_count, leaf);  // counts the leaves (one atomic per warp)
     Coeffs c;
     StageRec R;
     if (!cross) {
@@ -2033,13 +2080,13 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
             int* hist = (int*)track(dalloc<int>(kMaxHeight, st));
             int* order = (int*)track(dalloc<int>(count, st));
             FWN_CUDA_CHECK(cudaMemsetAsync(hist, 0, kMaxHeight * sizeof(int), st));
-            k_height_hist<<<grid_for(count, 256), 256, 0, st>>>(count, keys, first, last, flags, key,
+            k_height_hist<<<grid_for(count, 1024), 1024, 0, st>>>(count, keys, first, last, flags, key,
                                                                 hist, status);
             std::vector<int> h_hist(kMaxHeight);
             FWN_CUDA_CHECK(cudaMemcpyAsync(h_hist.data(), hist, kMaxHeight * sizeof(int),
                                            cudaMemcpyDeviceToHost, st));
             k_height_offsets<<<1, 32, 0, st>>>(hist);
-            k_height_sort<<<grid_for(count, 256), 256, 0, st>>>(count, keys, first, last, flags, key,
+            k_height_sort<<<grid_for(count, 1024), 1024, 0, st>>>(count, keys, first, last, flags, key,
                                                                 hist, order);
             FWN_CUDA_CHECK(cudaStreamSynchronize(st));
             std::vector<int> off(kMaxHeight + 1, 0);
