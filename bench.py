@@ -9,6 +9,9 @@ A step = one winding-number query pass over the 10M points against the built tre
              CUDA events on the launching stream, L2 flushed before every step)
   e2e        the same metric through the C ABI's host-buffer call fwn_query_host (pinned host
              buffers; H2D of the points and D2H of Omega + inside inside the timed region)
+  e2e_stream the same through fwn_query_host_batches: one call over K batches (a serving loop),
+             each batch's copies overlapping the walk of its neighbour; every copy is inside the
+             timed region
   plain_fp64 the plain FP64 form (FP64 everywhere, same tree), its queries/s and the max / RMS
              |dw| between the two forms over all queries (gate: <= 1e-4)
   roofline   FP32 roofline of the traversal kernel: algorithmic flops from device work
@@ -893,6 +896,31 @@ def run_ours(args, rank, world, local):
                          "unit": "queries/s",
                          "h2d_bytes_per_step": ne * 12, "d2h_bytes_per_step": ne * 5,
                          "ms_per_step": e2e_s * 1e3, "api": "fwn_query_host (pinned host buffers)"}
+
+        # a serving loop: K batches in one fwn_query_host_batches call, batch b's copy in and
+        # batch b - 1's copy out overlapping the walk between them (host wall clock, all copies
+        # inside; the same pinned points each batch, results into the same pinned buffers)
+        kb = max(3, args.steps)
+        pts = (C.c_void_p * kb)(*([Qh.data_ptr()] * kb))
+        cnt = (C.c_int64 * kb)(*([ne] * kb))
+        pw = (C.c_void_p * kb)(*([wh.data_ptr()] * kb))
+        pi = (C.c_void_p * kb)(*([ih.data_ptr()] * kb))
+
+        def stream_call(k):
+            fwn._check(L.fwn_query_host_batches(eng.handle, k, pts, cnt, pw, pi))
+        stream_call(2)
+        barrier(dist)
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        stream_call(kb)
+        st_s = max_over_ranks(dist, (time.perf_counter() - t0) / kb, dev)
+        result["e2e_stream"] = {
+            "value": (n / st_s) if args.split_queries else job_value(n, world, st_s),
+            "unit": "queries/s", "batches": kb, "ms_per_step": st_s * 1e3,
+            "h2d_bytes_per_step": ne * 12, "d2h_bytes_per_step": ne * 5,
+            "api": "fwn_query_host_batches (pinned host buffers, one batch per step; host "
+                   "wall clock over the whole call)"}
 
     # ---- CPU baseline (rank 0, N=1 only) -----------------------------------------------------
     if rank == 0 and world == 1 and not args.no_cpu:

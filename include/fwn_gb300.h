@@ -217,6 +217,19 @@ FWN_API fwn_status fwn_query_order(fwn_handle h, const float* d_points, int64_t 
 FWN_API fwn_status fwn_query_host(fwn_handle h, const float* points, int64_t n,
                                   float* omega, uint8_t* inside);
 
+/* No counterpart in the reference (a serving loop over many point sets). Queries num_batches
+ * HOST batches: batch b is points[b] ([counts[b] x 3] float), its results go to omega[b] and
+ * inside[b] (either array, or any entry of one, may be NULL). Each batch's results equal
+ * fwn_query_host on it. Batch b is copied in while batch b - 1 is queried and batch b - 1's
+ * results are copied out while batch b is queried (two device slots, the library's per-thread
+ * copy streams), so that for batches of millions of points the host link hides behind the walk;
+ * the copies overlap only from pinned host memory (pageable buffers are staged by the driver and
+ * serialise). The walk's device-side consistency check is read back after the last batch.
+ * Synchronous: returns when every batch's results are in host memory. */
+FWN_API fwn_status fwn_query_host_batches(fwn_handle h, int64_t num_batches,
+                                          const float* const* points, const int64_t* counts,
+                                          float* const* omega, uint8_t* const* inside);
+
 /* No counterpart in the reference. Same result as fwn_query with the handle's defaults, but it
  * allocates nothing: for callers that must not allocate device memory while they query (a
  * voxelizer or renderer working under a fixed per-frame device budget, or code where a

@@ -86,7 +86,7 @@ _lib = None
 # every entry point declared in include/fwn_gb300.h
 EXPORTS = ["fwn_config_default", "fwn_last_error", "fwn_version", "fwn_build", "fwn_build_device",
            "fwn_destroy", "fwn_get_info", "fwn_query", "fwn_query_ex", "fwn_query_host",
-           "fwn_export_tree", "fwn_export_moments", "fwn_export_nodes", "fwn_forest_build",
+           "fwn_query_host_batches", "fwn_export_tree", "fwn_export_moments", "fwn_export_nodes", "fwn_forest_build",
            "fwn_forest_build_device", "fwn_forest_query", "fwn_query_noalloc", "fwn_autotune",
            "fwn_query_grid", "fwn_orientation_criterion", "fwn_query_order",
            "fwn_forest_autotune", "fwn_forest_sort_key_bits", "fwn_probe_fp32_peak",
@@ -118,6 +118,7 @@ def library():
     L.fwn_query_ex.argtypes = [P, C.POINTER(fwn_query_opts), P, i64, P, P, P,
                                C.POINTER(fwn_query_stats), P]
     L.fwn_query_host.argtypes = [P, P, i64, P, P]
+    L.fwn_query_host_batches.argtypes = [P, i64, P, P, P, P]
     L.fwn_query_order.argtypes = [P, P, i64, P, P]
     L.fwn_export_tree.argtypes = [P, P, P, P, P, P, P]
     L.fwn_export_moments.argtypes = [P, P]
@@ -140,7 +141,8 @@ def library():
     L.fwn_save.argtypes = [P, C.c_char_p]
     L.fwn_load.argtypes = [C.c_char_p, C.POINTER(P)]
     for name in ("fwn_build", "fwn_build_device", "fwn_destroy", "fwn_get_info", "fwn_query",
-                 "fwn_query_ex", "fwn_query_host", "fwn_export_tree", "fwn_export_moments", "fwn_export_nodes",
+                 "fwn_query_ex", "fwn_query_host", "fwn_query_host_batches", "fwn_export_tree",
+                 "fwn_export_moments", "fwn_export_nodes",
                  "fwn_forest_build", "fwn_forest_build_device", "fwn_forest_query",
                  "fwn_query_noalloc", "fwn_autotune", "fwn_query_grid",
                  "fwn_orientation_criterion", "fwn_query_order", "fwn_forest_autotune",
@@ -355,6 +357,41 @@ class FastWindingNumber:
                          stream=stream)
         torch.cuda.synchronize()
         return tuple(r.cpu().numpy() if hasattr(r, "cpu") else r for r in res)
+
+    def query_host_batches(self, batches, omega=True, inside=True):
+        """Queries a list of host point sets ([n_b, 3] float32 numpy arrays or CPU tensors) in
+        one call (fwn_query_host_batches): batch b's copy in and batch b - 1's copy out overlap
+        the walk of the batch between them. Returns a list of (omega, inside) per batch, each
+        as fwn_query_host returns it, in the input's kind (numpy, or CPU tensors; pinned when
+        the input is pinned, which the copies need to overlap)."""
+        L = library()
+        nb = len(batches)
+        ins_, outs = [], []
+        for b in batches:
+            if hasattr(b, "is_pinned"):
+                import torch
+                Q = b.detach().to(torch.float32).contiguous().reshape(-1, 3)
+                if Q.is_cuda:
+                    raise ValueError("query_host_batches takes host point sets")
+                pin = Q.is_pinned()
+                mk = (lambda n, dt: torch.empty(n, dtype=dt).pin_memory()) if pin else \
+                    (lambda n, dt: torch.empty(n, dtype=dt))
+                w = mk(Q.shape[0], torch.float32) if omega else None
+                i = mk(Q.shape[0], torch.uint8) if inside else None
+                ptr = lambda t: t.data_ptr() if t is not None else None  # noqa: E731
+            else:
+                Q = np.ascontiguousarray(np.asarray(b), dtype=np.float32).reshape(-1, 3)
+                w = np.empty(len(Q), np.float32) if omega else None
+                i = np.empty(len(Q), np.uint8) if inside else None
+                ptr = lambda t: t.ctypes.data if t is not None else None  # noqa: E731
+            ins_.append(Q)
+            outs.append((w, i, ptr(Q), ptr(w), ptr(i)))
+        pts = (C.c_void_p * max(nb, 1))(*[o[2] for o in outs])
+        cnt = (C.c_int64 * max(nb, 1))(*[int(q.shape[0]) for q in ins_])
+        pw = (C.c_void_p * max(nb, 1))(*[o[3] for o in outs]) if omega else None
+        pi = (C.c_void_p * max(nb, 1))(*[o[4] for o in outs]) if inside else None
+        _check(L.fwn_query_host_batches(self._h, nb, pts, cnt, pw, pi))
+        return [(o[0], o[1]) for o in outs]
 
     def query_order(self, points, stream=None):
         """The permutation the query applies to group nearby points into warps (int64 CUDA

@@ -138,23 +138,27 @@ struct OwnedStream {
     }
 };
 
-// The stream of the synchronous host-buffer queries: one non-blocking stream per (host thread,
+// The streams of the synchronous host-buffer queries: non-blocking streams per (host thread,
 // device), created on first use and kept for the thread's lifetime; creating and destroying a
-// stream on every call costs more than a small query.
-cudaStream_t host_stream() {
+// stream on every call costs more than a small query. Stream 0 runs the queries; 1 and 2 copy
+// batches in and out while stream 0 works (fwn_query_host_batches).
+constexpr int kHostStreams = 3;
+
+cudaStream_t host_stream(int k = 0) {
     struct Streams {
-        cudaStream_t s[kMaxDevices] = {};
+        cudaStream_t s[kMaxDevices][kHostStreams] = {};
         ~Streams() {
-            for (cudaStream_t x : s)
-                if (x) cudaStreamDestroy(x);
+            for (auto& d : s)
+                for (cudaStream_t x : d)
+                    if (x) cudaStreamDestroy(x);
         }
     };
     thread_local Streams t;
     int dev = 0;
     FWN_CUDA_CHECK(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices) throw Error(FWN_INTERNAL, "device ordinal out of range");
-    if (!t.s[dev]) FWN_CUDA_CHECK(cudaStreamCreateWithFlags(&t.s[dev], cudaStreamNonBlocking));
-    return t.s[dev];
+    if (!t.s[dev][k]) FWN_CUDA_CHECK(cudaStreamCreateWithFlags(&t.s[dev][k], cudaStreamNonBlocking));
+    return t.s[dev][k];
 }
 
 Engine* engine_of(fwn_handle h) {
@@ -353,6 +357,74 @@ FWN_API fwn_status fwn_query_host(fwn_handle h, const float* points, int64_t n, 
         if (omega) FWN_CUDA_CHECK(cudaMemcpyAsync(omega, dw.p, n * sizeof(float), cudaMemcpyDeviceToHost, st));
         if (inside) FWN_CUDA_CHECK(cudaMemcpyAsync(inside, di.p, n, cudaMemcpyDeviceToHost, st));
         FWN_CUDA_CHECK(cudaStreamSynchronize(st));
+    });
+}
+
+FWN_API fwn_status fwn_query_host_batches(fwn_handle h, int64_t num_batches,
+                                          const float* const* points, const int64_t* counts,
+                                          float* const* omega, uint8_t* const* inside) {
+    return guarded([&] {
+        Engine* e = engine_of(h);
+        require_engine_device(*e);
+        if (e->nmeshes != 1) throw Error(FWN_INVALID_ARG, "forest handle: use fwn_forest_query");
+        if (num_batches < 0) throw Error(FWN_INVALID_ARG, "num_batches must be >= 0");
+        if (num_batches == 0) return;
+        if (!points || !counts) throw Error(FWN_INVALID_ARG, "points or counts is null");
+        int64_t nmax = 0;
+        for (int64_t b = 0; b < num_batches; ++b) {
+            check_points(counts[b], points[b]);
+            nmax = std::max(nmax, counts[b]);
+        }
+        if (nmax == 0) return;
+        QueryArgs a = resolve_query_args(*e, nullptr);
+        const cudaStream_t st = host_stream(0), in_st = host_stream(1), out_st = host_stream(2);
+        // two device slots: batch b copies into slot b % 2 while batch b - 1 runs in the other
+        Scratch dq[2] = {Scratch(nmax * 3 * sizeof(float), st), Scratch(nmax * 3 * sizeof(float), st)};
+        Scratch dw[2] = {Scratch(omega ? nmax * sizeof(float) : 0, st),
+                         Scratch(omega ? nmax * sizeof(float) : 0, st)};
+        Scratch di[2] = {Scratch(inside ? nmax : 0, st), Scratch(inside ? nmax : 0, st)};
+        cudaEvent_t ev[7];  // slot buffers ready, batch in (x2), query done (x2), batch out (x2)
+        for (cudaEvent_t& x : ev) FWN_CUDA_CHECK(cudaEventCreateWithFlags(&x, cudaEventDisableTiming));
+        std::unique_ptr<cudaEvent_t[], void (*)(cudaEvent_t*)> guard(
+            new cudaEvent_t[7]{ev[0], ev[1], ev[2], ev[3], ev[4], ev[5], ev[6]}, [](cudaEvent_t* p) {
+                for (int i = 0; i < 7; ++i) cudaEventDestroy(p[i]);
+                delete[] p;
+            });
+        cudaEvent_t ready = ev[0], in_done[2] = {ev[1], ev[2]}, q_done[2] = {ev[3], ev[4]},
+                    out_done[2] = {ev[5], ev[6]};
+        FWN_CUDA_CHECK(cudaEventRecord(ready, st));  // the slots' stream-ordered allocations
+        FWN_CUDA_CHECK(cudaStreamWaitEvent(in_st, ready, 0));
+        FWN_CUDA_CHECK(cudaStreamWaitEvent(out_st, ready, 0));
+        for (int64_t b = 0; b < num_batches; ++b) {
+            const int s = (int)(b & 1);
+            const int64_t n = counts[b];
+            if (b >= 2) {  // slot s was batch b - 2's: its points are read, its results out
+                FWN_CUDA_CHECK(cudaStreamWaitEvent(in_st, q_done[s], 0));
+                FWN_CUDA_CHECK(cudaStreamWaitEvent(st, out_done[s], 0));
+            }
+            if (n > 0)
+                FWN_CUDA_CHECK(cudaMemcpyAsync(dq[s].p, points[b], n * 3 * sizeof(float),
+                                               cudaMemcpyHostToDevice, in_st));
+            FWN_CUDA_CHECK(cudaEventRecord(in_done[s], in_st));
+            FWN_CUDA_CHECK(cudaStreamWaitEvent(st, in_done[s], 0));
+            // the walk's consistency check (a corrupt tree shows in every batch) is read back
+            // once, on the last batch, so that no batch waits for the host
+            query_mesh(*e, 0, a, dq[s].as<float>(), n, dw[s].as<float>(), di[s].as<uint8_t>(),
+                       nullptr, nullptr, st, /*check=*/b == num_batches - 1);
+            FWN_CUDA_CHECK(cudaEventRecord(q_done[s], st));
+            FWN_CUDA_CHECK(cudaStreamWaitEvent(out_st, q_done[s], 0));
+            if (n > 0 && omega && omega[b])
+                FWN_CUDA_CHECK(cudaMemcpyAsync(omega[b], dw[s].p, n * sizeof(float),
+                                               cudaMemcpyDeviceToHost, out_st));
+            if (n > 0 && inside && inside[b])
+                FWN_CUDA_CHECK(cudaMemcpyAsync(inside[b], di[s].p, n, cudaMemcpyDeviceToHost, out_st));
+            FWN_CUDA_CHECK(cudaEventRecord(out_done[s], out_st));
+        }
+        FWN_CUDA_CHECK(cudaStreamSynchronize(out_st));
+        FWN_CUDA_CHECK(cudaStreamSynchronize(in_st));
+        // the slots are freed on stream 0 (stream-ordered) after every copy that used them
+        FWN_CUDA_CHECK(cudaStreamWaitEvent(st, out_done[0], 0));
+        FWN_CUDA_CHECK(cudaStreamWaitEvent(st, out_done[1], 0));
     });
 }
 

@@ -66,6 +66,7 @@ def test_invalid_arguments_rejected_on_host(engine_lib):
 def test_null_handle_is_not_built(engine_lib):
     st = engine_lib.fwn_query_host(None, None, 0, None, None)
     assert st == 6
+    assert engine_lib.fwn_query_host_batches(None, 0, None, None, None, None) == 6
     eng = fwn.FastWindingNumber()
     with pytest.raises(fwn.WindingError) as e:
         eng.solid_angle(np.zeros(3, np.float32))

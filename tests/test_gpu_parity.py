@@ -706,3 +706,29 @@ def test_forest_many_ragged_meshes(torch_cuda, oracle_mod, builder):
     np.testing.assert_allclose(w, ref, rtol=2e-7, atol=1e-5 * FOUR_PI)
     empty = np.repeat(np.arange(3000) % 5 == 0, np.diff(qoff))
     assert np.all(w[empty] == 0) and not ins[empty].any()
+
+
+def test_query_host_batches_equal_single_calls(torch_cuda):
+    """fwn_query_host_batches (batch b copied in while batch b - 1 is queried, its results copied
+    out during batch b + 1) returns for every batch exactly what fwn_query_host returns for it:
+    batches of varying size including an empty one and a single point, from numpy arrays and
+    from pinned tensors, and with one output left out."""
+    torch = torch_cuda
+    g = np.load(GOLDEN / "displaced.npz")
+    eng = _engine(g["V"], g["F"], leaf_size=8, builder=1, records=fwn.RECORDS_F32)
+    rng = np.random.default_rng(8)
+    lo, hi = g["V"].min(0), g["V"].max(0)
+    batches = [rng.uniform(lo - 0.2, hi + 0.2, size=(k, 3)).astype(np.float32)
+               for k in (5000, 0, 1, 70000, 3, 20000)]
+    ref = [eng.query(b) for b in batches]  # numpy points: one fwn_query_host call each
+    as_np = lambda x: x.numpy() if hasattr(x, "numpy") else x  # noqa: E731
+    for inp in (batches, [torch.from_numpy(b).pin_memory() for b in batches]):
+        out = eng.query_host_batches(inp)
+        assert len(out) == len(batches)
+        for (w, i), (rw, ri) in zip(out, ref):
+            np.testing.assert_array_equal(as_np(w), rw)
+            np.testing.assert_array_equal(as_np(i), ri)
+    for (w, i), (rw, _) in zip(eng.query_host_batches(batches, inside=False), ref):
+        assert i is None
+        np.testing.assert_array_equal(w, rw)
+    assert eng.query_host_batches([]) == []
