@@ -140,9 +140,10 @@ struct OwnedStream {
 
 // The streams of the synchronous host-buffer queries: non-blocking streams per (host thread,
 // device), created on first use and kept for the thread's lifetime; creating and destroying a
-// stream on every call costs more than a small query. Stream 0 runs the queries; 1 and 2 copy
-// batches in and out while stream 0 works (fwn_query_host_batches).
-constexpr int kHostStreams = 3;
+// stream on every call costs more than a small query. Stream 0 runs the queries; in
+// fwn_query_host_batches streams 1 and 2 copy batches in and out, and odd batches run on stream 3
+// (so that a batch's key sort can start while the previous batch's walk finishes).
+constexpr int kHostStreams = 4;
 
 cudaStream_t host_stream(int k = 0) {
     struct Streams {
@@ -378,6 +379,7 @@ FWN_API fwn_status fwn_query_host_batches(fwn_handle h, int64_t num_batches,
         if (nmax == 0) return;
         QueryArgs a = resolve_query_args(*e, nullptr);
         const cudaStream_t st = host_stream(0), in_st = host_stream(1), out_st = host_stream(2);
+        const cudaStream_t qst[2] = {st, host_stream(3)};  // slot s's batches run on qst[s]
         // two device slots: batch b copies into slot b % 2 while batch b - 1 runs in the other
         Scratch dq[2] = {Scratch(nmax * 3 * sizeof(float), st), Scratch(nmax * 3 * sizeof(float), st)};
         Scratch dw[2] = {Scratch(omega ? nmax * sizeof(float) : 0, st),
@@ -395,23 +397,24 @@ FWN_API fwn_status fwn_query_host_batches(fwn_handle h, int64_t num_batches,
         FWN_CUDA_CHECK(cudaEventRecord(ready, st));  // the slots' stream-ordered allocations
         FWN_CUDA_CHECK(cudaStreamWaitEvent(in_st, ready, 0));
         FWN_CUDA_CHECK(cudaStreamWaitEvent(out_st, ready, 0));
+        FWN_CUDA_CHECK(cudaStreamWaitEvent(qst[1], ready, 0));
         for (int64_t b = 0; b < num_batches; ++b) {
             const int s = (int)(b & 1);
             const int64_t n = counts[b];
             if (b >= 2) {  // slot s was batch b - 2's: its points are read, its results out
                 FWN_CUDA_CHECK(cudaStreamWaitEvent(in_st, q_done[s], 0));
-                FWN_CUDA_CHECK(cudaStreamWaitEvent(st, out_done[s], 0));
+                FWN_CUDA_CHECK(cudaStreamWaitEvent(qst[s], out_done[s], 0));
             }
             if (n > 0)
                 FWN_CUDA_CHECK(cudaMemcpyAsync(dq[s].p, points[b], n * 3 * sizeof(float),
                                                cudaMemcpyHostToDevice, in_st));
             FWN_CUDA_CHECK(cudaEventRecord(in_done[s], in_st));
-            FWN_CUDA_CHECK(cudaStreamWaitEvent(st, in_done[s], 0));
+            FWN_CUDA_CHECK(cudaStreamWaitEvent(qst[s], in_done[s], 0));
             // the walk's consistency check (a corrupt tree shows in every batch) is read back
             // once, on the last batch, so that no batch waits for the host
             query_mesh(*e, 0, a, dq[s].as<float>(), n, dw[s].as<float>(), di[s].as<uint8_t>(),
-                       nullptr, nullptr, st, /*check=*/b == num_batches - 1);
-            FWN_CUDA_CHECK(cudaEventRecord(q_done[s], st));
+                       nullptr, nullptr, qst[s], /*check=*/b == num_batches - 1);
+            FWN_CUDA_CHECK(cudaEventRecord(q_done[s], qst[s]));
             FWN_CUDA_CHECK(cudaStreamWaitEvent(out_st, q_done[s], 0));
             if (n > 0 && omega && omega[b])
                 FWN_CUDA_CHECK(cudaMemcpyAsync(omega[b], dw[s].p, n * sizeof(float),
@@ -422,6 +425,7 @@ FWN_API fwn_status fwn_query_host_batches(fwn_handle h, int64_t num_batches,
         }
         FWN_CUDA_CHECK(cudaStreamSynchronize(out_st));
         FWN_CUDA_CHECK(cudaStreamSynchronize(in_st));
+        FWN_CUDA_CHECK(cudaStreamSynchronize(qst[1]));
         // the slots are freed on stream 0 (stream-ordered) after every copy that used them
         FWN_CUDA_CHECK(cudaStreamWaitEvent(st, out_done[0], 0));
         FWN_CUDA_CHECK(cudaStreamWaitEvent(st, out_done[1], 0));
