@@ -174,6 +174,27 @@ public:
         detail::check(fwn_query_host(m_handle, xyz, static_cast<int64_t>(n), nullptr, inside));
     }
 
+    /// A serving loop's host point sets in one call (fwn_query_host_batches): batch b is
+    /// xyz[b] (counts[b] points); omega / inside (either may be null, as may any entry) receive
+    /// its results. Copies of one batch overlap the walk of its neighbour when the buffers are
+    /// pinned.
+    void query_batches(
+        size_t num_batches,
+        const float* const* xyz,
+        const size_t* counts,
+        float* const* omega,
+        uint8_t* const* inside) const
+    {
+        std::vector<int64_t> n(counts, counts + num_batches);
+        detail::check(fwn_query_host_batches(
+            m_handle,
+            static_cast<int64_t>(num_batches),
+            xyz,
+            n.data(),
+            omega,
+            inside));
+    }
+
     /// Batched query on device buffers (asynchronous on `stream`, a cudaStream_t).
     void query_device(
         const float* d_xyz,

@@ -88,6 +88,17 @@ void run_instantiation()
     }
     CHECK(in[0] == 1 && in[1] == 1 && in[2] == 0 && in[3] == 0);
 
+    // several host batches in one call == one call each
+    const float* bx[3] = {pts.data(), pts.data() + 3, pts.data()};
+    const size_t bn[3] = {4, 2, 0};
+    std::vector<float> o0(4), o1(2);
+    std::vector<uint8_t> i0(4), i1(2);
+    float* bo[3] = {o0.data(), o1.data(), nullptr};
+    uint8_t* bi[3] = {i0.data(), i1.data(), nullptr};
+    engine.query_batches(3, bx, bn, bo, bi);
+    for (int i = 0; i < 4; ++i) CHECK(o0[i] == om[i] && i0[i] == in[i]);
+    for (int i = 0; i < 2; ++i) CHECK(o1[i] == om[i + 1] && i1[i] == in[i + 1]);
+
     // move semantics: moved-from objects are empty and throw NOT_BUILT when queried
     FastWindingNumber moved(std::move(engine));
     CHECK(moved.is_inside({0.f, 0.f, 0.f}));
