@@ -394,6 +394,14 @@ FWN_API fwn_status fwn_query_host_batches(fwn_handle h, int64_t num_batches,
             });
         cudaEvent_t ready = ev[0], in_done[2] = {ev[1], ev[2]}, q_done[2] = {ev[3], ev[4]},
                     out_done[2] = {ev[5], ev[6]};
+        // on every exit, an error included, the side streams finish before the slots (freed on
+        // stream 0 when they go out of scope, after this guard) can be reused
+        struct Drain {
+            cudaStream_t s[3];
+            ~Drain() {
+                for (cudaStream_t x : s) cudaStreamSynchronize(x);
+            }
+        } drain{{in_st, out_st, qst[1]}};
         FWN_CUDA_CHECK(cudaEventRecord(ready, st));  // the slots' stream-ordered allocations
         FWN_CUDA_CHECK(cudaStreamWaitEvent(in_st, ready, 0));
         FWN_CUDA_CHECK(cudaStreamWaitEvent(out_st, ready, 0));
