@@ -97,7 +97,7 @@ def parse():
     p.add_argument("--queries", type=int, default=None)
     p.add_argument("--leaf", type=int, default=0)  # 0: the autotuner picks (untimed)
     p.add_argument("--tuning", type=int, default=0)  # with --leaf: warp-schedule variant (0 auto)
-    p.add_argument("--builder", type=int, default=0)  # with --leaf: 0 LBVH, 1 top-down splits
+    p.add_argument("--builder", type=int, default=0)  # with --leaf: 0 LBVH, 1 top-down splits, 2 binned
     p.add_argument("--traversal", default="warp", choices=["thread", "warp"])
     p.add_argument("--block", type=int, default=128)
     p.add_argument("--fp64-steps", type=int, default=2)
@@ -269,6 +269,9 @@ def make_workload(args):
     if args.workload == "uvsphere":
         return W.uv_sphere_workload(n_queries=args.queries or 100_000)
     return W.displaced_icosphere_workload(nu=args.nu or 316, n_queries=args.queries or 10_000_000)
+
+
+BUILDER_NAMES = {0: "lbvh", 1: "split", 2: "binned"}
 
 
 def autotune_choice(fwn, Vd, Fd, Qd, sample: int = 16_000_000, seed: int = 5):
@@ -711,7 +714,7 @@ def run_ours(args, rank, world, local):
         "config": {"workload": wl.name, "triangles": int(len(wl.F)),
                    "queries_per_gpu": n // world if args.split_queries else n,
                    "beta": wl.beta, "leaf_size": args.leaf,
-                   "builder": "split" if builder == fwn.BUILDER_SPLIT else "lbvh",
+                   "builder": BUILDER_NAMES.get(builder, str(builder)),
                    "traversal": "warp" if trav == fwn.TRAVERSAL_WARP else "thread",
                    "block": args.block, "tuning": tuning, "autotuned": tuned,
                    "step": "plain launches" if args.no_graph else "CUDA graph of one query call",
@@ -1129,7 +1132,7 @@ def measure_forest(fo, dev, dist, rank, world, *, leaf=0, builder=0, tuning=0, s
         "data": "synthetic",
         "config": {"workload": fo.name, "meshes": M, "triangles": int(fo.foff[-1]),
                    "queries": n, "beta": fo.beta, "leaf_size": leaf,
-                   "builder": "split" if builder == fwn.BUILDER_SPLIT else "lbvh", "autotuned": tuned,
+                   "builder": BUILDER_NAMES.get(builder, str(builder)), "autotuned": tuned,
                    "l2": "flushed before every step (256 MB write)"},
         "build_ms": build_ms, "tree_nodes": forest.info()["num_nodes"],
         "meshes_per_s_build_plus_query": M / ((build_ms + ms) / 1e3),

@@ -19,14 +19,14 @@ import numpy as np
 __all__ = ["FastWindingNumber", "Forest", "WindingError", "library", "config_default", "autotune",
            "PRECISION_MIXED", "PRECISION_FP64", "TRAVERSAL_AUTO", "TRAVERSAL_THREAD",
            "TRAVERSAL_WARP", "RECORDS_F32", "RECORDS_F64", "RECORDS_MOMENTS", "BUILDER_LBVH",
-           "BUILDER_SPLIT"]
+           "BUILDER_SPLIT", "BUILDER_BINNED"]
 
 LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libfwn_gb300.so"
 
 PRECISION_MIXED, PRECISION_FP64 = 0, 1
 TRAVERSAL_AUTO, TRAVERSAL_THREAD, TRAVERSAL_WARP = 0, 1, 2
 RECORDS_F32, RECORDS_F64, RECORDS_MOMENTS = 1, 2, 4
-BUILDER_LBVH, BUILDER_SPLIT = 0, 1
+BUILDER_LBVH, BUILDER_SPLIT, BUILDER_BINNED = 0, 1, 2
 
 STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA_ERROR", 4: "TIMEOUT", 5: "INTERNAL",
           6: "NOT_BUILT"}

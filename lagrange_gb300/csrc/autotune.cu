@@ -38,7 +38,10 @@ const Candidate kCandidates[] = {
     {FWN_TRAVERSAL_THREAD, 256, 0},
 };
 const int kLeafSizes[] = {4, 8, 12, 16};
-const int kBuilders[] = {FWN_BUILDER_LBVH, FWN_BUILDER_SPLIT};
+// One mesh (queried many times) tries all three builders; a forest, built for each batch, the two
+// whose build suits that (the binned splits add a binning pass per level for ~2% on the query).
+const int kBuilders[] = {FWN_BUILDER_LBVH, FWN_BUILDER_SPLIT, FWN_BUILDER_BINNED};
+const int kForestBuilders[] = {FWN_BUILDER_LBVH, FWN_BUILDER_SPLIT};
 
 std::mutex g_cache_mutex;
 
@@ -78,7 +81,8 @@ bool cache_lookup(const char* path, const std::string& key, fwn_tune_result* out
         if (r.leaf_size < 1 || r.leaf_size > 16 || r.traversal < FWN_TRAVERSAL_AUTO ||
             r.traversal > FWN_TRAVERSAL_WARP || r.block_size < 0 || r.block_size > 1024 ||
             r.block_size % 32 != 0 || r.tuning < 0 || r.tuning > 6 ||
-            (r.builder != FWN_BUILDER_LBVH && r.builder != FWN_BUILDER_SPLIT))
+            (r.builder != FWN_BUILDER_LBVH && r.builder != FWN_BUILDER_SPLIT &&
+             r.builder != FWN_BUILDER_BINNED))
             continue;
         if (k == key) {
             r.from_cache = 1;
@@ -234,7 +238,7 @@ extern "C" FWN_API fwn_status fwn_forest_autotune(const float* d_V, const int64_
         std::memset(&best, 0, sizeof(best));
         best.ms = 1e300;
         int evaluated = 0;
-        for (int builder : kBuilders)
+        for (int builder : kForestBuilders)
         for (int leaf : kLeafSizes) {
             Engine e;
             e.cfg = cfg;

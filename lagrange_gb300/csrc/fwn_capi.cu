@@ -213,8 +213,10 @@ void validate_config(const fwn_config& c) {
     if (!(c.fp64_cond >= 0.f) || !std::isfinite(c.fp64_cond))
         throw Error(FWN_INVALID_ARG, "fp64_cond must be finite and >= 0");
     if (c.tuning < 0 || c.tuning > 7) throw Error(FWN_INVALID_ARG, "tuning must be in [0, 7]");
-    if (c.builder != FWN_BUILDER_LBVH && c.builder != FWN_BUILDER_SPLIT)
-        throw Error(FWN_INVALID_ARG, "builder must be FWN_BUILDER_LBVH or FWN_BUILDER_SPLIT");
+    if (c.builder != FWN_BUILDER_LBVH && c.builder != FWN_BUILDER_SPLIT &&
+        c.builder != FWN_BUILDER_BINNED)
+        throw Error(FWN_INVALID_ARG,
+                    "builder must be FWN_BUILDER_LBVH, FWN_BUILDER_SPLIT or FWN_BUILDER_BINNED");
 }
 
 }  // namespace fwn

@@ -15,8 +15,9 @@
 //       tree: its levels; LBVH: node heights from an integer atomic-counter ascent)
 //   K4a exact node radii (farthest vertex, float screen + FP64 terms for the candidates), then
 //       conversion to 128 B FP32 / 256 B FP64 records in DFS order
-// The alternative top-down builder (FWN_BUILDER_SPLIT) replaces K1-K3b with level-synchronous
-// midpoint splits of each segment's centroid box and shares K4-K4a.
+// The alternative top-down builders (FWN_BUILDER_SPLIT, FWN_BUILDER_BINNED) replace K1-K3b with
+// level-synchronous splits of each segment's centroid box (its midpoint; or, for the binned
+// builder and segments of the level loop, the binned plane of least cost) and share K4-K4a.
 //
 // This translation unit is compiled with -fmad=false: every floating-point operation is
 // individually rounded, in the order written, so the CPU restatement of the same build
@@ -365,6 +366,20 @@ constexpr int kSpatialLevels = 96;
 // subtrees in shared memory (k_split_finish), with the same splits.
 constexpr int kFinishSlots = 1024;
 constexpr int kFinishThreads = 512;
+// Segments of the level loop (more than kFinishSlots triangles) split at a binned plane: kSplitBins
+// bins per axis over the centroid box, bin(x) = min((int)((x - lo) / ext * 16), 15) in float, and
+// the plane with the least nL * dL + nR * dR (d = squared diagonal of a side's centroid bounds, in
+// double); ties go to the lower axis, then the lower plane; left = bin <= plane. A bin holds its
+// count and its centroid bounds (ordered-int encodings): kBinWords words.
+constexpr int kSplitBins = 16;
+constexpr int kBinWords = 7;
+constexpr int kSegBinWords = 3 * kSplitBins * kBinWords;  // 336 per segment
+constexpr int kBinChunk = 2048;  // slots per block of k_split_bins: at most 3 level-loop segments
+
+__device__ __forceinline__ int split_bin(float x, float lo, float ext) {
+    const int b = (int)((x - lo) / ext * (float)kSplitBins);
+    return b < 0 ? 0 : (b > kSplitBins - 1 ? kSplitBins - 1 : b);
+}
 
 struct SplitSlots {
     int* perm;  // triangle id per slot
@@ -540,7 +555,7 @@ __device__ __forceinline__ void split_decide(const unsigned* __restrict__ box, i
 
 __global__ void k_split_decide(int nact, bool by_position, const unsigned* __restrict__ box,
                                int* __restrict__ axis_of, float* __restrict__ split_of,
-                               int* __restrict__ spatial_of) {
+                               int* __restrict__ spatial_of, float* __restrict__ seg_box) {
     const int sg = blockIdx.x * blockDim.x + threadIdx.x;
     if (sg >= nact) return;
     unsigned b[6];
@@ -557,19 +572,254 @@ __global__ void k_split_decide(int nact, bool by_position, const unsigned* __res
         }
     }
     split_decide(b, 1, by_position, axis_of[sg], split_of[sg], spatial_of[sg]);
+#pragma unroll
+    for (int a = 0; a < 6; ++a) seg_box[6 * sg + a] = dec_float(b[a]);  // lo[3], hi[3]
+}
+
+__global__ void k_split_bins_init(int nwords, unsigned* __restrict__ bins) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nwords) return;
+    const int w = i % kBinWords;
+    bins[i] = w == 0 ? 0u : (w < 4 ? 0xffffffffu : 0u);  // count, lo (min of nothing), hi
+}
+
+// Per-segment bins of one level: a block takes kBinChunk consecutive slots, which meet at most
+// three of the level's segments (each holds more than kFinishSlots), accumulates their bins in
+// shared memory, then adds the non-empty ones to the segments' global bins.
+__global__ void __launch_bounds__(256) k_split_bins(int64_t n, SplitSlots cur,
+                                                    const float* __restrict__ seg_box,
+                                                    unsigned* __restrict__ bins) {
+    constexpr int kLocal = 4;
+    __shared__ int tab[kLocal];
+    __shared__ int ntab;
+    __shared__ unsigned sb[kLocal * kSegBinWords];
+    for (int i = threadIdx.x; i < kLocal * kSegBinWords; i += blockDim.x) {
+        const int w = i % kBinWords;
+        sb[i] = w == 0 ? 0u : (w < 4 ? 0xffffffffu : 0u);
+    }
+    if (threadIdx.x < kLocal) tab[threadIdx.x] = -1;
+    if (threadIdx.x == 0) ntab = 0;
+    __syncthreads();
+    const int64_t c0 = (int64_t)blockIdx.x * kBinChunk;
+    // a segment's slots are one run of positions: the run's first slot in the chunk claims the
+    // segment's local bins
+    for (int r = 0; r < kBinChunk / 256; ++r) {
+        const int64_t i = c0 + r * 256 + threadIdx.x;
+        if (i >= n) break;
+        const int sg = cur.seg[i];
+        if (sg >= 0 && (i == c0 || cur.seg[i - 1] != sg)) {
+            const int k = atomicAdd(&ntab, 1);
+            if (k < kLocal) tab[k] = sg;
+        }
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    for (int r = 0; r < kBinChunk / 256; ++r) {  // uniform trip count: every lane takes part
+        const int64_t i = c0 + r * 256 + threadIdx.x;
+        const int sg = i < n ? cur.seg[i] : -1;
+        int slot = -1;
+        if (sg >= 0)
+#pragma unroll
+            for (int k = 0; k < kLocal; ++k)
+                if (tab[k] == sg) slot = k;  // at most three segments meet a chunk
+        float c[3] = {0.f, 0.f, 0.f};
+        if (slot >= 0) {
+            c[0] = cur.cx[i];
+            c[1] = cur.cy[i];
+            c[2] = cur.cz[i];
+        }
+        const unsigned ec[3] = {enc_float(c[0]), enc_float(c[1]), enc_float(c[2])};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            // lanes adding to the same bin reduce together; one atomic per bin and word
+            int key = -1;
+            if (slot >= 0) {
+                const float lo = seg_box[6 * sg + a], ext = seg_box[6 * sg + 3 + a] - lo;
+                if (ext > 0.f) key = (slot * 3 + a) * kSplitBins + split_bin(c[a], lo, ext);
+            }
+            const unsigned act = __ballot_sync(0xffffffffu, key >= 0);
+            if (key >= 0) {
+                const unsigned peers = __match_any_sync(act, key);
+                const bool leader = lane == __ffs(peers) - 1;
+                unsigned lo3[3], hi3[3];
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    lo3[d] = __reduce_min_sync(peers, ec[d]);
+                    hi3[d] = __reduce_max_sync(peers, ec[d]);
+                }
+                if (leader) {
+                    unsigned* bw = sb + key * kBinWords;
+                    atomicAdd(&bw[0], (unsigned)__popc(peers));
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        atomicMin(&bw[1 + d], lo3[d]);
+                        atomicMax(&bw[4 + d], hi3[d]);
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+    for (int slot = 0; slot < kLocal; ++slot) {
+        const int sg = tab[slot];
+        if (sg < 0) continue;
+        const unsigned* src = sb + slot * kSegBinWords;
+        unsigned* dst = bins + (int64_t)sg * kSegBinWords;
+        for (int k = threadIdx.x; k < 3 * kSplitBins; k += blockDim.x) {
+            const unsigned* bw = src + k * kBinWords;
+            if (!bw[0]) continue;
+            atomicAdd(&dst[k * kBinWords], bw[0]);
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                atomicMin(&dst[k * kBinWords + 1 + d], bw[1 + d]);
+                atomicMax(&dst[k * kBinWords + 4 + d], bw[4 + d]);
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ double split_diag2(const float* lo, const float* hi) {
+    double t = 0.0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const double d = (double)hi[a] - (double)lo[a];
+        t = t + d * d;
+    }
+    return t;
+}
+
+// The binned plane of each segment (when some axis has extent): spatial_of = 2, axis_of, bin_of.
+// One warp per segment: lane k holds bin k of an axis, the left sides are inclusive prefix scans
+// over the lanes and the right sides suffix scans (min, max and integer counts are exact in any
+// order), lane j prices plane j, and the warp keeps the least (cost, axis, plane), the first
+// minimum in axis-then-plane order.
+__device__ __forceinline__ void bin_scan_up(unsigned& n, float (&lo)[3], float (&hi)[3], int lane) {
+#pragma unroll
+    for (int o = 1; o < kSplitBins; o <<= 1) {
+        const unsigned m = __shfl_up_sync(0xffffffffu, n, o);
+        float l[3], h[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            l[d] = __shfl_up_sync(0xffffffffu, lo[d], o);
+            h[d] = __shfl_up_sync(0xffffffffu, hi[d], o);
+        }
+        if (lane >= o) {
+            n += m;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                lo[d] = fminf(lo[d], l[d]);
+                hi[d] = fmaxf(hi[d], h[d]);
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void bin_scan_down(unsigned& n, float (&lo)[3], float (&hi)[3], int lane) {
+#pragma unroll
+    for (int o = 1; o < kSplitBins; o <<= 1) {
+        const unsigned m = __shfl_down_sync(0xffffffffu, n, o);
+        float l[3], h[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            l[d] = __shfl_down_sync(0xffffffffu, lo[d], o);
+            h[d] = __shfl_down_sync(0xffffffffu, hi[d], o);
+        }
+        if (lane + o < kSplitBins) {
+            n += m;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                lo[d] = fminf(lo[d], l[d]);
+                hi[d] = fmaxf(hi[d], h[d]);
+            }
+        }
+    }
+}
+
+__global__ void k_split_choose(int nact, const float* __restrict__ seg_box,
+                               const unsigned* __restrict__ bins, int* __restrict__ axis_of,
+                               int* __restrict__ bin_of, int* __restrict__ spatial_of) {
+    const int sg = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (sg >= nact) return;  // warp-uniform
+    const unsigned* sgb = bins + (int64_t)sg * kSegBinWords;
+    double best = INFINITY;
+    int best_a = 3, best_j = kSplitBins;
+    for (int a = 0; a < 3; ++a) {
+        if (!(seg_box[6 * sg + 3 + a] - seg_box[6 * sg + a] > 0.f)) continue;  // warp-uniform
+        unsigned n = 0;
+        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        if (lane < kSplitBins) {
+            const unsigned* bw = sgb + (a * kSplitBins + lane) * kBinWords;
+            n = bw[0];
+            if (n) {  // an empty bin's bounds are the identity
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    lo[d] = dec_float(bw[1 + d]);
+                    hi[d] = dec_float(bw[4 + d]);
+                }
+            }
+        }
+        unsigned nL = n, nR = n;
+        float Llo[3], Lhi[3], Rlo[3], Rhi[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            Llo[d] = Rlo[d] = lo[d];
+            Lhi[d] = Rhi[d] = hi[d];
+        }
+        bin_scan_up(nL, Llo, Lhi, lane);    // bins 0..lane
+        bin_scan_down(nR, Rlo, Rhi, lane);  // bins lane..15
+        // plane j = lane: left = bins 0..j, right = bins j+1..15 (the next lane's suffix)
+        const unsigned nRn = __shfl_down_sync(0xffffffffu, nR, 1);
+        float rlo[3], rhi[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            rlo[d] = __shfl_down_sync(0xffffffffu, Rlo[d], 1);
+            rhi[d] = __shfl_down_sync(0xffffffffu, Rhi[d], 1);
+        }
+        if (lane < kSplitBins - 1 && nL > 0 && nRn > 0) {
+            const double cost = (double)nL * split_diag2(Llo, Lhi) + (double)nRn * split_diag2(rlo, rhi);
+            if (cost < best) {  // axes in order: a lane keeps its first minimum
+                best = cost;
+                best_a = a;
+                best_j = lane;
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {  // least (cost, axis, plane) over the lanes
+        const double c2 = __shfl_xor_sync(0xffffffffu, best, o);
+        const int a2 = __shfl_xor_sync(0xffffffffu, best_a, o);
+        const int j2 = __shfl_xor_sync(0xffffffffu, best_j, o);
+        if (c2 < best || (c2 == best && (a2 < best_a || (a2 == best_a && j2 < best_j)))) {
+            best = c2;
+            best_a = a2;
+            best_j = j2;
+        }
+    }
+    if (lane == 0 && best_a < 3) {
+        axis_of[sg] = best_a;
+        bin_of[sg] = best_j;
+        spatial_of[sg] = 2;
+    }
 }
 
 __global__ void k_split_flags(int64_t n, SplitSlots cur, const int* __restrict__ s_start,
                               const int* __restrict__ s_end, const int* __restrict__ axis_of,
                               const float* __restrict__ split_of,
-                              const int* __restrict__ spatial_of, int* __restrict__ flags) {
+                              const int* __restrict__ spatial_of, const int* __restrict__ bin_of,
+                              const float* __restrict__ seg_box, int* __restrict__ flags) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i > n) return;
     int f = 0;
     if (i < n) {
         const int sg = cur.seg[i];
         if (sg >= 0) {
-            if (spatial_of[sg]) {
+            if (spatial_of[sg] == 2) {
+                const int a = axis_of[sg];
+                const float c = a == 0 ? cur.cx[i] : a == 1 ? cur.cy[i] : cur.cz[i];
+                const float lo = seg_box[6 * sg + a], ext = seg_box[6 * sg + 3 + a] - lo;
+                f = split_bin(c, lo, ext) <= bin_of[sg] ? 1 : 0;
+            } else if (spatial_of[sg]) {
                 const int a = axis_of[sg];
                 const float c = a == 0 ? cur.cx[i] : a == 1 ? cur.cy[i] : cur.cz[i];
                 f = c < split_of[sg] ? 1 : 0;
@@ -1810,7 +2060,8 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
 
     if (nf > 0) {
         const int n = (int)nf;
-        const bool split = e.cfg.builder == FWN_BUILDER_SPLIT;
+        const bool split = e.cfg.builder != FWN_BUILDER_LBVH;  // top-down (midpoint or binned)
+        const bool binned = e.cfg.builder == FWN_BUILDER_BINNED;
         // node arrays: the LBVH's Karras tree has 2n - 1 nodes (internal 0..n-2, leaves after);
         // a split tree at most 2n - 1 as well, ids in creation order
         const int cap = split ? 2 * n : 2 * n - 1;
@@ -1935,6 +2186,11 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
             int* axis_of = (int*)track(dalloc<int>(smax, st));
             float* split_of = (float*)track(dalloc<float>(smax, st));
             int* spatial_of = (int*)track(dalloc<int>(smax, st));
+            int* bin_of = (int*)track(dalloc<int>(smax, st));
+            float* seg_box = (float*)track(dalloc<float>(6 * (size_t)smax, st));
+            // level-loop segments other than the roots hold more than kFinishSlots triangles each
+            const int seg_bound = std::max((int)s_start.size(), n / (kFinishSlots + 1) + 1);
+            unsigned* bins = (unsigned*)track(dalloc<unsigned>((size_t)seg_bound * kSegBinWords, st));
             int* d_mesh_seg = (int*)track(dalloc<int>(nmeshes, st));
             int* d_root_node = (int*)track(dalloc<int>(nmeshes, st));
             FWN_CUDA_CHECK(cudaMemcpyAsync(d_mesh_seg, mesh_seg.data(), nmeshes * sizeof(int),
@@ -1972,11 +2228,21 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
                 if (level > kSpatialLevels + 64)  // position splits halve every segment
                     throw Error(FWN_INTERNAL, "split build did not converge");
                 if (node_base + 2 * nact > cap) throw Error(FWN_INTERNAL, "split build node overflow");
+                if (nact > seg_bound) throw Error(FWN_INTERNAL, "split build segment overflow");
                 k_split_decide<<<grid_for(nact, 128), 128, 0, st>>>(
-                    nact, level >= kSpatialLevels, box_a, axis_of, split_of, spatial_of);
+                    nact, level >= kSpatialLevels, box_a, axis_of, split_of, spatial_of, seg_box);
+                if (binned && level < kSpatialLevels) {  // the binned plane of each segment
+                    const int words = nact * kSegBinWords;
+                    k_split_bins_init<<<grid_for(words, 256), 256, 0, st>>>(words, bins);
+                    k_split_bins<<<(int)((n + kBinChunk - 1) / kBinChunk), 256, 0, st>>>(n, *cur, seg_box,
+                                                                                      bins);
+                    k_split_choose<<<grid_for(32 * nact, 128), 128, 0, st>>>(nact, seg_box, bins,
+                                                                             axis_of, bin_of,
+                                                                             spatial_of);
+                }
                 k_split_flags<<<grid_for(n + 1, 256), 256, 0, st>>>(n, *cur, seg_a[0], seg_a[1],
                                                                    axis_of, split_of, spatial_of,
-                                                                   lflags);
+                                                                   bin_of, seg_box, lflags);
                 exclusive_scan_i32(lflags, n + 1, scan_tmp, st);
                 const int h_counts[2] = {0, nsmall};
                 FWN_CUDA_CHECK(cudaMemcpyAsync(counts, h_counts, sizeof(h_counts),

@@ -234,7 +234,8 @@ class RefTree:
 
 class LbvhTree:
     """O3: CPU restatement of the device tree builds (builder 0: LBVH over Morton codes with a
-    Karras hierarchy; builder 1: top-down longest-axis midpoint splits) and of the plain FP64
+    Karras hierarchy; builder 1: top-down longest-axis midpoint splits; builder 2: the same with
+    binned least-cost planes above 1024 triangles) and of the plain FP64
     traversal."""
 
     def __init__(self, V, F, leaf_size: int = 8, near_scale: float = 1e-3, voff=None, foff=None,

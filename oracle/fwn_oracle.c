@@ -588,7 +588,7 @@ static void lb_combine(const lb_stage* a, const lb_stage* b, lb_stage* R) {
 
 /* Builds the forest; voff/foff are [nmeshes+1] prefix offsets, triangle indices local per mesh.
  * Returns NULL on invalid input (bad index / non-finite referenced vertex). */
-/* Top-down splitting build (builder 1), restating the device's level-synchronous build: a node
+/* Top-down splitting builds (builders 1 and 2), restating the device's level-synchronous build: a node
  * of m > K triangles splits its centroids' bounding box at the midpoint of its longest axis
  * (ties: the lowest axis), split = (lo + hi) * 0.5f, left = centroids below the split, both sides
  * keeping their order (a stable partition); when every centroid coincides, or the midpoint rounds
@@ -596,12 +596,35 @@ static void lb_combine(const lb_stage* a, const lb_stage* b, lb_stage* R) {
  * >= SP_SPATIAL_LEVELS does. Nodes are created here in DFS pre-order, which is the order the
  * device reaches with its position formula. */
 #define SP_SPATIAL_LEVELS 96
+/* Builder 2 (binned): nodes of more than SP_FINISH_SLOTS triangles (the device's level loop;
+ * smaller ones are finished per block in shared memory) split at a binned plane instead: SP_BINS bins per axis over
+ * the centroid box, bin(x) = min((int)((x - lo) / ext * 16), 15) in float, and the plane with the
+ * least nL * dL + nR * dR, d = the squared diagonal of a side's centroid bounds (in double from
+ * the float bounds); ties go to the lower axis, then the lower plane; left = bin <= plane. */
+#define SP_FINISH_SLOTS 1024
+#define SP_BINS 16
+
+static int sp_bin(float x, float lo, float ext) {
+    const int b = (int)((x - lo) / ext * (float)SP_BINS);
+    return b < 0 ? 0 : (b > SP_BINS - 1 ? SP_BINS - 1 : b);
+}
+
+static double sp_diag2(const float* lo, const float* hi) {
+    double t = 0.0;
+    for (int a = 0; a < 3; ++a) {
+        const double d = (double)hi[a] - (double)lo[a];
+        t = t + d * d;
+    }
+    return t;
+}
+
 typedef struct {
     lb_tree* T;
     const float* cen;   /* [nf*3] centroids, input triangle order */
     int32_t* perm;      /* triangle ids, partitioned in place */
     int32_t* tmp;
     int K;
+    int binned;         /* builder 2: binned planes above SP_FINISH_SLOTS triangles */
     int64_t E;          /* nodes created so far */
     int32_t* nfirst;    /* per node (DFS position): slot range and children */
     int32_t* nlast;
@@ -633,7 +656,73 @@ static int32_t sp_build_rec(sp_ctx* c, int64_t b, int64_t e, int depth) {
     const float split = (lo[axis] + hi[axis]) * 0.5f;
     const int spatial = depth < SP_SPATIAL_LEVELS && ext > 0.f && split > lo[axis];
     int64_t nl = 0;
-    if (spatial) {
+    int bin_axis = -1, bin_plane = -1;
+    if (c->binned && m > SP_FINISH_SLOTS && depth < SP_SPATIAL_LEVELS) {
+        int64_t cnt[3][SP_BINS];
+        float blo[3][SP_BINS][3], bhi[3][SP_BINS][3];
+        for (int a = 0; a < 3; ++a)
+            for (int k = 0; k < SP_BINS; ++k) {
+                cnt[a][k] = 0;
+                for (int d = 0; d < 3; ++d) {
+                    blo[a][k][d] = INFINITY;
+                    bhi[a][k][d] = -INFINITY;
+                }
+            }
+        for (int64_t i = b; i < e; ++i) {
+            const float* x = c->cen + 3 * (int64_t)c->perm[i];
+            for (int a = 0; a < 3; ++a) {
+                const float ea = hi[a] - lo[a];
+                if (!(ea > 0.f)) continue;
+                const int k = sp_bin(x[a], lo[a], ea);
+                ++cnt[a][k];
+                for (int d = 0; d < 3; ++d) {
+                    blo[a][k][d] = fminf(blo[a][k][d], x[d]);
+                    bhi[a][k][d] = fmaxf(bhi[a][k][d], x[d]);
+                }
+            }
+        }
+        double best = INFINITY;
+        for (int a = 0; a < 3; ++a) {
+            if (!(hi[a] - lo[a] > 0.f)) continue;
+            for (int j = 0; j < SP_BINS - 1; ++j) {
+                int64_t nL = 0, nR = 0;
+                float Llo[3] = {INFINITY, INFINITY, INFINITY}, Lhi[3] = {-INFINITY, -INFINITY, -INFINITY};
+                float Rlo[3] = {INFINITY, INFINITY, INFINITY}, Rhi[3] = {-INFINITY, -INFINITY, -INFINITY};
+                for (int k = 0; k < SP_BINS; ++k) {
+                    if (k <= j) {
+                        nL += cnt[a][k];
+                        for (int d = 0; d < 3; ++d) {
+                            Llo[d] = fminf(Llo[d], blo[a][k][d]);
+                            Lhi[d] = fmaxf(Lhi[d], bhi[a][k][d]);
+                        }
+                    } else {
+                        nR += cnt[a][k];
+                        for (int d = 0; d < 3; ++d) {
+                            Rlo[d] = fminf(Rlo[d], blo[a][k][d]);
+                            Rhi[d] = fmaxf(Rhi[d], bhi[a][k][d]);
+                        }
+                    }
+                }
+                if (nL == 0 || nR == 0) continue;
+                const double cost = (double)nL * sp_diag2(Llo, Lhi) + (double)nR * sp_diag2(Rlo, Rhi);
+                if (cost < best) {
+                    best = cost;
+                    bin_axis = a;
+                    bin_plane = j;
+                }
+            }
+        }
+    }
+    if (bin_axis >= 0) {
+        const float la = lo[bin_axis], ea = hi[bin_axis] - lo[bin_axis];
+        int64_t k = b;
+        for (int64_t i = b; i < e; ++i)
+            if (sp_bin(c->cen[3 * (int64_t)c->perm[i] + bin_axis], la, ea) <= bin_plane) c->tmp[k++] = c->perm[i];
+        nl = k - b;
+        for (int64_t i = b; i < e; ++i)
+            if (!(sp_bin(c->cen[3 * (int64_t)c->perm[i] + bin_axis], la, ea) <= bin_plane)) c->tmp[k++] = c->perm[i];
+        memcpy(c->perm + b, c->tmp + b, (size_t)m * sizeof(int32_t));
+    } else if (spatial) {
         int64_t k = b;
         for (int64_t i = b; i < e; ++i)  /* stable partition: left run, then right run */
             if (c->cen[3 * (int64_t)c->perm[i] + axis] < split) c->tmp[k++] = c->perm[i];
@@ -652,13 +741,15 @@ static int32_t sp_build_rec(sp_ctx* c, int64_t b, int64_t e, int depth) {
 /* Builder 1 after validation: per-mesh trees side by side (no node spans two meshes), then the
  * same refit and exact radii as the LBVH. */
 static void lb_split_finish(lb_tree* T, const float* V, const int64_t* voff, const int32_t* F,
-                            const int64_t* foff, int64_t nmeshes, int K, const float* cen) {
+                            const int64_t* foff, int64_t nmeshes, int K, const float* cen,
+                            int binned) {
     const int64_t n = T->nf;
     sp_ctx c;
     memset(&c, 0, sizeof(c));
     c.T = T;
     c.cen = cen;
     c.K = K;
+    c.binned = binned;
     c.perm = (int32_t*)malloc(n * sizeof(int32_t));
     c.tmp = (int32_t*)malloc(n * sizeof(int32_t));
     const int64_t cap = 2 * n;
@@ -786,9 +877,9 @@ void* oracle_lbvh_build(const float* V, const int64_t* voff, const int32_t* F, c
             kv[t].idx = (uint32_t)t;
         }
     }
-    if (builder == 1) {
+    if (builder == 1 || builder == 2) {
         free(kv);
-        lb_split_finish(T, V, voff, F, foff, nmeshes, K, cen);
+        lb_split_finish(T, V, voff, F, foff, nmeshes, K, cen, builder == 2);
         free(cen);
         free(inv);
         return T;

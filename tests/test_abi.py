@@ -57,7 +57,7 @@ def test_invalid_arguments_rejected_on_host(engine_lib):
                              ("block_size", 48, "block_size"), ("precision", 7, "precision"),
                              ("fp64_near_scale", -1.0, "fp64_near_scale"), ("tuning", 8, "tuning"),
                              ("tuning", -1, "tuning"), ("fp64_cond", -1.0, "fp64_cond"),
-                             ("builder", 2, "builder")):
+                             ("builder", 3, "builder")):
         cfg = fwn.config_default(**{field: val})
         st, msg, _ = _build_status(V.ctypes.data_as(C.c_void_p), 3, None, 0, cfg)
         assert st == 1 and frag in msg, (field, msg)

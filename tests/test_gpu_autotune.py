@@ -19,8 +19,8 @@ def test_autotune_choice_and_cache(tmp_path):
     wl = W.displaced_icosphere_workload(nu=60, n_queries=60_000)
     cache = tmp_path / "tune.txt"
     r = fwn.autotune(wl.V, wl.F, wl.Q, cache_path=str(cache))
-    assert r["from_cache"] == 0 and r["candidates"] == 72 and r["ms"] > 0  # 2 builders x 4 x 9
-    assert r["leaf_size"] in (4, 8, 12, 16) and r["builder"] in (0, 1)
+    assert r["from_cache"] == 0 and r["candidates"] == 108 and r["ms"] > 0  # 3 builders x 4 x 9
+    assert r["leaf_size"] in (4, 8, 12, 16) and r["builder"] in (0, 1, 2)
     assert r["traversal"] in (fwn.TRAVERSAL_THREAD, fwn.TRAVERSAL_WARP)
     assert r["block_size"] % 32 == 0
     # the cached answer comes back without timing
@@ -32,7 +32,7 @@ def test_autotune_choice_and_cache(tmp_path):
     key = cache.read_text().split()[0]
     cache.write_text(f"{key} 99 2 128 17 0 1.0\n")
     r3 = fwn.autotune(wl.V, wl.F, wl.Q, cache_path=str(cache))
-    assert r3["from_cache"] == 0 and r3["candidates"] == 72 and r3["leaf_size"] in (4, 8, 12, 16)
+    assert r3["from_cache"] == 0 and r3["candidates"] == 108 and r3["leaf_size"] in (4, 8, 12, 16)
     # the tuned engine agrees with the plain FP64 form built with the same leaf size
     eng = fwn.FastWindingNumber(wl.V, wl.F, records=fwn.RECORDS_F32 | fwn.RECORDS_F64,
                                 **r["config"])

@@ -46,7 +46,7 @@ def _engine(V, F, **kw):
 
 
 @pytest.mark.parametrize("leaf,builder", [(1, 0), (4, 0), (7, 0), (16, 0), (1, 1), (4, 1),
-                                          (12, 1), (16, 1)])
+                                          (12, 1), (16, 1), (1, 2), (8, 2), (16, 2)])
 def test_build_matches_cpu_restatement(torch_cuda, oracle_mod, leaf, builder):
     """Both builders (0: LBVH over Morton codes, 1: top-down longest-axis splits) against their
     CPU restatements: topology, skip links, leaf ranges, triangle order, centres and radii bit for
@@ -277,7 +277,7 @@ def test_concurrent_queries_one_handle(torch_cuda):
         np.testing.assert_array_equal(o, ref)
 
 
-@pytest.mark.parametrize("builder", [0, 1])
+@pytest.mark.parametrize("builder", [0, 1, 2])
 def test_forest_matches_cpu_restatement(torch_cuda, oracle_mod, builder):
     fo = W.batched_forest_workload(n_meshes=9, seed=11, f_lo=100, f_hi=20000, q_lo=50, q_hi=3000)
     # add an empty mesh in the middle
@@ -550,9 +550,9 @@ def test_split_builder_degenerate_geometry(torch_cuda, oracle_mod):
             assert got["tri_count"].max() <= leaf
 
 
-@pytest.mark.parametrize("leaf", [1, 8, 16])
-def test_split_builder_finisher_boundaries(torch_cuda, oracle_mod, leaf):
-    """The top-down builder hands every segment of at most 1024 triangles to a per-block
+@pytest.mark.parametrize("leaf,builder", [(1, 1), (8, 1), (16, 1), (1, 2), (8, 2)])
+def test_split_builder_finisher_boundaries(torch_cuda, oracle_mod, leaf, builder):
+    """The top-down builders hand every segment of at most 1024 triangles to a per-block
     finisher in shared memory. Meshes on either side of that size (1024 / 1025, 2048 / 2049
     triangles, scattered random triangles), a mesh of 1024 and one of 3000 copies of a single
     triangle (every split by position, inside the finisher and before it) and small meshes, in
@@ -570,15 +570,15 @@ def test_split_builder_finisher_boundaries(torch_cuda, oracle_mod, leaf):
     V = np.concatenate([v for v, _ in meshes])
     F = np.concatenate([f for _, f in meshes])
     keys = ("skip", "tri_begin", "tri_count", "sorted_tri", "mesh_root")
-    forest = fwn.Forest(V, voff, F, foff, records=BOTH, leaf_size=leaf, builder=1)
+    forest = fwn.Forest(V, voff, F, foff, records=BOTH, leaf_size=leaf, builder=builder)
     got = forest.export_tree()
-    ref = oracle_mod.LbvhTree(V, F, leaf_size=leaf, voff=voff, foff=foff, builder=1).export()
+    ref = oracle_mod.LbvhTree(V, F, leaf_size=leaf, voff=voff, foff=foff, builder=builder).export()
     for k in keys:
         np.testing.assert_array_equal(got[k], ref[k], err_msg=k)
     np.testing.assert_array_equal(got["center_radius"], ref["center_radius"])
     for Vm, Fm in meshes[:2] + meshes[-2:]:
-        got = _engine(Vm, Fm, leaf_size=leaf, builder=1).export_tree()
-        ref = oracle_mod.LbvhTree(Vm, Fm, leaf_size=leaf, builder=1).export()
+        got = _engine(Vm, Fm, leaf_size=leaf, builder=builder).export_tree()
+        ref = oracle_mod.LbvhTree(Vm, Fm, leaf_size=leaf, builder=builder).export()
         for k in keys:
             np.testing.assert_array_equal(got[k], ref[k], err_msg=k)
         np.testing.assert_array_equal(got["center_radius"], ref["center_radius"])
