@@ -81,7 +81,8 @@ CPU_LEAF = 8  # leaf size of the CPU restatement of the reference tree, in every
 # the same bench command lines; other configurations: not captured (traffic null)
 NCU_TRAFFIC = {("displaced_icosphere_nu316_q10000000", 12, 4, 0): 952.36e6 + 57.72e6,
                ("displaced_icosphere_nu316_q10000000", 8, 4, 1): 973.63e6 + 52.19e6,
-               ("displaced_icosphere_nu316_q10000000", 8, 6, 1): 976.28e6 + 53.64e6}
+               ("displaced_icosphere_nu316_q10000000", 8, 6, 1): 976.28e6 + 53.64e6,
+               ("displaced_icosphere_nu316_q10000000", 8, 4, 2): 972.76e6 + 52.60e6}
 
 
 def parse():
