@@ -82,7 +82,8 @@ CPU_LEAF = 8  # leaf size of the CPU restatement of the reference tree, in every
 NCU_TRAFFIC = {("displaced_icosphere_nu316_q10000000", 12, 4, 0): 952.36e6 + 57.72e6,
                ("displaced_icosphere_nu316_q10000000", 8, 4, 1): 973.63e6 + 52.19e6,
                ("displaced_icosphere_nu316_q10000000", 8, 6, 1): 976.28e6 + 53.64e6,
-               ("displaced_icosphere_nu316_q10000000", 8, 4, 2): 972.76e6 + 52.60e6}
+               ("displaced_icosphere_nu316_q10000000", 8, 4, 2): 972.76e6 + 52.60e6,
+               ("displaced_icosphere_nu316_q10000000", 8, 6, 2): 973.71e6 + 52.88e6}
 
 
 def parse():
