@@ -585,7 +585,7 @@ def test_split_builder_finisher_boundaries(torch_cuda, oracle_mod, leaf, builder
         assert got["tri_count"].max() <= leaf
 
 
-@pytest.mark.parametrize("builder", [0, 1])
+@pytest.mark.parametrize("builder", [0, 1, 2])
 def test_save_load_round_trip(torch_cuda, tmp_path, builder):
     """An engine written with fwn_save and read back with fwn_load has the same tree and answers
     every query with the same bits (mixed and FP64 forms); a forest with an empty mesh too. A
@@ -622,7 +622,7 @@ def test_save_load_round_trip(torch_cuda, tmp_path, builder):
     assert torch_cuda.equal(w1, w2) and torch_cuda.equal(i1, i2)
 
 
-@pytest.mark.parametrize("builder", [0, 1])
+@pytest.mark.parametrize("builder", [0, 1, 2])
 def test_fp32_records_round_fp64_records(torch_cuda, builder):
     """Every coefficient of an FP32 node record is its FP64 record's value rounded to nearest
     even (the build converts on the integer pipes; numpy's cast is the IEEE reference), and the
