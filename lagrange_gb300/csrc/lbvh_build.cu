@@ -588,7 +588,8 @@ __global__ void k_split_bins_init(int nwords, unsigned* __restrict__ bins) {
 // shared memory, then adds the non-empty ones to the segments' global bins.
 __global__ void __launch_bounds__(256) k_split_bins(int64_t n, SplitSlots cur,
                                                     const float* __restrict__ seg_box,
-                                                    unsigned* __restrict__ bins) {
+                                                    unsigned* __restrict__ bins,
+                                                    unsigned* __restrict__ status) {
     constexpr int kLocal = 4;
     __shared__ int tab[kLocal];
     __shared__ int ntab;
@@ -610,6 +611,7 @@ __global__ void __launch_bounds__(256) k_split_bins(int64_t n, SplitSlots cur,
         if (sg >= 0 && (i == c0 || cur.seg[i - 1] != sg)) {
             const int k = atomicAdd(&ntab, 1);
             if (k < kLocal) tab[k] = sg;
+            else atomicOr(status, ST_BUILD_BOUND);  // cannot happen: segments hold > 1024 slots
         }
     }
     __syncthreads();
@@ -2234,8 +2236,8 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
                 if (binned && level < kSpatialLevels) {  // the binned plane of each segment
                     const int words = nact * kSegBinWords;
                     k_split_bins_init<<<grid_for(words, 256), 256, 0, st>>>(words, bins);
-                    k_split_bins<<<(int)((n + kBinChunk - 1) / kBinChunk), 256, 0, st>>>(n, *cur, seg_box,
-                                                                                      bins);
+                    k_split_bins<<<(int)((n + kBinChunk - 1) / kBinChunk), 256, 0, st>>>(
+                        n, *cur, seg_box, bins, status);
                     k_split_choose<<<grid_for(32 * nact, 128), 128, 0, st>>>(nact, seg_box, bins,
                                                                              axis_of, bin_of,
                                                                              spatial_of);
@@ -2412,6 +2414,7 @@ void build_forest(Engine& e, const float* d_V, const int64_t* voff_h, const int3
         FWN_CUDA_CHECK(cudaStreamSynchronize(st));
         e.num_leaves = lc;
         if (st_h & ST_REFIT_ORPHAN) throw Error(FWN_INTERNAL, "refit found an inconsistent tree");
+        if (st_h & ST_BUILD_BOUND) throw Error(FWN_INTERNAL, "split build passed its node or depth bound");
     }
     FWN_CUDA_CHECK(cudaEventRecord(ev1, st));
     FWN_CUDA_CHECK(cudaMemcpyAsync(e.meshes_h, e.meshes, nmeshes * sizeof(MeshInfo),
