@@ -243,3 +243,31 @@ def test_reference_engine_when_present(oracle_mod):
     assert np.max(np.abs(om / (4 * np.pi) - exact)) <= 1e-2
     band = np.abs(exact - 0.5) > 1e-3
     np.testing.assert_array_equal(ins[band].astype(bool), exact[band] > 0.5)
+
+
+@pytest.mark.parametrize("leaf", [1, 8])
+def test_split_builders_tree_invariants(oracle_mod, leaf):
+    """The restated top-down builds (1: midpoints; 2: least-cost binned planes above 1024
+    triangles): every triangle in exactly one leaf, leaves of at most leaf_size triangles,
+    pre-order skip links (a node's subtree is the run of positions up to its skip), each internal
+    node's range the union of its children's, and the binned rule changing the tree of a mesh
+    large enough to use it."""
+    wl = W.displaced_icosphere_workload(nu=40, n_queries=400)  # 32,000 triangles
+    trees = {}
+    for builder in (1, 2):
+        ex = oracle_mod.LbvhTree(wl.V, wl.F, leaf_size=leaf, builder=builder).export()
+        skip, tb, tc = ex["skip"], ex["tri_begin"], ex["tri_count"]
+        E = len(skip)
+        assert np.array_equal(np.sort(ex["sorted_tri"]), np.arange(len(wl.F)))
+        leaves = tc > 0
+        assert tc.max() <= leaf and tc[leaves].sum() == len(wl.F)
+        # leaves tile the slots in order
+        starts = tb[leaves]
+        assert np.array_equal(starts, np.concatenate([[0], np.cumsum(tc[leaves])[:-1]]))
+        assert np.all(skip[:-1] > np.arange(E - 1)) and skip[0] == E
+        internal = np.flatnonzero(~leaves)
+        assert np.all(skip[internal + 1] < skip[internal])  # the left child ends before its parent
+        right = skip[internal + 1]
+        assert np.all(skip[right] == skip[internal])          # the right child ends with it
+        trees[builder] = ex
+    assert not np.array_equal(trees[1]["sorted_tri"], trees[2]["sorted_tri"])
